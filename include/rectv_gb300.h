@@ -1,0 +1,156 @@
+/*
+ * rectv_gb300 -- C ABI of the GB300 (sm_103a) implementation of rectv_gpu's
+ * 4D time-resolved tomographic reconstruction (USFFT Radon + temporal basis +
+ * 4D total variation, linearised ADMM).
+ *
+ * Every entry point returns 0 on success and a nonzero RECTV_ERR_* code on
+ * failure; rectv_last_error() then returns a message for the calling thread.
+ * Pointers are plain addresses; sizes are element counts.  No entry point
+ * resets the device.
+ *
+ * Reference interface replaced (nikitinvv/rectv_gpu):
+ *   class rectv, SWIG interface src/cuda/rectv.i:9-28, declared in
+ *   src/include/rectv.cuh:7-55, implemented in src/cuda/rectv.cu.
+ */
+#ifndef RECTV_GB300_H
+#define RECTV_GB300_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct rectv_handle rectv_handle;
+
+enum {
+    RECTV_OK = 0,
+    RECTV_ERR_ARG = 1,     /* invalid argument or shape */
+    RECTV_ERR_CUDA = 2,    /* CUDA runtime error */
+    RECTV_ERR_CUFFT = 3,   /* cuFFT error */
+    RECTV_ERR_STATE = 4,   /* handle freed / call order */
+    RECTV_ERR_NOMEM = 5    /* device memory exhausted */
+};
+
+/* Message of the last failing call on this thread ("" if none). */
+const char *rectv_last_error(void);
+
+/* Library version string. */
+const char *rectv_version(void);
+
+/* ---------------------------------------------------------------------------
+ * Reference-compatible object API
+ * ------------------------------------------------------------------------- */
+
+/* Replaces rectv::rectv(int n, int ntheta, int m, int nz, int nzp, int ngpus)
+ * (src/cuda/rectv.cu:5-59; rectv.i:21).  ngpus is clamped to
+ * min(ngpus, nz/nzp) as in rectv.cu:9; all work runs on the current CUDA
+ * device.  Device memory is allocated here, as in the reference. */
+int rectv_create(int n, int ntheta, int m, int nz, int nzp, int ngpus, rectv_handle **out);
+
+/* Read-only attributes n, ntheta, m, nz of the SWIG class (rectv.i:14-18),
+ * plus nzp and the effective ngpus.  Any output pointer may be NULL. */
+int rectv_get_dims(const rectv_handle *h, int *n, int *ntheta, int *m, int *nz, int *nzp,
+                   int *ngpus);
+
+/* Replaces rectv::run(size_t fres, size_t g, size_t theta, size_t phi, float center,
+ * float lambda0, float lambda1, int niter, int titer) (src/cuda/rectv.cu:102-252;
+ * rectv.i:23-25).  Host pointers, C-contiguous float32:
+ *   fres  [nz][m][n][n]   output (written)
+ *   g     [nz][ntheta][n] projection data
+ *   theta [ntheta]        angles in radians
+ *   phi   [m][2*ntheta]   complex temporal basis, interleaved (re, im)
+ * lambda0 is used as given (the Python Solver multiplies it by lambda1 first,
+ * src/rectv_gpu/solver.py:76).  Starts from zero, as the reference does.
+ * Prints "iter (k/niter), rdiff ||f(k+1)-f(k)||:..." to stderr per outer
+ * iteration like rectv.cu:238 unless rectv_set_verbose(h, 0). */
+int rectv_run(rectv_handle *h, float *fres, const float *g, const float *theta, const float *phi,
+              float center, float lambda0, float lambda1, int niter, int titer);
+
+/* Replaces rectv::check_adjoints(size_t res, size_t g, size_t theta, size_t phi,
+ * float lambda1, float center) (src/cuda/rectv.cu:255-290; rectv.i:26).
+ * Requires nz == nzp (the reference reads nz+1 gradient planes from a buffer
+ * of nzp+1 planes).  res is a host float64 [6] ACCUMULATED into (+=), exactly
+ * as in the reference:
+ *   res[0] = <R*g, R*g>, res[1] = <g, R R*g>, res[2] = <R R*g, R R*g>,
+ *   res[3] = <f, D G f>, res[4] = sum of squares of the first
+ *   (n+1)^2 (m+1)(nz+1) floats of the float4 gradient array (rectv.cu:287),
+ *   res[5] = <D G f, D G f>,  with f = R* g. */
+int rectv_check_adjoints(rectv_handle *h, double *res, const float *g, const float *theta,
+                         const float *phi, float lambda1, float center);
+
+/* Replaces rectv::free() (src/cuda/rectv.cu:63-91; rectv.i:27).  Releases all
+ * device memory; idempotent; does NOT call cudaDeviceReset.  After it, only
+ * rectv_get_dims and rectv_destroy are valid. */
+int rectv_free(rectv_handle *h);
+
+/* Replaces rectv::~rectv (src/cuda/rectv.cu:61): frees and deletes the handle. */
+void rectv_destroy(rectv_handle *h);
+
+/* Per-iteration log to stderr on (1, default) or off (0). */
+int rectv_set_verbose(rectv_handle *h, int verbose);
+
+/* ---------------------------------------------------------------------------
+ * Device-resident session API (splits rectv::run, src/cuda/rectv.cu:102-252)
+ * All pointers are device pointers; work is queued on the handle's stream.
+ * ------------------------------------------------------------------------- */
+
+/* Copies data/angles/basis, builds the angle plan, zeroes f, psi, mu and sets
+ * rho = 0.5 (rectv.cu:107-125). */
+int rectv_setup_device(rectv_handle *h, const float *d_g, const float *d_theta,
+                       const float *d_phi, float center, float lambda0, float lambda1, int titer);
+
+/* Runs niter outer ADMM iterations (rectv.cu:140-246) asynchronously. */
+int rectv_iterate(rectv_handle *h, int niter);
+
+/* Copies the current iterate f [nz][m][n][n] to d_f (device pointer). */
+int rectv_get_result_device(rectv_handle *h, float *d_f);
+
+/* The CUDA stream (cudaStream_t) all work of this handle is queued on. */
+int rectv_get_stream(rectv_handle *h, void **stream);
+
+/* Waits for the handle's stream. */
+int rectv_synchronize(rectv_handle *h);
+
+/* Per-outer-iteration statistics of the last run/iterate calls, host arrays of
+ * length >= *count on input; *count receives the number of iterations recorded.
+ * rdiff = ||f(k+1)-f(k)||^2 (rectv.cu:235-238), rho after the update, and the
+ * squared primal/dual residual sums r and s of the rho rule (rectv.cu:223-232). */
+int rectv_get_history(rectv_handle *h, double *rdiff, double *rho, double *r, double *s,
+                      int *count);
+
+/* Use (1, default) or bypass (0) CUDA-graph replay of the outer iteration. */
+int rectv_set_graphs(rectv_handle *h, int enable);
+
+/* ---------------------------------------------------------------------------
+ * Operator-level entry points (device pointers), the reference's private
+ * operators exposed for parity testing.  rectv_op_set_geometry must be called
+ * first; it uploads theta/phi and the rotation centre.
+ * ------------------------------------------------------------------------- */
+
+/* d_theta [ntheta], d_phi [m][2*ntheta] device pointers; center as in run. */
+int rectv_op_set_geometry(rectv_handle *h, const float *d_theta, const float *d_phi, float center);
+
+/* rectv::radonapr (src/cuda/operators.cu:6-32): d_g = tau * R_apr d_f.
+ * d_f [nslices][m][n][n], d_g [nslices][ntheta][n]; nslices <= nz. */
+int rectv_op_radonapr(rectv_handle *h, float *d_g, const float *d_f, int nslices, float tau);
+
+/* rectv::radonapradj (src/cuda/operators.cu:34-58): d_f += tau * R_apr^T d_g. */
+int rectv_op_radonapradj(rectv_handle *h, float *d_f, const float *d_g, int nslices, float tau);
+
+/* rectv::gradient (src/cuda/operators.cu:60-66) on one chunk:
+ * d_fm [nzp+2][m][n][n] (slab 0 and nzp+1 are the z-halo), flgl/flgr say
+ * whether the halo slabs are used (extendf, kernels_operators.cuh:4-20);
+ * d_h2 [nzp+1][m+1][n+1][n+1][4] float (float4 layout of the reference). */
+int rectv_op_gradient(rectv_handle *h, float *d_h2, const float *d_fm, float lambda1, int flgl,
+                      int flgr);
+
+/* rectv::divergent (src/cuda/operators.cu:68-71): d_fn [nzp][m][n][n] +=
+ * tau * div(d_h2) (kernels_operators.cuh:46-73). */
+int rectv_op_divergent(rectv_handle *h, float *d_fn, const float *d_h2, float lambda1, float tau);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* RECTV_GB300_H */

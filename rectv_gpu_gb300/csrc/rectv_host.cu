@@ -1,0 +1,900 @@
+// Host driver and C ABI of librectv_gb300.
+//
+// Replaces class rectv of the reference (src/include/rectv.cuh:7-55,
+// src/cuda/rectv.cu:1-290) for one GPU.  Differences in mechanism, not in
+// results:
+//  * every buffer is device memory (no managed-memory streaming: the whole
+//    state of the largest configuration fits in HBM), allocated at creation;
+//  * chunks of nzp slices keep their own dual variables and z-halo semantics,
+//    but several chunks are processed per kernel launch ("batch" of zb slices);
+//  * an outer ADMM iteration is a fixed sequence of kernels and cuFFT calls
+//    on one stream, captured once as a CUDA graph per buffer rotation and
+//    replayed; rho lives on the device and is updated by a kernel, so the
+//    host only reads the per-iteration log values (with one iteration of lag).
+#include <cuda_runtime.h>
+#include <cufft.h>
+
+#include <algorithm>
+#include <cmath>
+#include <complex>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "rectv_gb300.h"
+#include "rectv_internal.cuh"
+
+namespace rectv {
+
+void cuda_check(cudaError_t e, const char *what, const char *file, int line) {
+    if (e == cudaSuccess) return;
+    const int code = (e == cudaErrorMemoryAllocation) ? RECTV_ERR_NOMEM : RECTV_ERR_CUDA;
+    throw Error(code, std::string(what) + ": " + cudaGetErrorString(e) + " (" + file + ":" +
+                          std::to_string(line) + ")");
+}
+
+void cufft_check(cufftResult e, const char *what, const char *file, int line) {
+    if (e == CUFFT_SUCCESS) return;
+    const int code = (e == CUFFT_ALLOC_FAILED) ? RECTV_ERR_NOMEM : RECTV_ERR_CUFFT;
+    throw Error(code, std::string(what) + ": cufft error " + std::to_string((int)e) + " (" + file + ":" +
+                          std::to_string(line) + ")");
+}
+
+namespace {
+
+thread_local std::string g_last_error;
+
+template <class T>
+T *dalloc(size_t count, std::vector<void *> &owned) {
+    void *p = nullptr;
+    if (count == 0) count = 1;
+    CUDA_CHECK(cudaMalloc(&p, count * sizeof(T)));
+    owned.push_back(p);
+    return static_cast<T *>(p);
+}
+
+int usfft_radius(int n, float *mu_out) {
+    // radonusfft.cu:10-11
+    const float eps = 1e-3f;
+    const float mu = (float)(-std::log((double)eps) / (2.0 * n * (double)n));
+    const double r = std::ceil(2.0 * n / kPiUsfft *
+                               std::sqrt(-(double)mu * std::log((double)eps) + ((double)mu * n) * ((double)mu * n) / 4.0));
+    *mu_out = mu;
+    return (int)r;
+}
+
+}  // namespace
+
+struct Handle {
+    // dimensions (rectv.cuh:43-47)
+    int n, ntheta, m, nz, nzp, ngpus, nchunks, nzc;
+    int device = 0;
+    bool freed = false;
+    bool verbose = true;
+    bool use_graphs = true;
+    cudaStream_t stream = nullptr;
+    std::vector<void *> owned;
+
+    UsGeo ug{};
+    TvGeo tv{};
+    float mu_us = 0.f;
+    int zb = 0;        // slices per batch (multiple of nzp, divides nzc)
+    int nbatch = 0;
+    long long slab = 0;  // n*n*m
+    long long gp = 0;    // dual points per chunk
+
+    // device buffers
+    float *U[3] = {nullptr, nullptr, nullptr};
+    float *gdata = nullptr;
+    float *psi = nullptr, *mu = nullptr;
+    float *h1 = nullptr;
+    float2 *spec = nullptr;
+    float2 *rows = nullptr;
+    double *partials = nullptr;
+    int nparts_batch = 0;
+    double *dot_part = nullptr;
+    double *dot_out = nullptr;
+    float *rho_d = nullptr;
+    int *iter_ctr = nullptr;
+    double *stats = nullptr;
+    int stats_cap = 0;
+    GeoDev gd;
+    std::vector<void *> geo_owned;
+
+    // cuFFT
+    cufftHandle p_r2c2d = 0, p_c2c2d = 0, p_rows_c2c = 0, p_rows_r2c = 0;
+    bool plans_made = false;
+    int img_per_fft = 0;
+    void *fft_work = nullptr;
+
+    // session
+    bool session = false;
+    int cur = 0;
+    float lambda0 = 0.f, lambda1 = 1.f;
+    int titer = 0;
+    int iters_done = 0;
+    std::vector<double> h_rdiff, h_rho, h_r, h_s;
+    double *stats_host = nullptr;  // pinned
+    cudaGraphExec_t graphs[3] = {nullptr, nullptr, nullptr};
+
+    Handle(int n_, int ntheta_, int m_, int nz_, int nzp_, int ngpus_) {
+        n = n_;
+        ntheta = ntheta_;
+        m = m_;
+        nz = nz_;
+        nzp = nzp_;
+        if (n < 2 || ntheta < 1 || m < 1 || nz < 1 || nzp < 1)
+            throw Error(RECTV_ERR_ARG, "rectv: n>=2, ntheta>=1, m>=1, nz>=1, nzp>=1 required");
+        if (nzp > nz) throw Error(RECTV_ERR_ARG, "rectv: nzp must not exceed nz");
+        if ((long long)n * ntheta >= (1LL << 32)) throw Error(RECTV_ERR_ARG, "rectv: n*ntheta too large");
+        nchunks = nz / nzp;
+        nzc = nchunks * nzp;
+        ngpus = std::max(1, std::min(ngpus_, nchunks));  // rectv.cu:9
+        CUDA_CHECK(cudaGetDevice(&device));
+        const int r = usfft_radius(n, &mu_us);
+        if (r != kR) throw Error(RECTV_ERR_ARG, "rectv: USFFT radius " + std::to_string(r) + " != 4");
+        try {
+            init();
+        } catch (...) {
+            release();
+            throw;
+        }
+    }
+
+    ~Handle() { release(); }
+
+    void init() {
+        CUDA_CHECK(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
+        usfft_prepare();
+        const int P = 2 * n;
+        ug.n = n;
+        ug.ntheta = ntheta;
+        ug.m = m;
+        ug.P = P;
+        ug.hp = P / 2 + 1;
+        ug.img_fwd = (long long)P * ug.hp;
+        ug.img_adj = (long long)P * P;
+        ug.tn = (float)(2 * n);
+        ug.inv2n = (float)(1.0 / (2.0 * n));
+        ug.wexp = (float)(kPiUsfft * kPiUsfft / (double)mu_us);
+        ug.cw = (float)(kPiUsfft / (double)mu_us / (double)n);
+        ug.T = 16;
+        ug.NT = (P + ug.T - 1) / ug.T;
+
+        slab = (long long)n * n * m;
+        gp = (long long)(n + 1) * (n + 1) * (m + 1) * (nzp + 1);
+
+        // batch size: largest zb = nzp*d, d | nchunks, with per-batch scratch under budget
+        double budget = 40.0 * (1ull << 30);
+        if (const char *e = std::getenv("RECTV_BATCH_BYTES")) budget = std::atof(e);
+        const double per_slice = (double)m * P * (double)P * 8.0 + (double)ntheta * n * 12.0;
+        int d = 1;
+        for (int cand = nchunks; cand >= 1; --cand) {
+            if (nchunks % cand) continue;
+            if (cand == 1 || per_slice * nzp * cand <= budget) {
+                d = cand;
+                break;
+            }
+        }
+        zb = nzp * d;
+        nbatch = nchunks / d;
+
+        for (int i = 0; i < 3; ++i) U[i] = dalloc<float>((size_t)nzc * slab, owned);
+        gdata = dalloc<float>((size_t)nz * ntheta * n, owned);
+        psi = dalloc<float>((size_t)4 * nchunks * gp, owned);
+        mu = dalloc<float>((size_t)4 * nchunks * gp, owned);
+        h1 = dalloc<float>((size_t)zb * ntheta * n, owned);
+        // spectra; also the float4 gradient scratch of check_adjoints
+        const size_t spec_elems =
+            std::max<size_t>((size_t)zb * m * (size_t)ug.img_adj, (size_t)2 * (n + 1) * (n + 1) * (m + 1) * (nzp + 1));
+        spec = dalloc<float2>(spec_elems, owned);
+        rows = dalloc<float2>((size_t)zb * ntheta * (size_t)std::max(n, n / 2 + 1), owned);
+
+        tv.n = n;
+        tv.m = m;
+        tv.nzp = nzp;
+        tv.nchunks = d;
+        tv.vol_slab = slab;
+        tv.gp = gp;
+        tv.comp_stride = (long long)nchunks * gp;
+        set_lambda1(1.0f);
+        nparts_batch = shrink_blocks(tv, d);
+        partials = dalloc<double>((size_t)3 * nparts_batch * nbatch, owned);
+        dot_part = dalloc<double>((size_t)dot_parts(), owned);
+        dot_out = dalloc<double>(8, owned);
+        rho_d = dalloc<float>(1, owned);
+        iter_ctr = dalloc<int>(1, owned);
+        gd.err = dalloc<int>(1, owned);
+        CUDA_CHECK(cudaMemsetAsync(gd.err, 0, sizeof(int), stream));
+        CUDA_CHECK(cudaMallocHost(&stats_host, sizeof(double) * 4));
+        make_fft_plans();
+        CUDA_CHECK(cudaStreamSynchronize(stream));
+    }
+
+    void set_lambda1(float l1) {
+        lambda1 = l1;
+        tv.lambda1 = l1;
+        // kernels_operators.cuh:40-43 and 69-72
+        tv.sg = (float)(1.0 / (2.0 * std::cbrt(2.0) * ((double)l1 / 2.0)));
+        tv.sd = (float)(1.0 / (4.0 * std::cbrt(2.0) * ((double)l1 / 2.0)));
+    }
+
+    void make_fft_plans() {
+        const int P = 2 * n;
+        const double img_bytes = (double)P * P * 8.0;
+        const int nimg = zb * m;
+        int per = nimg;
+        const double cap = 8.0 * (1ull << 30);
+        while (per > 1 && per * img_bytes > cap) {
+            int nx = per - 1;
+            while (nx > 1 && nimg % nx) --nx;
+            per = nx;
+        }
+        img_per_fft = per;
+        size_t ws = 0, w1 = 0;
+        CUFFT_CHECK(cufftCreate(&p_r2c2d));
+        CUFFT_CHECK(cufftCreate(&p_c2c2d));
+        CUFFT_CHECK(cufftCreate(&p_rows_c2c));
+        CUFFT_CHECK(cufftCreate(&p_rows_r2c));
+        plans_made = true;
+        for (cufftHandle h : {p_r2c2d, p_c2c2d, p_rows_c2c, p_rows_r2c}) CUFFT_CHECK(cufftSetAutoAllocation(h, 0));
+        {  // 2D R2C in place: real rows of P+2 floats -> P/2+1 complex
+            int nn[2] = {P, P};
+            int inem[2] = {P, P + 2};
+            int onem[2] = {P, P / 2 + 1};
+            CUFFT_CHECK(cufftMakePlanMany(p_r2c2d, 2, nn, inem, 1, P * (P + 2), onem, 1, P * (P / 2 + 1),
+                                          CUFFT_R2C, per, &w1));
+            ws = std::max(ws, w1);
+        }
+        {  // 2D C2C full plane
+            int nn[2] = {P, P};
+            CUFFT_CHECK(cufftMakePlanMany(p_c2c2d, 2, nn, nullptr, 1, P * P, nullptr, 1, P * P, CUFFT_C2C, per,
+                                          &w1));
+            ws = std::max(ws, w1);
+        }
+        const int nrows = zb * ntheta;
+        {  // rows C2C (forward operator's inverse transform)
+            int nn[1] = {n};
+            CUFFT_CHECK(cufftMakePlanMany(p_rows_c2c, 1, nn, nullptr, 1, n, nullptr, 1, n, CUFFT_C2C, nrows, &w1));
+            ws = std::max(ws, w1);
+        }
+        {  // rows R2C in place (adjoint): 2(n/2+1) floats -> n/2+1 complex
+            int nn[1] = {n};
+            int inem[1] = {2 * (n / 2 + 1)};
+            int onem[1] = {n / 2 + 1};
+            CUFFT_CHECK(cufftMakePlanMany(p_rows_r2c, 1, nn, inem, 1, 2 * (n / 2 + 1), onem, 1, n / 2 + 1,
+                                          CUFFT_R2C, nrows, &w1));
+            ws = std::max(ws, w1);
+        }
+        if (ws > 0) fft_work = dalloc<char>(ws, owned);
+        for (cufftHandle h : {p_r2c2d, p_c2c2d, p_rows_c2c, p_rows_r2c}) {
+            CUFFT_CHECK(cufftSetWorkArea(h, fft_work));
+            CUFFT_CHECK(cufftSetStream(h, stream));
+        }
+    }
+
+    void drop_graphs() {
+        for (auto &g : graphs)
+            if (g) {
+                cudaGraphExecDestroy(g);
+                g = nullptr;
+            }
+    }
+
+    void free_geo() {
+        for (void *p : geo_owned) cudaFree(p);
+        geo_owned.clear();
+        int *err = gd.err;
+        gd = GeoDev();
+        gd.err = err;
+    }
+
+    void release() {
+        if (stream) cudaStreamSynchronize(stream);
+        drop_graphs();
+        free_geo();
+        if (plans_made) {
+            cufftDestroy(p_r2c2d);
+            cufftDestroy(p_c2c2d);
+            cufftDestroy(p_rows_c2c);
+            cufftDestroy(p_rows_r2c);
+            plans_made = false;
+        }
+        for (void *p : owned) cudaFree(p);
+        owned.clear();
+        if (stats_host) cudaFreeHost(stats_host);
+        stats_host = nullptr;
+        if (stream) cudaStreamDestroy(stream);
+        stream = nullptr;
+        freed = true;
+        session = false;
+    }
+
+    void check_live() const {
+        if (freed) throw Error(RECTV_ERR_STATE, "rectv: object was freed");
+    }
+
+    // ---- geometry: angle plan, basis mixing matrix, centre shifts ----
+    void set_geometry(const float *theta_h, const float *phi_h, float center) {
+        drop_graphs();
+        free_geo();
+        HostPlan hp = build_plan(theta_h, n, ntheta, ug.T, 256, 256);
+        auto up = [&](const void *src, size_t bytes) -> void * {
+            void *p = nullptr;
+            CUDA_CHECK(cudaMalloc(&p, std::max<size_t>(bytes, 16)));
+            geo_owned.push_back(p);
+            if (bytes) CUDA_CHECK(cudaMemcpyAsync(p, src, bytes, cudaMemcpyHostToDevice, stream));
+            return p;
+        };
+        gd.sincos = (float2 *)up(hp.sincos.data(), hp.sincos.size() * sizeof(float2));
+        gd.fwd_pts = (uint32_t *)up(hp.fwd_pts.data(), hp.fwd_pts.size() * 4);
+        gd.fwd_items = (int4 *)up(hp.fwd_items.data(), hp.fwd_items.size() * sizeof(int4));
+        gd.n_fwd_items = (int)hp.fwd_items.size();
+        gd.adj_pts = (uint32_t *)up(hp.adj_pts.data(), hp.adj_pts.size() * 4);
+        gd.adj_items = (int4 *)up(hp.adj_items.data(), hp.adj_items.size() * sizeof(int4));
+        gd.n_adj_items = (int)hp.adj_items.size();
+        gd.split_tiles = (int *)up(hp.split_tiles.data(), hp.split_tiles.size() * 4);
+        gd.n_split_tiles = (int)hp.split_tiles.size();
+        if (gd.n_fwd_items > 2147483647 || gd.n_adj_items > 2147483647)
+            throw Error(RECTV_ERR_ARG, "rectv: plan too large");
+
+        // K'(theta, j) = ntheta/sqrt(m) sum_i phi_i(theta) conj(phi_i(t_j)),
+        // t_j = j*ntheta/m: decphi/mulphi/recphi (kernels_operators.cuh:99-149)
+        std::vector<float2> kmat((size_t)ntheta * m);
+        const double cphi = (double)ntheta / std::sqrt((double)m);
+        for (int th = 0; th < ntheta; ++th)
+            for (int j = 0; j < m; ++j) {
+                const int tj = (int)(((long long)j * ntheta) / m);
+                std::complex<double> acc(0.0, 0.0);
+                for (int i = 0; i < m; ++i) {
+                    const std::complex<double> a(phi_h[(size_t)i * 2 * ntheta + 2 * th],
+                                                 phi_h[(size_t)i * 2 * ntheta + 2 * th + 1]);
+                    const std::complex<double> b(phi_h[(size_t)i * 2 * ntheta + 2 * tj],
+                                                 phi_h[(size_t)i * 2 * ntheta + 2 * tj + 1]);
+                    acc += a * std::conj(b);
+                }
+                acc *= cphi;
+                kmat[(size_t)th * m + j] = make_float2((float)acc.real(), (float)acc.imag());
+            }
+        gd.kmat = (float2 *)up(kmat.data(), kmat.size() * sizeof(float2));
+        // set_center (radonusfft.cu:70-75, takeshift kernels_radonusfft.cuh:191-198)
+        std::vector<float2> sf(n), sa(n);
+        for (int k = 0; k < n; ++k) {
+            const double cf = -((double)center - n / 2.0), ca = (double)center - n / 2.0;
+            const double af = 2 * kPiUsfft * cf * (k - n / 2.0) / n;
+            const double aa = 2 * kPiUsfft * ca * (k - n / 2.0) / n;
+            sf[k] = make_float2((float)std::cos(af), (float)std::sin(af));
+            sa[k] = make_float2((float)std::cos(aa), (float)std::sin(aa));
+        }
+        gd.shiftfwd = (float2 *)up(sf.data(), n * sizeof(float2));
+        gd.shiftadj = (float2 *)up(sa.data(), n * sizeof(float2));
+        // 1/phi of divphi (kernels_radonusfft.cuh:11), separable
+        std::vector<float> dp(n);
+        for (int x = 0; x < n; ++x) {
+            const double d = (double)(x - n / 2);
+            dp[x] = (float)std::exp((double)mu_us * d * d);
+        }
+        gd.deapod = (float *)up(dp.data(), n * sizeof(float));
+        CUDA_CHECK(cudaStreamSynchronize(stream));  // host vectors go out of scope
+    }
+
+    // ---- operators on one batch of zb slices ----
+    // out = tau R_apr u  (residual: out = R_apr u - gb)
+    void forward(const float *u, const float *gb, float *out, float tau, int residual) {
+        launch_deapod_pad(u, reinterpret_cast<float *>(spec), zb * m, gd.deapod, ug, stream);
+        const int nimg = zb * m;
+        for (int i = 0; i < nimg; i += img_per_fft) {
+            cufftComplex *p = reinterpret_cast<cufftComplex *>(spec + (size_t)i * ug.img_fwd);
+            CUFFT_CHECK(cufftExecR2C(p_r2c2d, reinterpret_cast<cufftReal *>(p), p));
+        }
+        launch_gather_fwd(spec, rows, zb, gd, ug, stream);
+        CUFFT_CHECK(cufftExecC2C(p_rows_c2c, reinterpret_cast<cufftComplex *>(rows),
+                                 reinterpret_cast<cufftComplex *>(rows), CUFFT_INVERSE));
+        launch_finish_fwd(rows, gb, out, zb, tau, residual, ug, stream);
+    }
+
+    // u += tau R_apr^T h
+    void adjoint(const float *h, float *u, float tau) {
+        launch_adj_prep(h, reinterpret_cast<float *>(rows), zb, ug, stream);
+        CUFFT_CHECK(cufftExecR2C(p_rows_r2c, reinterpret_cast<cufftReal *>(rows),
+                                 reinterpret_cast<cufftComplex *>(rows)));
+        launch_zero_split(spec, zb, gd, ug, stream);
+        launch_scatter_adj(rows, spec, zb, gd, ug, stream);
+        const int nimg = zb * m;
+        for (int i = 0; i < nimg; i += img_per_fft) {
+            cufftComplex *p = reinterpret_cast<cufftComplex *>(spec + (size_t)i * ug.img_adj);
+            CUFFT_CHECK(cufftExecC2C(p_c2c2d, p, p, CUFFT_INVERSE));
+        }
+        launch_crop_accum(spec, u, zb, tau, gd.deapod, ug, stream);
+    }
+
+    // ---- one outer ADMM iteration (rectv.cu:140-245 for all chunks) ----
+    void enqueue_outer(int old) {
+        const int a = (old + 1) % 3, b = (old + 2) % 3;
+        int src = old;
+        const int dpb = zb / nzp;  // chunks per batch
+        for (int k = 0; k < titer; ++k) {
+            const int dst = (k % 2 == 0) ? a : b;
+            for (int bb = 0; bb < nbatch; ++bb) {
+                const long long z0 = (long long)bb * zb;
+                const int c0 = bb * dpb;
+                forward(U[src] + z0 * slab, gdata + z0 * ntheta * n, h1, 1.0f, 1);
+                launch_graddiv(U[src], U[old], U[dst], psi, mu, rho_d, c0, nchunks, tv, stream);
+                adjoint(h1, U[dst] + z0 * slab, -0.5f);
+            }
+            src = dst;
+        }
+        for (int bb = 0; bb < nbatch; ++bb) {
+            launch_shrink(U[src], U[old], psi, mu, rho_d, lambda0, bb * dpb, nchunks, tv,
+                          partials + (size_t)3 * nparts_batch * bb, stream);
+        }
+        launch_reduce_rho(partials, nparts_batch * nbatch, rho_d, stats, iter_ctr, stats_cap, stream);
+    }
+
+    int next_cur(int old) const {
+        if (titer == 0) return old;
+        return (titer % 2 == 1) ? (old + 1) % 3 : (old + 2) % 3;
+    }
+
+    void launch_outer() {
+        const int old = cur;
+        if (use_graphs) {
+            if (!graphs[old]) {
+                cudaGraph_t g = nullptr;
+                CUDA_CHECK(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
+                try {
+                    enqueue_outer(old);
+                } catch (...) {
+                    cudaStreamEndCapture(stream, &g);
+                    if (g) cudaGraphDestroy(g);
+                    throw;
+                }
+                CUDA_CHECK(cudaStreamEndCapture(stream, &g));
+                cudaGraphExec_t ge = nullptr;
+                cudaError_t e = cudaGraphInstantiate(&ge, g, 0);
+                cudaGraphDestroy(g);
+                CUDA_CHECK(e);
+                graphs[old] = ge;
+            }
+            CUDA_CHECK(cudaGraphLaunch(graphs[old], stream));
+        } else {
+            enqueue_outer(old);
+        }
+        cur = next_cur(old);
+    }
+
+    void setup(const float *theta_h, const float *phi_h, float center, float lambda0_, float lambda1_,
+               int titer_) {
+        check_live();
+        if (titer_ < 0) throw Error(RECTV_ERR_ARG, "rectv: titer must be >= 0");
+        set_geometry(theta_h, phi_h, center);
+        lambda0 = lambda0_;
+        set_lambda1(lambda1_);
+        titer = titer_;
+        drop_graphs();
+        // initial guess and ADMM state (rectv.cu:119-125)
+        cur = 0;
+        CUDA_CHECK(cudaMemsetAsync(U[0], 0, sizeof(float) * (size_t)nzc * slab, stream));
+        CUDA_CHECK(cudaMemsetAsync(psi, 0, sizeof(float) * (size_t)4 * nchunks * gp, stream));
+        CUDA_CHECK(cudaMemsetAsync(mu, 0, sizeof(float) * (size_t)4 * nchunks * gp, stream));
+        const float rho0 = 0.5f;
+        CUDA_CHECK(cudaMemcpyAsync(rho_d, &rho0, sizeof(float), cudaMemcpyHostToDevice, stream));
+        CUDA_CHECK(cudaStreamSynchronize(stream));
+        iters_done = 0;
+        h_rdiff.clear();
+        h_rho.clear();
+        h_r.clear();
+        h_s.clear();
+        session = true;
+    }
+
+    void ensure_stats(int cap) {
+        if (cap <= stats_cap) return;
+        drop_graphs();  // graphs hold the stats pointer
+        if (stats) {
+            cudaFree(stats);
+            owned.erase(std::find(owned.begin(), owned.end(), (void *)stats));
+        }
+        stats = dalloc<double>((size_t)4 * cap, owned);
+        if (stats_host) cudaFreeHost(stats_host);
+        stats_host = nullptr;
+        CUDA_CHECK(cudaMallocHost(&stats_host, sizeof(double) * 4 * cap));
+        stats_cap = cap;
+    }
+
+    void report(int it, int niter_total, const double *row) {
+        h_rdiff.push_back(row[0]);
+        h_rho.push_back(row[1]);
+        h_r.push_back(row[2]);
+        h_s.push_back(row[3]);
+        if (verbose) {
+            std::fprintf(stderr, "iter (%d/%d), rdiff ||f(k+1)-f(k)||:%f \n", it, niter_total, row[0]);
+            std::fflush(stderr);
+        }
+    }
+
+    void iterate(int niter) {
+        check_live();
+        if (!session) throw Error(RECTV_ERR_STATE, "rectv: setup must precede iterate");
+        if (niter < 0) throw Error(RECTV_ERR_ARG, "rectv: niter must be >= 0");
+        if (niter == 0) return;
+        ensure_stats(niter);
+        CUDA_CHECK(cudaMemsetAsync(iter_ctr, 0, sizeof(int), stream));
+        std::vector<cudaEvent_t> ev;
+        if (verbose) {
+            ev.resize(niter);
+            for (auto &e : ev) CUDA_CHECK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+        }
+        int reported = 0;
+        try {
+            for (int it = 0; it < niter; ++it) {
+                launch_outer();
+                if (verbose) {
+                    CUDA_CHECK(cudaMemcpyAsync(stats_host + 4 * it, stats + 4 * it, 4 * sizeof(double),
+                                               cudaMemcpyDeviceToHost, stream));
+                    CUDA_CHECK(cudaEventRecord(ev[it], stream));
+                    // report the previous iteration while this one runs
+                    while (reported < it) {
+                        CUDA_CHECK(cudaEventSynchronize(ev[reported]));
+                        report(iters_done + reported, niter, stats_host + 4 * reported);
+                        ++reported;
+                    }
+                }
+            }
+            if (verbose) {
+                while (reported < niter) {
+                    CUDA_CHECK(cudaEventSynchronize(ev[reported]));
+                    report(iters_done + reported, niter, stats_host + 4 * reported);
+                    ++reported;
+                }
+            } else {
+                CUDA_CHECK(cudaMemcpyAsync(stats_host, stats, 4 * sizeof(double) * niter, cudaMemcpyDeviceToHost,
+                                           stream));
+                CUDA_CHECK(cudaStreamSynchronize(stream));
+                for (int it = 0; it < niter; ++it) {
+                    h_rdiff.push_back(stats_host[4 * it]);
+                    h_rho.push_back(stats_host[4 * it + 1]);
+                    h_r.push_back(stats_host[4 * it + 2]);
+                    h_s.push_back(stats_host[4 * it + 3]);
+                }
+            }
+        } catch (...) {
+            for (auto &e : ev) cudaEventDestroy(e);
+            throw;
+        }
+        for (auto &e : ev) cudaEventDestroy(e);
+        iters_done += niter;
+        int errs = 0;
+        CUDA_CHECK(cudaMemcpyAsync(&errs, gd.err, sizeof(int), cudaMemcpyDeviceToHost, stream));
+        CUDA_CHECK(cudaStreamSynchronize(stream));
+        if (errs) throw Error(RECTV_ERR_STATE, "rectv: internal plan/stencil mismatch");
+    }
+
+    // ---- operator API helpers: any number of slices via zero-padded batches ----
+    void op_forward(float *out, const float *u, int nslices, float tau) {
+        for (int z0 = 0; z0 < nslices; z0 += zb) {
+            const int nb = std::min(zb, nslices - z0);
+            const float *src = u + (size_t)z0 * slab;
+            float *dst = out + (size_t)z0 * ntheta * n;
+            if (nb == zb) {
+                forward(src, nullptr, dst, tau, 0);
+            } else {
+                float *tmp = U[2];
+                CUDA_CHECK(cudaMemsetAsync(tmp, 0, sizeof(float) * zb * slab, stream));
+                CUDA_CHECK(cudaMemcpyAsync(tmp, src, sizeof(float) * nb * slab, cudaMemcpyDeviceToDevice, stream));
+                forward(tmp, nullptr, h1, tau, 0);
+                CUDA_CHECK(cudaMemcpyAsync(dst, h1, sizeof(float) * nb * ntheta * n, cudaMemcpyDeviceToDevice,
+                                           stream));
+            }
+        }
+    }
+
+    void op_adjoint(float *u, const float *g, int nslices, float tau) {
+        for (int z0 = 0; z0 < nslices; z0 += zb) {
+            const int nb = std::min(zb, nslices - z0);
+            const float *src = g + (size_t)z0 * ntheta * n;
+            float *dst = u + (size_t)z0 * slab;
+            if (nb == zb) {
+                adjoint(src, dst, tau);
+            } else {
+                CUDA_CHECK(cudaMemsetAsync(h1, 0, sizeof(float) * zb * ntheta * n, stream));
+                CUDA_CHECK(cudaMemcpyAsync(h1, src, sizeof(float) * nb * ntheta * n, cudaMemcpyDeviceToDevice,
+                                           stream));
+                float *tmp = U[2];
+                CUDA_CHECK(cudaMemsetAsync(tmp, 0, sizeof(float) * zb * slab, stream));
+                adjoint(h1, tmp, 1.0f);
+                launch_axpy(dst, tmp, tau, (long long)nb * slab);
+            }
+        }
+    }
+
+    void launch_axpy(float *y, const float *x, float a, long long count);
+
+    void check_adjoints(double *res, const float *g_h, const float *theta_h, const float *phi_h,
+                        float lambda1_, float center) {
+        check_live();
+        if (nz != nzp)
+            throw Error(RECTV_ERR_ARG, "rectv: check_adjoints needs nz == nzp (one chunk), as in rectv.cu:258");
+        session = false;
+        drop_graphs();
+        set_geometry(theta_h, phi_h, center);
+        set_lambda1(lambda1_);
+        CUDA_CHECK(cudaMemcpyAsync(gdata, g_h, sizeof(float) * (size_t)nz * ntheta * n, cudaMemcpyHostToDevice,
+                                   stream));
+        float *f = U[0], *fn = U[1];
+        CUDA_CHECK(cudaMemsetAsync(f, 0, sizeof(float) * (size_t)nzc * slab, stream));
+        CUDA_CHECK(cudaMemsetAsync(fn, 0, sizeof(float) * (size_t)nzc * slab, stream));
+        CUDA_CHECK(cudaMemsetAsync(dot_out, 0, sizeof(double) * 8, stream));
+        // rectv.cu:266-275
+        adjoint(gdata, f, 1.0f);
+        forward(f, nullptr, h1, 1.0f, 0);
+        const long long nf = (long long)nzc * slab, ng = (long long)nz * ntheta * n;
+        launch_dot(f, f, nf, dot_part, dot_parts(), dot_out + 0, stream);
+        launch_dot(gdata, h1, ng, dot_part, dot_parts(), dot_out + 1, stream);
+        launch_dot(h1, h1, ng, dot_part, dot_parts(), dot_out + 2, stream);
+        // rectv.cu:278-288 (gradient into the spectrum scratch, float4 layout)
+        float *h2 = reinterpret_cast<float *>(spec);
+        TvGeo t1 = tv;
+        t1.nchunks = 1;
+        launch_gradient_ref(f, 0, h2, 0, 0, t1, stream);
+        launch_divergent_ref(fn, h2, 1.0f, t1, stream);
+        launch_dot(f, fn, nf, dot_part, dot_parts(), dot_out + 3, stream);
+        const long long npts = (long long)(n + 1) * (n + 1) * (m + 1) * (nz + 1);
+        launch_dot(h2, h2, npts, dot_part, dot_parts(), dot_out + 4, stream);
+        launch_dot(fn, fn, nf, dot_part, dot_parts(), dot_out + 5, stream);
+        double r[8];
+        CUDA_CHECK(cudaMemcpyAsync(r, dot_out, sizeof(double) * 8, cudaMemcpyDeviceToHost, stream));
+        CUDA_CHECK(cudaStreamSynchronize(stream));
+        for (int i = 0; i < 6; ++i) res[i] += r[i];
+    }
+};
+
+__global__ void k_axpy(float *y, const float *x, float a, long long count) {
+    const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (i < count) y[i] += a * x[i];
+}
+
+void Handle::launch_axpy(float *y, const float *x, float a, long long count) {
+    k_axpy<<<(unsigned)((count + 255) / 256), 256, 0, stream>>>(y, x, a, count);
+    LAUNCH_CHECK("k_axpy");
+}
+
+}  // namespace rectv
+
+// ===========================================================================
+// C ABI
+// ===========================================================================
+struct rectv_handle {
+    rectv::Handle *h;
+    int n, ntheta, m, nz, nzp, ngpus;
+};
+
+namespace {
+
+template <class F>
+int guarded(F &&f) {
+    try {
+        f();
+        rectv::g_last_error.clear();
+        return RECTV_OK;
+    } catch (const rectv::Error &e) {
+        rectv::g_last_error = e.what();
+        return e.code;
+    } catch (const std::bad_alloc &) {
+        rectv::g_last_error = "host out of memory";
+        return RECTV_ERR_NOMEM;
+    } catch (const std::exception &e) {
+        rectv::g_last_error = e.what();
+        return RECTV_ERR_ARG;
+    }
+}
+
+rectv::Handle *live(rectv_handle *h) {
+    if (!h) throw rectv::Error(RECTV_ERR_ARG, "rectv: null handle");
+    if (!h->h || h->h->freed) throw rectv::Error(RECTV_ERR_STATE, "rectv: object was freed");
+    return h->h;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char *rectv_last_error(void) { return rectv::g_last_error.c_str(); }
+
+const char *rectv_version(void) { return "rectv_gb300 1.0 (sm_103a)"; }
+
+int rectv_create(int n, int ntheta, int m, int nz, int nzp, int ngpus, rectv_handle **out) {
+    return guarded([&] {
+        if (!out) throw rectv::Error(RECTV_ERR_ARG, "rectv_create: null output");
+        *out = nullptr;
+        auto *hh = new rectv::Handle(n, ntheta, m, nz, nzp, ngpus);
+        auto *w = new rectv_handle{hh, n, ntheta, m, nz, nzp, hh->ngpus};
+        *out = w;
+    });
+}
+
+int rectv_get_dims(const rectv_handle *h, int *n, int *ntheta, int *m, int *nz, int *nzp, int *ngpus) {
+    return guarded([&] {
+        if (!h) throw rectv::Error(RECTV_ERR_ARG, "rectv: null handle");
+        if (n) *n = h->n;
+        if (ntheta) *ntheta = h->ntheta;
+        if (m) *m = h->m;
+        if (nz) *nz = h->nz;
+        if (nzp) *nzp = h->nzp;
+        if (ngpus) *ngpus = h->ngpus;
+    });
+}
+
+int rectv_run(rectv_handle *h, float *fres, const float *g, const float *theta, const float *phi, float center,
+              float lambda0, float lambda1, int niter, int titer) {
+    return guarded([&] {
+        rectv::Handle *H = live(h);
+        if (!fres || !g || !theta || !phi) throw rectv::Error(RECTV_ERR_ARG, "rectv_run: null pointer");
+        CUDA_CHECK(cudaMemcpyAsync(H->gdata, g, sizeof(float) * (size_t)H->nz * H->ntheta * H->n,
+                                   cudaMemcpyHostToDevice, H->stream));
+        H->setup(theta, phi, center, lambda0, lambda1, titer);
+        H->iterate(niter);
+        const size_t nf = (size_t)H->nzc * H->slab;
+        CUDA_CHECK(cudaMemcpyAsync(fres, H->U[H->cur], sizeof(float) * nf, cudaMemcpyDeviceToHost, H->stream));
+        CUDA_CHECK(cudaStreamSynchronize(H->stream));
+        const size_t total = (size_t)H->nz * H->slab;
+        if (total > nf) std::memset(fres + nf, 0, sizeof(float) * (total - nf));
+    });
+}
+
+int rectv_check_adjoints(rectv_handle *h, double *res, const float *g, const float *theta, const float *phi,
+                         float lambda1, float center) {
+    return guarded([&] {
+        rectv::Handle *H = live(h);
+        if (!res || !g || !theta || !phi) throw rectv::Error(RECTV_ERR_ARG, "rectv_check_adjoints: null pointer");
+        H->check_adjoints(res, g, theta, phi, lambda1, center);
+    });
+}
+
+int rectv_free(rectv_handle *h) {
+    return guarded([&] {
+        if (!h) throw rectv::Error(RECTV_ERR_ARG, "rectv: null handle");
+        if (h->h) {
+            delete h->h;
+            h->h = nullptr;
+        }
+    });
+}
+
+void rectv_destroy(rectv_handle *h) {
+    if (!h) return;
+    if (h->h) delete h->h;
+    delete h;
+}
+
+int rectv_set_verbose(rectv_handle *h, int verbose) {
+    return guarded([&] { live(h)->verbose = verbose != 0; });
+}
+
+int rectv_set_graphs(rectv_handle *h, int enable) {
+    return guarded([&] {
+        rectv::Handle *H = live(h);
+        H->use_graphs = enable != 0;
+        H->drop_graphs();
+    });
+}
+
+int rectv_setup_device(rectv_handle *h, const float *d_g, const float *d_theta, const float *d_phi, float center,
+                       float lambda0, float lambda1, int titer) {
+    return guarded([&] {
+        rectv::Handle *H = live(h);
+        std::vector<float> th(H->ntheta), ph((size_t)2 * H->ntheta * H->m);
+        CUDA_CHECK(cudaMemcpyAsync(H->gdata, d_g, sizeof(float) * (size_t)H->nz * H->ntheta * H->n,
+                                   cudaMemcpyDeviceToDevice, H->stream));
+        CUDA_CHECK(cudaMemcpyAsync(th.data(), d_theta, sizeof(float) * th.size(), cudaMemcpyDeviceToHost, H->stream));
+        CUDA_CHECK(cudaMemcpyAsync(ph.data(), d_phi, sizeof(float) * ph.size(), cudaMemcpyDeviceToHost, H->stream));
+        CUDA_CHECK(cudaStreamSynchronize(H->stream));
+        H->setup(th.data(), ph.data(), center, lambda0, lambda1, titer);
+    });
+}
+
+int rectv_iterate(rectv_handle *h, int niter) {
+    return guarded([&] { live(h)->iterate(niter); });
+}
+
+int rectv_get_result_device(rectv_handle *h, float *d_f) {
+    return guarded([&] {
+        rectv::Handle *H = live(h);
+        const size_t nf = (size_t)H->nzc * H->slab;
+        CUDA_CHECK(cudaMemcpyAsync(d_f, H->U[H->cur], sizeof(float) * nf, cudaMemcpyDeviceToDevice, H->stream));
+        const size_t total = (size_t)H->nz * H->slab;
+        if (total > nf) CUDA_CHECK(cudaMemsetAsync(d_f + nf, 0, sizeof(float) * (total - nf), H->stream));
+    });
+}
+
+int rectv_get_stream(rectv_handle *h, void **stream) {
+    return guarded([&] {
+        if (!stream) throw rectv::Error(RECTV_ERR_ARG, "rectv_get_stream: null output");
+        *stream = (void *)live(h)->stream;
+    });
+}
+
+int rectv_synchronize(rectv_handle *h) {
+    return guarded([&] { CUDA_CHECK(cudaStreamSynchronize(live(h)->stream)); });
+}
+
+int rectv_get_history(rectv_handle *h, double *rdiff, double *rho, double *r, double *s, int *count) {
+    return guarded([&] {
+        rectv::Handle *H = live(h);
+        if (!count) throw rectv::Error(RECTV_ERR_ARG, "rectv_get_history: null count");
+        const int cap = *count;
+        const int nrec = (int)H->h_rdiff.size();
+        for (int i = 0; i < std::min(cap, nrec); ++i) {
+            if (rdiff) rdiff[i] = H->h_rdiff[i];
+            if (rho) rho[i] = H->h_rho[i];
+            if (r) r[i] = H->h_r[i];
+            if (s) s[i] = H->h_s[i];
+        }
+        *count = nrec;
+    });
+}
+
+int rectv_op_set_geometry(rectv_handle *h, const float *d_theta, const float *d_phi, float center) {
+    return guarded([&] {
+        rectv::Handle *H = live(h);
+        std::vector<float> th(H->ntheta), ph((size_t)2 * H->ntheta * H->m);
+        CUDA_CHECK(cudaMemcpyAsync(th.data(), d_theta, sizeof(float) * th.size(), cudaMemcpyDeviceToHost, H->stream));
+        CUDA_CHECK(cudaMemcpyAsync(ph.data(), d_phi, sizeof(float) * ph.size(), cudaMemcpyDeviceToHost, H->stream));
+        CUDA_CHECK(cudaStreamSynchronize(H->stream));
+        H->session = false;
+        H->set_geometry(th.data(), ph.data(), center);
+    });
+}
+
+int rectv_op_radonapr(rectv_handle *h, float *d_g, const float *d_f, int nslices, float tau) {
+    return guarded([&] {
+        rectv::Handle *H = live(h);
+        if (!H->gd.sincos) throw rectv::Error(RECTV_ERR_STATE, "rectv_op_radonapr: set geometry first");
+        if (nslices < 1 || nslices > H->nz) throw rectv::Error(RECTV_ERR_ARG, "rectv_op_radonapr: bad nslices");
+        H->session = false;
+        H->op_forward(d_g, d_f, nslices, tau);
+        CUDA_CHECK(cudaStreamSynchronize(H->stream));
+    });
+}
+
+int rectv_op_radonapradj(rectv_handle *h, float *d_f, const float *d_g, int nslices, float tau) {
+    return guarded([&] {
+        rectv::Handle *H = live(h);
+        if (!H->gd.sincos) throw rectv::Error(RECTV_ERR_STATE, "rectv_op_radonapradj: set geometry first");
+        if (nslices < 1 || nslices > H->nz) throw rectv::Error(RECTV_ERR_ARG, "rectv_op_radonapradj: bad nslices");
+        H->session = false;
+        H->op_adjoint(d_f, d_g, nslices, tau);
+        CUDA_CHECK(cudaStreamSynchronize(H->stream));
+    });
+}
+
+int rectv_op_gradient(rectv_handle *h, float *d_h2, const float *d_fm, float lambda1, int flgl, int flgr) {
+    return guarded([&] {
+        rectv::Handle *H = live(h);
+        rectv::TvGeo t = H->tv;
+        t.nchunks = 1;
+        t.lambda1 = lambda1;
+        t.sg = (float)(1.0 / (2.0 * std::cbrt(2.0) * ((double)lambda1 / 2.0)));
+        t.sd = (float)(1.0 / (4.0 * std::cbrt(2.0) * ((double)lambda1 / 2.0)));
+        rectv::launch_gradient_ref(d_fm, 1, d_h2, flgl ? 1 : 0, flgr ? 1 : 0, t, H->stream);
+        CUDA_CHECK(cudaStreamSynchronize(H->stream));
+    });
+}
+
+int rectv_op_divergent(rectv_handle *h, float *d_fn, const float *d_h2, float lambda1, float tau) {
+    return guarded([&] {
+        rectv::Handle *H = live(h);
+        rectv::TvGeo t = H->tv;
+        t.nchunks = 1;
+        t.lambda1 = lambda1;
+        t.sg = (float)(1.0 / (2.0 * std::cbrt(2.0) * ((double)lambda1 / 2.0)));
+        t.sd = (float)(1.0 / (4.0 * std::cbrt(2.0) * ((double)lambda1 / 2.0)));
+        rectv::launch_divergent_ref(d_fn, d_h2, tau, t, H->stream);
+        CUDA_CHECK(cudaStreamSynchronize(H->stream));
+    });
+}
+
+}  // extern "C"

@@ -1,0 +1,137 @@
+// Internal declarations shared by the CUDA translation units of librectv_gb300.
+//
+// Data layout in HBM (all float32 unless stated):
+//   volume  u  [z][t][y][x]            z < nz, t < m (time samples), y,x < n
+//   data    g  [z][theta][s]           s < n (detector)
+//   dual    psi, mu: SoA [4][chunk][qz][qt][qy][qx], qz<=nzp, qt<=m, qy,qx<=n
+//   spectra half-plane R2C images [z][t][P][P/2+1] complex (forward) or full
+//           periodic planes [z][t][P][P] complex (adjoint), P = 2n
+//   rows    [z][theta][n] complex (forward), [z][theta][n+2] real / n/2+1
+//           complex in-place R2C (adjoint)
+#pragma once
+
+#include <cuda_runtime.h>
+#include <cufft.h>
+#include <cstdint>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+namespace rectv {
+
+// USFFT interpolation radius.  radonusfft.cu:11 evaluates to 4 for every n;
+// kernels are specialised for it and the host checks the formula.
+constexpr int kR = 4;
+constexpr int kTaps = 2 * kR + 1;
+// The USFFT kernels of the reference use this truncated value of pi
+// (kernels_radonusfft.cuh:1).
+constexpr double kPiUsfft = 3.1415926535;
+
+struct Error : std::runtime_error {
+    int code;
+    Error(int c, const std::string &m) : std::runtime_error(m), code(c) {}
+};
+
+void cuda_check(cudaError_t e, const char *what, const char *file, int line);
+void cufft_check(cufftResult e, const char *what, const char *file, int line);
+#define CUDA_CHECK(x) ::rectv::cuda_check((x), #x, __FILE__, __LINE__)
+#define CUFFT_CHECK(x) ::rectv::cufft_check((x), #x, __FILE__, __LINE__)
+#define LAUNCH_CHECK(what) ::rectv::cuda_check(cudaGetLastError(), what, __FILE__, __LINE__)
+
+// Geometry of the USFFT kernels.
+struct UsGeo {
+    int n, ntheta, m;   // detector width, projections, time samples
+    int P;              // oversampled grid side 2n
+    int hp;             // half-plane row length P/2+1 (complex)
+    long long img_fwd;  // complex elements per forward image (P*hp)
+    long long img_adj;  // complex elements per adjoint image (P*P)
+    float tn;           // (float)(2n)
+    float inv2n;        // 1/(2n)
+    float wexp;         // pi^2/mu
+    float cw;           // (pi/mu)/n : gather weight scale and 1/n of gather
+    int T;              // tile core side
+    int NT;             // tiles per side P/T
+};
+
+// Per-angle constants uploaded at geometry set-up.
+struct GeoDev {
+    float2 *sincos = nullptr;    // [ntheta] (sin, cos) of theta
+    float2 *kmat = nullptr;      // [ntheta][m]  K'(theta,j) = ntheta/sqrt(m) sum_i phi_i(theta) conj(phi_i(t_j))
+    float2 *shiftfwd = nullptr;  // [n]
+    float2 *shiftadj = nullptr;  // [n]
+    float *deapod = nullptr;     // [n] exp(mu (x-n/2)^2)
+    uint32_t *fwd_pts = nullptr; // point ids theta*n+k sorted by tile
+    int4 *fwd_items = nullptr;   // (tile, start, count, 0)
+    int n_fwd_items = 0;
+    uint32_t *adj_pts = nullptr; // point ids, one entry per tile a stencil touches
+    int4 *adj_items = nullptr;   // (tile, start, count, split)
+    int n_adj_items = 0;
+    int *split_tiles = nullptr;  // tiles with more than one adjoint item
+    int n_split_tiles = 0;
+    int *err = nullptr;          // device counter of host/device bin disagreements
+};
+
+// Host-side angle plan (built in plan.cpp).
+struct HostPlan {
+    std::vector<float2> sincos;
+    std::vector<uint32_t> fwd_pts;
+    std::vector<int4> fwd_items;
+    std::vector<uint32_t> adj_pts;
+    std::vector<int4> adj_items;
+    std::vector<int> split_tiles;
+};
+
+HostPlan build_plan(const float *theta, int n, int ntheta, int T, int fwd_cap, int adj_cap);
+
+// ---- USFFT kernel launchers (usfft_kernels.cu) ----
+void launch_deapod_pad(const float *u, float *spec, int nimg, const float *deapod, const UsGeo &g,
+                       cudaStream_t s);
+void launch_gather_fwd(const float2 *spec, float2 *rows, int zb, const GeoDev &gd, const UsGeo &g,
+                       cudaStream_t s);
+void launch_finish_fwd(const float2 *rows, const float *gdata, float *out, int zb, float tau,
+                       int residual, const UsGeo &g, cudaStream_t s);
+void launch_adj_prep(const float *h, float *rowsr, int zb, const UsGeo &g, cudaStream_t s);
+void launch_zero_split(float2 *spec, int zb, const GeoDev &gd, const UsGeo &g, cudaStream_t s);
+void launch_scatter_adj(const float2 *rowsc, float2 *spec, int zb, const GeoDev &gd,
+                        const UsGeo &g, cudaStream_t s);
+void launch_crop_accum(const float2 *spec, float *u, int zb, float tau, const float *deapod,
+                       const UsGeo &g, cudaStream_t s);
+size_t gather_fwd_smem(const UsGeo &g);
+size_t scatter_adj_smem(const UsGeo &g);
+void usfft_prepare();  // kernel attributes; call once, outside stream capture
+
+// ---- TV / ADMM kernel launchers (tv_kernels.cu) ----
+struct TvGeo {
+    int n, m, nzp, nchunks;  // chunks processed: nchunks of nzp slices
+    long long vol_slab;      // n*n*m
+    long long gp;            // grid points per chunk (n+1)^2 (m+1)(nzp+1)
+    long long comp_stride;   // elements between SoA components = nchunks_total*gp
+    float sg;                // gradient scale 1/(2 cbrt2 lambda1/2)
+    float sd;                // divergence scale 1/(4 cbrt2 lambda1/2)
+    float lambda1;
+};
+
+// u_out = u_in - 0.5 * div(rho (G u_in - psi) + mu) for chunks [c0, c0+nchunks)
+void launch_graddiv(const float *u_in, const float *u_old, float *u_out, const float *psi,
+                    const float *mu, const float *rho, int c0, int nchunks_total, const TvGeo &t,
+                    cudaStream_t s);
+// shrink + dual update + residual sums into per-block partials
+int launch_shrink(const float *u_cur, const float *u_old, float *psi, float *mu, const float *rho,
+                  float lambda0, int c0, int nchunks_total, const TvGeo &t, double *partials,
+                  cudaStream_t s);
+int shrink_blocks(const TvGeo &t, int nchunks);
+// sum partials in fixed order, apply the rho rule, append a stats row at *ctr
+void launch_reduce_rho(const double *partials, int nparts, float *rho, double *stats, int *ctr,
+                       int cap, cudaStream_t s);
+// reference-layout gradient / divergence for the operator API and check_adjoints
+// fm points at slab zbase-1 of the extended chunk (zbase = 1 when fm holds
+// the two halo slabs, 0 when it holds the chunk only and flgl = flgr = 0)
+void launch_gradient_ref(const float *fm, int zbase, float *h2, int flgl, int flgr, const TvGeo &t,
+                         cudaStream_t s);
+void launch_divergent_ref(float *fn, const float *h2, float tau, const TvGeo &t, cudaStream_t s);
+// FP64 dot products: out[0] += sum a*b over count (a==b allowed); deterministic two-pass
+void launch_dot(const float *a, const float *b, long long count, double *partials, int nparts,
+                double *out, cudaStream_t s);
+int dot_parts();
+
+}  // namespace rectv

@@ -1,0 +1,389 @@
+// 4D total-variation and ADMM kernels (x, y, time, z) for sm_103a.
+//
+// The reference builds an extended copy of the chunk (extendf), writes the
+// float4 gradient (gradf), then runs separate axpby passes and the divergence
+// (kernels_operators.cuh:4-73, admm.cu:5-122).  Here the inner step
+//   u <- u - 1/2 div( rho (G u - psi) + mu )          (admm.cu:85-95)
+// is one kernel that forms each needed gradient component on the fly, and the
+// end-of-iteration shrink / dual update / residual norms (admm.cu:101-117)
+// are another.  The norms are reduced in float64 in a fixed order so the rho
+// rule (rectv.cu:223-232) is deterministic.
+//
+// Chunk semantics (rectv.cu:161-173, extendf): chunk c covers slices
+// [c nzp, (c+1) nzp); the slice below/above a chunk is read from the previous
+// outer iterate u_old (never the one being updated) and at the volume ends the
+// border value is replicated.  Each chunk owns a dual grid of
+// (n+1)^2 (m+1)(nzp+1) points whose point q sees voxel q-1 (clamped).
+#include <cuda_runtime.h>
+
+#include "rectv_internal.cuh"
+
+namespace rectv {
+
+namespace {
+
+struct ChunkView {
+    const float *u;     // current iterate, global [z][t][y][x]
+    const float *uold;  // previous outer iterate (halo source)
+    int n, m, nzp, c, nch;
+    long long slab;     // n*n*m
+};
+
+// Value of the extended chunk at voxel coordinates (x,y,t) in [0,n)x[0,n)x[0,m)
+// and chunk-local slice zl in [-1, nzp] (extendf, kernels_operators.cuh:14-19).
+__device__ __forceinline__ float ext_val(const ChunkView &v, int x, int y, int t, int zl) {
+    const long long inplane = ((long long)t * v.n + y) * v.n + x;
+    const long long z0 = (long long)v.c * v.nzp;
+    if (zl < 0) {
+        if (v.c > 0) return v.uold[(z0 - 1) * v.slab + inplane];
+        zl = 0;
+    } else if (zl >= v.nzp) {
+        if (v.c < v.nch - 1) return v.uold[(z0 + v.nzp) * v.slab + inplane];
+        zl = v.nzp - 1;
+    }
+    return v.u[(z0 + zl) * v.slab + inplane];
+}
+
+__device__ __forceinline__ int clampi(int a, int lo, int hi) { return a < lo ? lo : (a > hi ? hi : a); }
+
+template <int NW>
+__device__ __forceinline__ void block_reduce3(double a, double b, double c, double *out) {
+    __shared__ double sh[3][NW];
+    for (int o = 16; o > 0; o >>= 1) {
+        a += __shfl_down_sync(0xffffffffu, a, o);
+        b += __shfl_down_sync(0xffffffffu, b, o);
+        c += __shfl_down_sync(0xffffffffu, c, o);
+    }
+    const int tid = threadIdx.y * blockDim.x + threadIdx.x;  // 2D blocks
+    const int lane = tid & 31, w = tid >> 5;
+    if (lane == 0) {
+        sh[0][w] = a;
+        sh[1][w] = b;
+        sh[2][w] = c;
+    }
+    __syncthreads();
+    if (tid == 0) {
+        double s0 = 0, s1 = 0, s2 = 0;
+        for (int i = 0; i < NW; ++i) {
+            s0 += sh[0][i];
+            s1 += sh[1][i];
+            s2 += sh[2][i];
+        }
+        out[0] = s0;
+        out[1] = s1;
+        out[2] = s2;
+    }
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// Fused inner step (gradient, lin4, divergent of admm.cu:85-95 with tau=-0.5):
+//   u_out(v) = u_in(v) + tau sd sum_d [h_d(q-e_d) - h_d(q)],  q = v+1,
+//   h = rho (G u_in - psi) + mu.
+// One thread per voxel; blocks of 32x8 over (x, y), grid.z over (slice, t).
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(256)
+    k_graddiv(const float *__restrict__ uin, const float *__restrict__ uold, float *__restrict__ uout,
+              const float *__restrict__ psi, const float *__restrict__ mu, const float *__restrict__ rhop,
+              TvGeo t, int c0, int nch_total, float tau) {
+    const int x = blockIdx.x * blockDim.x + threadIdx.x;
+    const int y = blockIdx.y * blockDim.y + threadIdx.y;
+    const int pl = blockIdx.z;
+    const int tt = pl % t.m;
+    const int zr = pl / t.m;
+    if (x >= t.n || y >= t.n) return;
+    const int n = t.n, m = t.m, nzp = t.nzp;
+    const int c = c0 + zr / nzp, zl = zr % nzp;
+    const long long slab = t.vol_slab;
+    const long long v = ((long long)c * nzp + zl) * slab + ((long long)tt * n + y) * n + x;
+    const float f0 = uin[v];
+    const float fxp = uin[v + (x < n - 1 ? 1 : 0)], fxm = uin[v - (x > 0 ? 1 : 0)];
+    const float fyp = uin[v + (y < n - 1 ? n : 0)], fym = uin[v - (y > 0 ? n : 0)];
+    const long long nn = (long long)n * n;
+    const float ftp = uin[v + (tt < m - 1 ? nn : 0)], ftm = uin[v - (tt > 0 ? nn : 0)];
+    float fzp, fzm;
+    if (zl < nzp - 1) fzp = uin[v + slab];
+    else fzp = (c < nch_total - 1) ? uold[v + slab] : f0;
+    if (zl > 0) fzm = uin[v - slab];
+    else fzm = (c > 0) ? uold[v - slab] : f0;
+
+    const float rho = *rhop;
+    const long long sx = 1, sy = n + 1, st = (long long)(n + 1) * (n + 1), sz = st * (m + 1);
+    const long long q = (long long)c * t.gp + (zl + 1) * sz + (tt + 1) * st + (y + 1) * sy + (x + 1);
+    const long long cs = t.comp_stride;
+    const float sg = t.sg;
+    float d;
+    {  // x
+        const float hq = rho * (sg * (fxp - f0) - psi[q]) + mu[q];
+        const float hm = rho * (sg * (f0 - fxm) - psi[q - sx]) + mu[q - sx];
+        d = hm - hq;
+    }
+    {  // y
+        const float hq = rho * (sg * (fyp - f0) - psi[cs + q]) + mu[cs + q];
+        const float hm = rho * (sg * (f0 - fym) - psi[cs + q - sy]) + mu[cs + q - sy];
+        d += hm - hq;
+    }
+    {  // t (scaled by lambda1 in both gradient and divergence)
+        const float sgt = sg * t.lambda1;
+        const float hq = rho * (sgt * (ftp - f0) - psi[2 * cs + q]) + mu[2 * cs + q];
+        const float hm = rho * (sgt * (f0 - ftm) - psi[2 * cs + q - st]) + mu[2 * cs + q - st];
+        d += t.lambda1 * (hm - hq);
+    }
+    {  // z
+        const float hq = rho * (sg * (fzp - f0) - psi[3 * cs + q]) + mu[3 * cs + q];
+        const float hm = rho * (sg * (f0 - fzm) - psi[3 * cs + q - sz]) + mu[3 * cs + q - sz];
+        d += hm - hq;
+    }
+    uout[v] = f0 + tau * t.sd * d;
+}
+
+void launch_graddiv(const float *u_in, const float *u_old, float *u_out, const float *psi,
+                    const float *mu, const float *rho, int c0, int nchunks_total, const TvGeo &t,
+                    cudaStream_t s) {
+    dim3 bs(32, 8), gs((t.n + 31) / 32, (t.n + 7) / 8, t.nchunks * t.nzp * t.m);
+    k_graddiv<<<gs, bs, 0, s>>>(u_in, u_old, u_out, psi, mu, rho, t, c0, nchunks_total, -0.5f);
+    LAUNCH_CHECK("k_graddiv");
+}
+
+// ---------------------------------------------------------------------------
+// End of outer iteration for one chunk (admm.cu:101-117):
+//   h = G u_cur, ho = G u_old (the reference's h2stored),
+//   psi = shrink(h + mu/rho, lambda0/rho), mu += rho h - rho psi,
+//   partial sums of |h-psi|^2, |ho-h|^2 and, for q >= 1, (u_cur-u_old)^2.
+// One thread per dual grid point, blocks of 32x8 over (qx, qy).
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(256)
+    k_shrink(const float *__restrict__ ucur, const float *__restrict__ uold, float *__restrict__ psi,
+             float *__restrict__ mu, const float *__restrict__ rhop, float lambda0, TvGeo t, int c0,
+             int nch_total, double *__restrict__ partials) {
+    const int qx = blockIdx.x * blockDim.x + threadIdx.x;
+    const int qy = blockIdx.y * blockDim.y + threadIdx.y;
+    const int pl = blockIdx.z;
+    const int n = t.n, m = t.m, nzp = t.nzp;
+    const int qt = pl % (m + 1);
+    const int cz = pl / (m + 1);
+    const int qz = cz % (nzp + 1);
+    const int c = c0 + cz / (nzp + 1);
+    double a0 = 0.0, a1 = 0.0, a2 = 0.0;
+    if (qx <= n && qy <= n) {
+        ChunkView vc{ucur, uold, n, m, nzp, c, nch_total, t.vol_slab};
+        ChunkView vo{uold, uold, n, m, nzp, c, nch_total, t.vol_slab};
+        const int x0 = clampi(qx - 1, 0, n - 1), x1 = clampi(qx, 0, n - 1);
+        const int y0 = clampi(qy - 1, 0, n - 1), y1 = clampi(qy, 0, n - 1);
+        const int t0 = clampi(qt - 1, 0, m - 1), t1 = clampi(qt, 0, m - 1);
+        const int z0 = qz - 1, z1 = qz;
+        const float sg = t.sg, sgt = t.sg * t.lambda1;
+        const float fc = ext_val(vc, x0, y0, t0, z0);
+        float h[4] = {sg * (ext_val(vc, x1, y0, t0, z0) - fc), sg * (ext_val(vc, x0, y1, t0, z0) - fc),
+                      sgt * (ext_val(vc, x0, y0, t1, z0) - fc), sg * (ext_val(vc, x0, y0, t0, z1) - fc)};
+        const float fo = ext_val(vo, x0, y0, t0, z0);
+        float ho[4] = {sg * (ext_val(vo, x1, y0, t0, z0) - fo), sg * (ext_val(vo, x0, y1, t0, z0) - fo),
+                       sgt * (ext_val(vo, x0, y0, t1, z0) - fo), sg * (ext_val(vo, x0, y0, t0, z1) - fo)};
+        const float rho = *rhop;
+        const long long q = (long long)c * t.gp + (((long long)qz * (m + 1) + qt) * (n + 1) + qy) * (n + 1) + qx;
+        const long long cs = t.comp_stride;
+        float mv[4], ps[4];
+        float za2 = 0.f;
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+            mv[i] = mu[i * cs + q];
+            ps[i] = h[i] + mv[i] / rho;  // solve_reg_ker, admm.cu:49-52
+            za2 += ps[i] * ps[i];
+        }
+        const float za = sqrtf(za2);
+        const float thr = lambda0 / rho;
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+            ps[i] = (za <= thr) ? 0.f : ps[i] - thr * ps[i] / za;
+            const float mn = mv[i] + rho * h[i] - rho * ps[i];  // lin4(mu,h2,psi,1,rho,-rho)
+            psi[i * cs + q] = ps[i];
+            mu[i * cs + q] = mn;
+            const double dr = (double)h[i] - (double)ps[i];
+            const double ds = (double)ho[i] - (double)h[i];
+            a0 += dr * dr;
+            a1 += ds * ds;
+        }
+        if (qx >= 1 && qy >= 1 && qt >= 1 && qz >= 1) {
+            const long long vv = ((long long)c * nzp + (qz - 1)) * t.vol_slab +
+                                 ((long long)(qt - 1) * n + (qy - 1)) * n + (qx - 1);
+            const double dd = (double)ucur[vv] - (double)uold[vv];
+            a2 = dd * dd;
+        }
+    }
+    const long long bid = ((long long)blockIdx.z * gridDim.y + blockIdx.y) * gridDim.x + blockIdx.x;
+    block_reduce3<8>(a0, a1, a2, partials + 3 * bid);
+}
+
+int shrink_blocks(const TvGeo &t, int nchunks) {
+    return ((t.n + 1 + 31) / 32) * ((t.n + 1 + 7) / 8) * nchunks * (t.nzp + 1) * (t.m + 1);
+}
+
+int launch_shrink(const float *u_cur, const float *u_old, float *psi, float *mu, const float *rho,
+                  float lambda0, int c0, int nchunks_total, const TvGeo &t, double *partials,
+                  cudaStream_t s) {
+    dim3 bs(32, 8), gs((t.n + 1 + 31) / 32, (t.n + 1 + 7) / 8, t.nchunks * (t.nzp + 1) * (t.m + 1));
+    k_shrink<<<gs, bs, 0, s>>>(u_cur, u_old, psi, mu, rho, lambda0, t, c0, nchunks_total, partials);
+    LAUNCH_CHECK("k_shrink");
+    return (int)(gs.x * gs.y * gs.z);
+}
+
+// ---------------------------------------------------------------------------
+// Fixed-order FP64 sum of the shrink partials and the rho rule
+// (rectv.cu:223-232): r = sum |h-psi|^2, s = rho^2 sum |dG u|^2;
+// r > 10 s -> rho *= 2, s > 10 r -> rho *= 0.5.
+// stats row = (||u_new - u_old||^2, rho_new, r, s); *iter_ctr counts rows.
+// ---------------------------------------------------------------------------
+__global__ void k_reduce_rho(const double *__restrict__ partials, int nparts, float *rho,
+                             double *stats, int *iter_ctr, int stats_cap) {
+    __shared__ double sh[3][256];
+    double a = 0, b = 0, c = 0;
+    for (int i = threadIdx.x; i < nparts; i += blockDim.x) {
+        a += partials[3 * i];
+        b += partials[3 * i + 1];
+        c += partials[3 * i + 2];
+    }
+    sh[0][threadIdx.x] = a;
+    sh[1][threadIdx.x] = b;
+    sh[2][threadIdx.x] = c;
+    __syncthreads();
+    for (int o = 128; o > 0; o >>= 1) {
+        if ((int)threadIdx.x < o) {
+            sh[0][threadIdx.x] += sh[0][threadIdx.x + o];
+            sh[1][threadIdx.x] += sh[1][threadIdx.x + o];
+            sh[2][threadIdx.x] += sh[2][threadIdx.x + o];
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        const float r0 = *rho;
+        const double r = sh[0][0];
+        const double sv = (double)r0 * (double)r0 * sh[1][0];
+        float rn = r0;
+        if (r > 10.0 * sv) rn = r0 * 2.0f;
+        else if (sv > 10.0 * r) rn = r0 * 0.5f;
+        *rho = rn;
+        const int it = *iter_ctr;
+        if (it < stats_cap) {
+            stats[4 * it + 0] = sh[2][0];
+            stats[4 * it + 1] = rn;
+            stats[4 * it + 2] = r;
+            stats[4 * it + 3] = sv;
+        }
+        *iter_ctr = it + 1;
+    }
+}
+
+void launch_reduce_rho(const double *partials, int nparts, float *rho, double *stats, int *ctr,
+                       int cap, cudaStream_t s) {
+    k_reduce_rho<<<1, 256, 0, s>>>(partials, nparts, rho, stats, ctr, cap);
+    LAUNCH_CHECK("k_reduce_rho");
+}
+
+// ---------------------------------------------------------------------------
+// Reference-layout gradient (extendf + gradf, kernels_operators.cuh:4-44):
+// fm [nzp+2][m][n][n] with halo slabs at 0 and nzp+1, h2 float4
+// [nzp+1][m+1][n+1][n+1].
+// ---------------------------------------------------------------------------
+__global__ void k_gradient_ref(const float *__restrict__ fm, int zbase, float4 *__restrict__ h2, int flgl,
+                               int flgr, TvGeo t) {
+    const int qx = blockIdx.x * blockDim.x + threadIdx.x;
+    const int qy = blockIdx.y * blockDim.y + threadIdx.y;
+    const int pl = blockIdx.z;
+    const int n = t.n, m = t.m, nzp = t.nzp;
+    const int qt = pl % (m + 1), qz = pl / (m + 1);
+    if (qx > n || qy > n) return;
+    auto fe = [&](int a, int b, int c, int d) -> float {
+        const int x = clampi(a - 1, 0, n - 1), y = clampi(b - 1, 0, n - 1), tt = clampi(c - 1, 0, m - 1);
+        const int z = clampi(d - 1, -flgl, nzp - 1 + flgr) + zbase;
+        return fm[(((long long)z * m + tt) * n + y) * n + x];
+    };
+    const float f0 = fe(qx, qy, qt, qz);
+    const float s = t.sg;
+    float4 h;
+    h.x = (fe(qx + 1, qy, qt, qz) - f0) * s;
+    h.y = (fe(qx, qy + 1, qt, qz) - f0) * s;
+    h.z = (fe(qx, qy, qt + 1, qz) - f0) * s * t.lambda1;
+    h.w = (fe(qx, qy, qt, qz + 1) - f0) * s;
+    h2[(((long long)qz * (m + 1) + qt) * (n + 1) + qy) * (n + 1) + qx] = h;
+}
+
+void launch_gradient_ref(const float *fm, int zbase, float *h2, int flgl, int flgr, const TvGeo &t,
+                         cudaStream_t s) {
+    dim3 bs(32, 8), gs((t.n + 1 + 31) / 32, (t.n + 1 + 7) / 8, (t.nzp + 1) * (t.m + 1));
+    k_gradient_ref<<<gs, bs, 0, s>>>(fm, zbase, reinterpret_cast<float4 *>(h2), flgl, flgr, t);
+    LAUNCH_CHECK("k_gradient_ref");
+}
+
+// Reference-layout divergence (div, kernels_operators.cuh:46-73): four
+// separately rounded accumulations, as in the reference.
+__global__ void k_divergent_ref(float *__restrict__ fn, const float4 *__restrict__ h2, float tau,
+                                TvGeo t) {
+    const int x = blockIdx.x * blockDim.x + threadIdx.x;
+    const int y = blockIdx.y * blockDim.y + threadIdx.y;
+    const int pl = blockIdx.z;
+    const int n = t.n, m = t.m;
+    const int tt = pl % m, z = pl / m;
+    if (x >= n || y >= n) return;
+    const long long v = (((long long)z * m + tt) * n + y) * n + x;
+    const long long sy = n + 1, st = sy * (n + 1), sz = st * (m + 1);
+    const long long q = (z + 1) * sz + (tt + 1) * st + (y + 1) * sy + (x + 1);
+    const float s = t.sd;
+    float f = fn[v];
+    f += tau * (h2[q - 1].x - h2[q].x) * s;
+    f += tau * (h2[q - sy].y - h2[q].y) * s;
+    f += tau * (h2[q - st].z - h2[q].z) * s * t.lambda1;
+    f += tau * (h2[q - sz].w - h2[q].w) * s;
+    fn[v] = f;
+}
+
+void launch_divergent_ref(float *fn, const float *h2, float tau, const TvGeo &t, cudaStream_t s) {
+    dim3 bs(32, 8), gs((t.n + 31) / 32, (t.n + 7) / 8, t.nzp * t.m);
+    k_divergent_ref<<<gs, bs, 0, s>>>(fn, reinterpret_cast<const float4 *>(h2), tau, t);
+    LAUNCH_CHECK("k_divergent_ref");
+}
+
+// ---------------------------------------------------------------------------
+// FP64 dot product sum_i a_i b_i of float32 arrays, two fixed-order passes.
+// ---------------------------------------------------------------------------
+constexpr int kDotParts = 1024;
+int dot_parts() { return kDotParts; }
+
+__global__ void k_dot_part(const float *__restrict__ a, const float *__restrict__ b, long long count,
+                           double *__restrict__ partials) {
+    double acc = 0.0;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < count;
+         i += (long long)gridDim.x * blockDim.x)
+        acc += (double)a[i] * (double)b[i];
+    __shared__ double sh[256];
+    sh[threadIdx.x] = acc;
+    __syncthreads();
+    for (int o = 128; o > 0; o >>= 1) {
+        if ((int)threadIdx.x < o) sh[threadIdx.x] += sh[threadIdx.x + o];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) partials[blockIdx.x] = sh[0];
+}
+
+__global__ void k_dot_final(const double *__restrict__ partials, int nparts, double *out) {
+    __shared__ double sh[256];
+    double acc = 0.0;
+    for (int i = threadIdx.x; i < nparts; i += blockDim.x) acc += partials[i];
+    sh[threadIdx.x] = acc;
+    __syncthreads();
+    for (int o = 128; o > 0; o >>= 1) {
+        if ((int)threadIdx.x < o) sh[threadIdx.x] += sh[threadIdx.x + o];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) *out += sh[0];
+}
+
+void launch_dot(const float *a, const float *b, long long count, double *partials, int nparts,
+                double *out, cudaStream_t s) {
+    k_dot_part<<<nparts, 256, 0, s>>>(a, b, count, partials);
+    LAUNCH_CHECK("k_dot_part");
+    k_dot_final<<<1, 256, 0, s>>>(partials, nparts, out);
+    LAUNCH_CHECK("k_dot_final");
+}
+
+}  // namespace rectv

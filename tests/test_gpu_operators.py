@@ -1,0 +1,142 @@
+"""GPU parity of the reference's operators (radonapr, radonapradj, gradient,
+divergent) against the FP64 oracle, through the C ABI.
+
+Tolerances: operators are FP32 on the GPU; relative L2 error against the FP64
+oracle must be below 2e-5, and the GPU adjoint identity
+<R u, g> = <u, R* g> must hold to 1e-5 relative.
+"""
+
+import numpy as np
+import pytest
+
+from oracle import rectv_oracle as orc
+
+pytestmark = pytest.mark.gpu
+
+OP_TOL = 2e-5
+
+
+def rel(a, b):
+    return float(np.linalg.norm(np.asarray(a, np.float64) - b) / max(np.linalg.norm(b), 1e-300))
+
+
+@pytest.fixture(scope="module")
+def env(lib_built, torch_cuda):
+    from rectv_gpu_gb300 import rectv
+    return torch_cuda, rectv
+
+
+def dev(torch, a):
+    return torch.from_numpy(np.ascontiguousarray(a)).cuda()
+
+
+CASES = [
+    # n, ntheta, m, nz, nzp, nrot, center_offset
+    (32, 64, 4, 2, 2, 4, 0.0),
+    (64, 128, 8, 3, 3, 4, 2.5),
+    (48, 90, 16, 2, 1, 8, -1.0),
+    (40, 60, 5, 2, 2, 2, 0.0),     # m not a power of two, 2n not a multiple of 16
+    (64, 100, 1, 1, 1, 1, 0.0),
+    (32, 64, 20, 1, 1, 4, 0.0),    # m > 16: two passes over time-sample groups
+]
+
+
+def _geometry(n, ntheta, m, nrot, seed):
+    theta = np.linspace(0, nrot * np.pi, ntheta, endpoint=False).astype(np.float32)
+    rng = np.random.default_rng(seed)
+    if m <= 16 and seed % 2 == 0:
+        phi = orc.takephi(ntheta, m)
+    else:
+        phi = (rng.standard_normal((m, 2 * ntheta)) / np.sqrt(ntheta)).astype(np.float32)
+    return theta, phi
+
+
+@pytest.mark.parametrize("case", CASES)
+def test_radonapr_matches_oracle(env, case):
+    torch, rectv = env
+    n, ntheta, m, nz, nzp, nrot, dc = case
+    center = n / 2 + dc
+    theta, phi = _geometry(n, ntheta, m, nrot, n + m)
+    rng = np.random.default_rng(1)
+    f = rng.standard_normal((nz, m, n, n)).astype(np.float32)
+    ops = orc.Operators(n, ntheta, m, theta, phi, center)
+    ref = ops.radonapr(f.astype(np.float64), 1.0)
+    obj = rectv(n, ntheta, m, nz, nzp, 1)
+    dth, dph, df = dev(torch, theta), dev(torch, phi), dev(torch, f)
+    dg = torch.zeros((nz, ntheta, n), dtype=torch.float32, device="cuda")
+    torch.cuda.synchronize()
+    obj.op_set_geometry(dth.data_ptr(), dph.data_ptr(), center)
+    obj.op_radonapr(dg.data_ptr(), df.data_ptr(), nz, 1.0)
+    got = dg.cpu().numpy()
+    obj.free()
+    assert rel(got, ref) < OP_TOL, rel(got, ref)
+
+
+@pytest.mark.parametrize("case", CASES)
+def test_radonapradj_matches_oracle(env, case):
+    torch, rectv = env
+    n, ntheta, m, nz, nzp, nrot, dc = case
+    center = n / 2 + dc
+    theta, phi = _geometry(n, ntheta, m, nrot, n + m)
+    rng = np.random.default_rng(2)
+    g = rng.standard_normal((nz, ntheta, n)).astype(np.float32)
+    f0 = rng.standard_normal((nz, m, n, n)).astype(np.float32)
+    tau = -0.5
+    ops = orc.Operators(n, ntheta, m, theta, phi, center)
+    ref = f0.astype(np.float64) + ops.radonapradj(g.astype(np.float64), tau)
+    obj = rectv(n, ntheta, m, nz, nzp, 1)
+    dth, dph, dg, df = dev(torch, theta), dev(torch, phi), dev(torch, g), dev(torch, f0)
+    torch.cuda.synchronize()
+    obj.op_set_geometry(dth.data_ptr(), dph.data_ptr(), center)
+    obj.op_radonapradj(df.data_ptr(), dg.data_ptr(), nz, tau)
+    got = df.cpu().numpy()
+    obj.free()
+    inc_ref = ref - f0
+    assert rel(got - f0, inc_ref) < OP_TOL, rel(got - f0, inc_ref)
+
+
+def test_gpu_adjoint_identity(env):
+    torch, rectv = env
+    n, ntheta, m, nz = 64, 180, 8, 2
+    theta = np.linspace(0, 8 * np.pi, ntheta, endpoint=False).astype(np.float32)
+    phi = orc.takephi(ntheta, m)
+    rng = np.random.default_rng(3)
+    f = rng.standard_normal((nz, m, n, n)).astype(np.float32)
+    g = rng.standard_normal((nz, ntheta, n)).astype(np.float32)
+    obj = rectv(n, ntheta, m, nz, nz, 1)
+    dth, dph, df, dg = dev(torch, theta), dev(torch, phi), dev(torch, f), dev(torch, g)
+    rf = torch.zeros_like(dg)
+    ag = torch.zeros_like(df)
+    torch.cuda.synchronize()
+    obj.op_set_geometry(dth.data_ptr(), dph.data_ptr(), n / 2)
+    obj.op_radonapr(rf.data_ptr(), df.data_ptr(), nz, 1.0)
+    obj.op_radonapradj(ag.data_ptr(), dg.data_ptr(), nz, 1.0)
+    a = float(np.sum(rf.cpu().numpy().astype(np.float64) * g))
+    b = float(np.sum(ag.cpu().numpy().astype(np.float64) * f))
+    obj.free()
+    assert abs(a - b) / abs(a) < 1e-5
+
+
+@pytest.mark.parametrize("flg", [(0, 0), (1, 0), (0, 1), (1, 1)])
+def test_gradient_divergent_match_oracle(env, flg):
+    torch, rectv = env
+    n, m, nzp, lam1 = 24, 5, 3, 4.0
+    flgl, flgr = flg
+    rng = np.random.default_rng(4)
+    fm = rng.standard_normal((nzp + 2, m, n, n)).astype(np.float32)
+    obj = rectv(n, 8, m, nzp, nzp, 1)
+    dfm = dev(torch, fm)
+    dh = torch.zeros((nzp + 1, m + 1, n + 1, n + 1, 4), dtype=torch.float32, device="cuda")
+    torch.cuda.synchronize()
+    obj.op_gradient(dh.data_ptr(), dfm.data_ptr(), lam1, flgl, flgr)
+    h = dh.cpu().numpy()
+    href = orc.gradient(fm.astype(np.float64), lam1, flgl, flgr)
+    assert rel(h, href) < 1e-6
+    fn0 = rng.standard_normal((nzp, m, n, n)).astype(np.float32)
+    dfn = dev(torch, fn0)
+    torch.cuda.synchronize()
+    obj.op_divergent(dfn.data_ptr(), dh.data_ptr(), lam1, -0.5)
+    got = dfn.cpu().numpy() - fn0
+    ref = orc.divergent(h.astype(np.float64), lam1, -0.5)
+    obj.free()
+    assert rel(got, ref) < 1e-5
