@@ -123,6 +123,26 @@ int rectv_get_history(rectv_handle *h, double *rdiff, double *rho, double *r, do
 int rectv_set_graphs(rectv_handle *h, int enable);
 
 /* ---------------------------------------------------------------------------
+ * Instrumentation (no reference counterpart).  Kernel ids:
+ *   0 forward USFFT gather, 1 adjoint USFFT scatter, 2 fused gradient-
+ *   divergence step, 3 shrink + dual update + residual sums.
+ * ------------------------------------------------------------------------- */
+
+/* Enqueue `reps` launches of one kernel over one batch of slices on the
+ * handle's stream, on the buffers of the current session (after
+ * rectv_setup_device); the caller times them with events on that stream.
+ * Kernel 3 overwrites the session's dual variables: use after the last
+ * rectv_iterate of a session. */
+int rectv_launch_kernel(rectv_handle *h, int which, int reps);
+
+/* Algorithmic DRAM bytes and FP32 flops of one such launch. */
+int rectv_kernel_cost(rectv_handle *h, int which, double *bytes, double *flops);
+
+/* Per outer ADMM iteration: launches of this library's kernels and cuFFT
+ * executions; and the batch size in slices. */
+int rectv_get_launch_counts(rectv_handle *h, int *kernels, int *fft_execs, int *batch_slices);
+
+/* ---------------------------------------------------------------------------
  * Operator-level entry points (device pointers), the reference's private
  * operators exposed for parity testing.  rectv_op_set_geometry must be called
  * first; it uploads theta/phi and the rotation centre.

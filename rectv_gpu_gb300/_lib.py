@@ -38,6 +38,9 @@ SIGNATURES = {
     "rectv_op_radonapradj": (_I, [_P, _P, _P, _I, _F]),
     "rectv_op_gradient": (_I, [_P, _P, _P, _F, _I, _I]),
     "rectv_op_divergent": (_I, [_P, _P, _P, _F, _F]),
+    "rectv_launch_kernel": (_I, [_P, _I, _I]),
+    "rectv_kernel_cost": (_I, [_P, _I, _P, _P]),
+    "rectv_get_launch_counts": (_I, [_P, _IP, _IP, _IP]),
 }
 
 _lib = None

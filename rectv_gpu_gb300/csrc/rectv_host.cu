@@ -613,6 +613,57 @@ struct Handle {
 
     void launch_axpy(float *y, const float *x, float a, long long count);
 
+    // ---- instrumentation ----
+    int jgroups() const { return (m + 15) / 16; }
+    void launch_counts(int *kern, int *ffts) const {
+        const int nimg = zb * m;
+        const int f2 = (nimg + img_per_fft - 1) / img_per_fft;
+        const int fwd_k = 3 + jgroups(), fwd_f = f2 + 1;
+        const int adj_k = 2 + (gd.n_split_tiles > 0 ? 1 : 0) + jgroups(), adj_f = 1 + f2;
+        *kern = titer * nbatch * (fwd_k + 1 + adj_k) + nbatch + 1;
+        *ffts = titer * nbatch * (fwd_f + adj_f);
+    }
+
+    void kernel_cost(int which, double *bytes, double *flops) const {
+        const double P = 2.0 * n;
+        const double npts = (double)ntheta * (n - 1) * zb;  // polar samples per launch
+        const int dpb = zb / nzp;
+        switch (which) {
+            case 0:  // gather: half-plane spectra in, complex rows out
+                *bytes = (double)zb * m * P * (P / 2 + 1) * 8.0 + (double)zb * ntheta * n * 8.0;
+                *flops = npts * (81.0 * 2.0 * m * 2.0 + 8.0 * m + 18.0 * 4.0);
+                break;
+            case 1:  // scatter: half row spectra in, full-plane grids out
+                *bytes = (double)zb * ntheta * (n / 2 + 1) * 8.0 + (double)zb * m * P * P * 8.0;
+                *flops = npts * (81.0 * 2.0 * m * 2.0 + 8.0 * m + 18.0 * 4.0);
+                break;
+            case 2:  // graddiv: u in, u out, psi and mu in
+                *bytes = (double)zb * slab * 8.0 + 2.0 * 4.0 * dpb * gp * 4.0;
+                *flops = (double)zb * slab * 60.0;
+                break;
+            default:  // shrink: u_cur, u_old in, mu in, psi and mu out
+                *bytes = (double)zb * slab * 8.0 + 3.0 * 4.0 * dpb * gp * 4.0;
+                *flops = (double)dpb * gp * 80.0;
+                break;
+        }
+    }
+
+    void launch_kernel(int which, int reps) {
+        check_live();
+        if (!session) throw Error(RECTV_ERR_STATE, "rectv_launch_kernel: needs a set-up session");
+        for (int r = 0; r < reps; ++r) {
+            switch (which) {
+                case 0: launch_gather_fwd(spec, rows, zb, gd, ug, stream); break;
+                case 1: launch_scatter_adj(rows, spec, zb, gd, ug, stream); break;
+                case 2: launch_graddiv(U[cur], U[cur], U[(cur + 1) % 3], psi, mu, rho_d, 0, nchunks, tv, stream); break;
+                case 3:  // overwrites the session's dual variables
+                    launch_shrink(U[cur], U[cur], psi, mu, rho_d, lambda0, 0, nchunks, tv, partials, stream);
+                    break;
+                default: throw Error(RECTV_ERR_ARG, "rectv_launch_kernel: unknown kernel id");
+            }
+        }
+    }
+
     void check_adjoints(double *res, const float *g_h, const float *theta_h, const float *phi_h,
                         float lambda1_, float center) {
         check_live();
@@ -894,6 +945,32 @@ int rectv_op_divergent(rectv_handle *h, float *d_fn, const float *d_h2, float la
         t.sd = (float)(1.0 / (4.0 * std::cbrt(2.0) * ((double)lambda1 / 2.0)));
         rectv::launch_divergent_ref(d_fn, d_h2, tau, t, H->stream);
         CUDA_CHECK(cudaStreamSynchronize(H->stream));
+    });
+}
+
+}  // extern "C"
+
+extern "C" {
+
+int rectv_launch_kernel(rectv_handle *h, int which, int reps) {
+    return guarded([&] { live(h)->launch_kernel(which, reps); });
+}
+
+int rectv_kernel_cost(rectv_handle *h, int which, double *bytes, double *flops) {
+    return guarded([&] {
+        if (!bytes || !flops) throw rectv::Error(RECTV_ERR_ARG, "rectv_kernel_cost: null output");
+        live(h)->kernel_cost(which, bytes, flops);
+    });
+}
+
+int rectv_get_launch_counts(rectv_handle *h, int *kernels, int *fft_execs, int *batch_slices) {
+    return guarded([&] {
+        rectv::Handle *H = live(h);
+        int k = 0, f = 0;
+        H->launch_counts(&k, &f);
+        if (kernels) *kernels = k;
+        if (fft_execs) *fft_execs = f;
+        if (batch_slices) *batch_slices = H->zb;
     });
 }
 
