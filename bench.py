@@ -1,0 +1,425 @@
+#!/usr/bin/env python
+"""Benchmark of the 4D time-resolved TV reconstruction (rectv::run hot path).
+
+Workload (one GPU): N=1024, Nz=64, Nzp=16, Ntheta=2880 over Nrot=8 half-turns,
+M=16 time samples, titer=4, lambda0=1e-3, lambda1=4, centre N/2; synthetic
+data = our forward operator applied to a seeded phantom of 10 moving
+ellipsoids plus 1% Gaussian noise.  One step = one outer ADMM iteration over
+the whole volume (titer forward/adjoint pairs, gradient-divergence steps,
+shrink, dual update, rho rule).
+
+  value  iterations/s with data resident in HBM (device-side session API),
+         timed with CUDA events on the library's stream.
+  e2e    iterations/s through the reference-facing C-ABI call rectv_run with
+         pinned host buffers: upload, set-up, K iterations, download.
+
+Usage: python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+For N > 1 launch with torch.distributed.run; every rank reconstructs its own
+volume (independent replicas, weak scaling).
+"""
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+WORKLOAD = dict(n=1024, nz=64, nzp=16, ntheta=2880, nrot=8, m=16, titer=4, lambda0=1e-3, lambda1=4.0)
+SMALL = dict(n=256, nz=16, nzp=8, ntheta=720, nrot=8, m=16, titer=4, lambda0=1e-3, lambda1=4.0)
+METRIC = "ADMM iters/s (outer iterations, titer=4) of the 4D TV reconstruction"
+KERNEL_NAMES = {0: "k_gather_fwd", 1: "k_scatter_adj", 2: "k_graddiv", 3: "k_shrink"}
+
+
+def workload_name(w):
+    return ("N=%(n)d Nz=%(nz)d Nzp=%(nzp)d Ntheta=%(ntheta)d Nrot=%(nrot)d M=%(m)d titer=%(titer)d" % w)
+
+
+def measured_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            p = json.load(f)
+        return float(p["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def ncu_traffic(kernel, wl):
+    """DRAM bytes per launch of `kernel` recorded from an ncu capture (profiles/)."""
+    try:
+        with open(os.path.join(ROOT, "profiles", "ncu_traffic.json")) as f:
+            d = json.load(f)
+        e = d.get(kernel, {}).get(wl)
+        return None if e is None else float(e)
+    except Exception:
+        return None
+
+
+# ---------------------------------------------------------------------------
+# clocks sampled during the timed region
+# ---------------------------------------------------------------------------
+class ClockSampler:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.out = open(self.path, "w")
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.FIELDS, "--format=csv,noheader",
+                 "-lms", "200"], stdout=self.out, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.out.close()
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        with open(self.path) as f:
+            for line in f:
+                p = [x.strip() for x in line.split(",")]
+                if len(p) < 9:
+                    continue
+                try:
+                    sm.append(float(p[1].split()[0]))
+                    mx.append(float(p[2].split()[0]))
+                except ValueError:
+                    continue
+                for nm, v in zip(names, p[5:9]):
+                    if v.lower().startswith("active"):
+                        reasons.add(nm)
+        os.unlink(self.path)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+# ---------------------------------------------------------------------------
+# synthetic input on the device
+# ---------------------------------------------------------------------------
+def phantom_device(torch, w, seed, device):
+    """phantom4d (rectv_gpu_gb300.phantom) evaluated on the GPU: same seeded
+    parameter draws, ellipsoids rasterised with torch."""
+    n, nz, m, ntheta = w["n"], w["nz"], w["m"], w["ntheta"]
+    rng = np.random.default_rng(seed)
+    x = torch.arange(n, dtype=torch.float32, device=device) - n / 2 + 0.5
+    z = torch.arange(nz, dtype=torch.float32, device=device) - nz / 2 + 0.5
+    u = torch.zeros((nz, m, n, n), dtype=torch.float32, device=device)
+    tj = (np.arange(m) * ntheta) // m
+    Y = x.view(1, n, 1)
+    X = x.view(1, 1, n)
+    Z = z.view(nz, 1, 1)
+    for _ in range(10):
+        c0 = np.array([rng.uniform(-0.3, 0.3) * nz, rng.uniform(-0.3, 0.3) * n, rng.uniform(-0.3, 0.3) * n])
+        ax = np.array([rng.uniform(0.05, 0.3) * nz, rng.uniform(0.05, 0.3) * n, rng.uniform(0.05, 0.3) * n])
+        ax = np.maximum(ax, 0.75)
+        dens = rng.uniform(0.1, 1.0)
+        ang = rng.uniform(0, np.pi)
+        direc = rng.normal(size=2)
+        direc /= np.linalg.norm(direc) + 1e-12
+        disp = direc * rng.uniform(0, 0.1 * n)
+        ca, sa = float(np.cos(ang)), float(np.sin(ang))
+        for j in range(m):
+            tau = tj[j] / ntheta
+            cy = float(c0[1] + tau * disp[0])
+            cx = float(c0[2] + tau * disp[1])
+            dy, dx = Y - cy, X - cx
+            ry = ca * dy - sa * dx
+            rx = sa * dy + ca * dx
+            inside = ((Z - float(c0[0])) / float(ax[0])) ** 2 + (ry / float(ax[1])) ** 2 + \
+                (rx / float(ax[2])) ** 2 <= 1.0
+            u[:, j] += dens * inside.to(torch.float32)
+    return u
+
+
+# ---------------------------------------------------------------------------
+# CPU baseline: the FP64 oracle on a bounded sample, extrapolated
+# ---------------------------------------------------------------------------
+def cpu_sample(w, angle_stride=30):
+    """Time one basis function of the oracle's fwdR and adjR for one slice on
+    every `angle_stride`-th angle, plus one slice of gradient/divergence, and
+    extrapolate to one outer ADMM iteration of the whole workload."""
+    import scipy.fft as sfft
+    from oracle import rectv_oracle as orc
+    n, ntheta, m, nz, titer = w["n"], w["ntheta"], w["m"], w["nz"], w["titer"]
+    theta = np.linspace(0, w["nrot"] * np.pi, ntheta, endpoint=False).astype(np.float32)
+    sub = theta[::angle_stride]
+    frac = ntheta / sub.size
+    U = orc.USFFT(n, sub, n / 2)
+    rng = np.random.default_rng(0)
+    f = rng.standard_normal((1, n, n)) + 0j
+    g = rng.standard_normal((1, sub.size, n)) + 0j
+    workers = os.cpu_count() or 1
+    with sfft.set_workers(workers):
+        orig_fft2, orig_ifft2 = np.fft.fft2, np.fft.ifft2
+        np.fft.fft2 = lambda a: sfft.fft2(a, workers=workers)
+        np.fft.ifft2 = lambda a: sfft.ifft2(a, workers=workers)
+        try:
+            t0 = time.perf_counter()
+            U.fwd(f)
+            t1 = time.perf_counter()
+            U.adj(g)
+            t2 = time.perf_counter()
+        finally:
+            np.fft.fft2, np.fft.ifft2 = orig_fft2, orig_ifft2
+    # split the measured times into the angle-proportional and fixed parts
+    P = 2 * n
+    a = rng.standard_normal((P, P)) + 0j
+    t3 = time.perf_counter()
+    sfft.fft2(a, workers=workers)
+    t4 = time.perf_counter()
+    tfft2 = t4 - t3
+    fwd = max(tfft2, t1 - t0)
+    adj = max(tfft2, t2 - t1)
+    per_slice_basis = 2 * tfft2 + (fwd - tfft2) * frac + (adj - tfft2) * frac
+    # gradient + divergence of one slice chunk (the TV part)
+    fm = rng.standard_normal((3, m, n, n))
+    t5 = time.perf_counter()
+    h = orc.gradient(fm, w["lambda1"], 0, 0)
+    orc.divergent(h, w["lambda1"], -0.5)
+    t6 = time.perf_counter()
+    tv_slice = t6 - t5
+    t_iter = titer * nz * (m * per_slice_basis + tv_slice) + nz * tv_slice
+    sample = ("FP64 oracle: fwdR+adjR of 1 slice x 1 basis on %d of %d angles (+ one 2048^2 FFT pair), "
+              "gradient/divergence of 1 slice; extrapolated x%d bases x%d slices x%d inner steps"
+              % (sub.size, ntheta, m, nz, titer))
+    return 1.0 / t_iter, t6 - t0 + (t4 - t3), sample, workers
+
+
+def run_reference_arm(args, rank):
+    """--impl reference: the reference's algorithm (FP64 oracle restatement; the
+    reference has no CPU path and its CUDA build cannot travel) on host cores."""
+    if rank != 0:
+        return 0
+    w = SMALL if args.small else WORKLOAD
+    for _ in range(args.warmup):
+        cpu_sample(w)
+    vals, secs = [], 0.0
+    for _ in range(args.steps):
+        v, s, sample, workers = cpu_sample(w)
+        vals.append(v)
+        secs += s
+    value = statistics.median(vals)
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": "iter/s", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 / value, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": workload_name(w), "kind": "cpu oracle sample, extrapolated"},
+        "cpu_baseline": {"value": value, "unit": "iter/s", "cores": workers, "kind": "port", "sample": sample},
+        "e2e": {"value": value, "unit": "iter/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+    return 0
+
+
+# ---------------------------------------------------------------------------
+# our arm
+# ---------------------------------------------------------------------------
+def run_ours(args, rank, world, local_rank):
+    import torch
+
+    import __graft_entry__
+    __graft_entry__.build()
+    from rectv_gpu_gb300 import rectv, takephi
+    from rectv_gpu_gb300 import _lib
+    from rectv_gpu_gb300.phantom import scan_angles
+
+    torch.cuda.set_device(local_rank)
+    dev = torch.device("cuda", local_rank)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=dev)
+
+    w = SMALL if args.small else WORKLOAD
+    n, nz, nzp, ntheta, m, titer = w["n"], w["nz"], w["nzp"], w["ntheta"], w["m"], w["titer"]
+    lam0, lam1 = w["lambda0"] * w["lambda1"], w["lambda1"]
+    center = n / 2
+    theta = scan_angles(ntheta, w["nrot"])
+    phi = takephi(ntheta, m)
+
+    obj = rectv(n, ntheta, m, nz, nzp, 1)
+    obj.set_verbose(False)
+    lib = _lib.load()
+    stream = torch.cuda.ExternalStream(obj.stream, device=dev)
+
+    # synthetic data: phantom -> our forward operator -> +1% noise
+    d_theta = torch.from_numpy(theta).to(dev)
+    d_phi = torch.from_numpy(phi).to(dev)
+    u = phantom_device(torch, w, seed=rank, device=dev)
+    d_g = torch.empty((nz, ntheta, n), dtype=torch.float32, device=dev)
+    torch.cuda.synchronize()
+    obj.op_set_geometry(d_theta.data_ptr(), d_phi.data_ptr(), center)
+    obj.op_radonapr(d_g.data_ptr(), u.data_ptr(), nz, 1.0)
+    gen = torch.Generator(device=dev).manual_seed(1000 + rank)
+    sigma = 0.01 * float(d_g.abs().max())
+    d_g += sigma * torch.randn(d_g.shape, generator=gen, device=dev)
+    del u
+    torch.cuda.synchronize()
+
+    # ---- device-resident timed region ----
+    obj.setup_device(d_g.data_ptr(), d_theta.data_ptr(), d_phi.data_ptr(), center, lam0, lam1, titer)
+    obj.iterate(args.warmup)
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    sampler = ClockSampler(local_rank)
+    sampler.start()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    obj.iterate(args.steps)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    clocks = sampler.stop()
+    ms = e0.elapsed_time(e1)
+    if dist:
+        t = torch.tensor([ms], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+        dist.barrier()
+    hist = obj.history()
+
+    kern = ctypes_int()
+    ffts = ctypes_int()
+    zbs = ctypes_int()
+    _lib.check(lib.rectv_get_launch_counts(obj._h, kern[1], ffts[1], zbs[1]))
+    launches_per_iter = kern[0].value
+
+    # ---- per-kernel timing (roofline of the dominant kernel) ----
+    import ctypes
+    reps = 3
+    ktimes = {}
+    for kid in (0, 1, 2, 3):
+        lib.rectv_launch_kernel(obj._h, kid, 1)  # warm
+        a = torch.cuda.Event(enable_timing=True)
+        b = torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        a.record(stream)
+        _lib.check(lib.rectv_launch_kernel(obj._h, kid, reps))
+        b.record(stream)
+        torch.cuda.synchronize()
+        ktimes[kid] = a.elapsed_time(b) / reps
+    # launches per outer iteration of each kernel: titer*nbatch (0,1,2), nbatch (3)
+    nbatch = nz // zbs[0].value if zbs[0].value else 1
+    share = {0: titer * nbatch * ktimes[0], 1: titer * nbatch * ktimes[1], 2: titer * nbatch * ktimes[2],
+             3: nbatch * ktimes[3]}
+    dom = max(share, key=share.get)
+    bytes_ = ctypes.c_double()
+    flops = ctypes.c_double()
+    _lib.check(lib.rectv_kernel_cost(obj._h, dom, ctypes.byref(bytes_), ctypes.byref(flops)))
+    peak, peak_kind = measured_peaks()
+    achieved = bytes_.value / (ktimes[dom] * 1e-3) / 1e9
+    roofline = {"bound": "hbm", "kernel": KERNEL_NAMES[dom], "achieved": achieved, "peak": peak,
+                "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / peak,
+                "traffic": ncu_traffic(KERNEL_NAMES[dom], workload_name(w)),
+                "algorithmic_bytes": bytes_.value, "fp32_tflops": flops.value / (ktimes[dom] * 1e-3) / 1e12,
+                "ms_per_launch": ktimes[dom],
+                "per_iteration_ms": {KERNEL_NAMES[k]: share[k] for k in share}}
+
+    # ---- end-to-end through rectv_run with pinned host buffers ----
+    g_h = torch.empty((nz, ntheta, n), dtype=torch.float32, pin_memory=True)
+    g_h.copy_(d_g.cpu())
+    th_h = torch.from_numpy(theta).pin_memory()
+    ph_h = torch.from_numpy(phi).pin_memory()
+    f_h = torch.empty((nz, m, n, n), dtype=torch.float32, pin_memory=True)
+    del d_g
+    if dist:
+        dist.barrier()
+    t0 = time.perf_counter()
+    obj.run(f_h.data_ptr(), g_h.data_ptr(), th_h.data_ptr(), ph_h.data_ptr(), center, lam0, lam1, args.steps,
+            titer)
+    t1 = time.perf_counter()
+    e2e_s = t1 - t0
+    if dist:
+        t = torch.tensor([e2e_s], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_s = float(t.item())
+    h2d = g_h.numel() * 4 + th_h.numel() * 4 + ph_h.numel() * 4
+    d2h = f_h.numel() * 4
+    finite = bool(np.isfinite(f_h[:, :, ::64, ::64].numpy()).all())
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu:
+        v, s, sample, workers = cpu_sample(w)
+        cpu = {"value": v, "unit": "iter/s", "cores": workers, "kind": "port", "sample": sample}
+
+    value = world * args.steps / (ms * 1e-3)
+    voxels = float(n) * n * m * nz
+    line = {
+        "metric": METRIC, "value": value, "unit": "iter/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic: 10 moving ellipsoids, forward-projected with this library + 1% Gaussian noise",
+        "config": {"workload": workload_name(w), "lambda0": w["lambda0"], "lambda1": lam1, "center": center,
+                   "chunks": nz // nzp, "batch_slices": zbs[0].value,
+                   "l2": "inputs larger than L2 (iterate 4.3 GB, dual variables 2x19 GB)",
+                   "parallelism": "replicas" if world > 1 else "single"},
+        "voxel_updates_per_s": value * voxels,
+        "e2e": {"value": world * args.steps / e2e_s, "unit": "iter/s", "h2d_bytes_per_step": h2d / args.steps,
+                "d2h_bytes_per_step": d2h / args.steps, "seconds": e2e_s, "api": "rectv_run (C ABI)"},
+        "roofline": roofline,
+        "cpu_baseline": cpu,
+        "clocks": clocks,
+        "gpu_launches": launches_per_iter * args.steps,
+        "cufft_execs": ffts[0].value * args.steps,
+        "rho_final": float(hist["rho"][-1]) if len(hist["rho"]) else None,
+        "result_finite": finite,
+    }
+    obj.free()
+    if rank == 0:
+        print(json.dumps(line))
+    if dist:
+        dist.destroy_process_group()
+    return 0
+
+
+def ctypes_int():
+    import ctypes
+    v = ctypes.c_int(0)
+    return v, ctypes.byref(v)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--small", action="store_true", help="N=256 workload (quick check)")
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
+    args = ap.parse_args()
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+    if args.impl == "reference":
+        return run_reference_arm(args, rank)
+    return run_ours(args, rank, world, local_rank)
+
+
+if __name__ == "__main__":
+    sys.exit(main())
