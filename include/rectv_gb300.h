@@ -143,6 +143,38 @@ int rectv_kernel_cost(rectv_handle *h, int which, double *bytes, double *flops);
 int rectv_get_launch_counts(rectv_handle *h, int *kernels, int *fft_execs, int *batch_slices);
 
 /* ---------------------------------------------------------------------------
+ * Allocation-free entry point (no counterpart in the reference).
+ *
+ * For callers that cannot let a library allocate device memory -- an
+ * application that owns the whole device budget through its own pool and
+ * passes in only its own buffers, or a processing loop that must not stall,
+ * since cudaMalloc/cudaFree can synchronise the device and can fail at run
+ * time when memory is fragmented.  It needs no handle and calls no
+ * cudaMalloc, cudaFree or allocating library routine.
+ *
+ * One end-of-iteration ADMM shrink step (solve_reg_ker, the mu update and the
+ * two residual norms of admm.cu:101-117, as rectv_iterate runs it) over
+ * nchunks chunks of nzp slices, queued on `stream` (a cudaStream_t, or NULL):
+ *   d_u_cur, d_u_old  [nchunks*nzp][m][n][n]  iterate after the inner steps,
+ *                     and the previous outer iterate (source of the z-halo)
+ *   d_psi (out), d_mu (in/out)  [4][nchunks][nzp+1][m+1][n+1][n+1]
+ *   d_sums (out)      device double[3]: sum |grad u_cur - psi|^2,
+ *                     sum |grad u_old - grad u_cur|^2, sum (u_cur - u_old)^2
+ * Its only scratch (FP64 per-block partial sums and the rho value) is a fixed
+ * static device array of 1.5 MiB that every GPU loading this library holds
+ * until the process exits.  Limit: ceil((n+1)/32)*ceil((n+1)/8)*nchunks*
+ * (nzp+1)*(m+1) <= 65536 thread blocks (e.g. n=256, m=16, nzp=8, nchunks=1);
+ * larger problems are rejected with RECTV_ERR_ARG.  The first call on a
+ * device looks up the array's device address, so make that first call before
+ * any stream capture.  All calls share the array, which keeps the last call's
+ * contents; each call writes every entry it reads before reading it, so
+ * nothing needs clearing.  Calls that can run at the same time on one device
+ * (for example on different streams) race on the array. */
+int rectv_shrink_noalloc(const float *d_u_cur, const float *d_u_old, float *d_psi, float *d_mu, int n,
+                         int m, int nzp, int nchunks, float rho, float lambda0, float lambda1,
+                         double *d_sums, void *stream);
+
+/* ---------------------------------------------------------------------------
  * Operator-level entry points (device pointers), the reference's private
  * operators exposed for parity testing.  rectv_op_set_geometry must be called
  * first; it uploads theta/phi and the rotation centre.

@@ -21,6 +21,7 @@
 #include <cstdlib>
 #include <cstring>
 #include <memory>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -975,3 +976,119 @@ int rectv_get_launch_counts(rectv_handle *h, int *kernels, int *fft_execs, int *
 }
 
 }  // extern "C"
+
+// ===========================================================================
+// Allocation-free ADMM shrink step.
+//
+// Some callers cannot let a library allocate device memory: an application
+// that owns the whole device budget through its own pool and hands this code
+// only its buffers, or a processing loop that must not stall, since
+// cudaMalloc/cudaFree can synchronise the device and can fail at run time
+// when memory is fragmented.  rectv_shrink_noalloc serves them: the caller
+// passes every input and output, and the only scratch (the FP64 per-block
+// partial sums of the residual norms, and the rho value the kernel reads from
+// device memory) lives in the file-scope array below, which every GPU that
+// loads this library holds until the process exits.
+// ===========================================================================
+namespace rectv {
+namespace {
+
+// At most this many thread blocks per call: 3 doubles of partial sums each.
+constexpr int kNoAllocMaxBlocks = 65536;
+constexpr int kNoAllocRhoSlot = 3 * kNoAllocMaxBlocks;  // one double slot holds rho
+static __device__ __align__(256) double g_noalloc_scratch[3 * kNoAllocMaxBlocks + 2];
+
+constexpr int kNoAllocMaxDevices = 256;
+std::mutex g_noalloc_mu;
+double *g_noalloc_ptr[kNoAllocMaxDevices] = {};
+
+// Device address of g_noalloc_scratch on the current device.  The first call
+// on a device looks it up (host code cannot use the symbol itself as a device
+// address); that first call should therefore come before any stream capture.
+double *noalloc_scratch() {
+    int dev = 0;
+    CUDA_CHECK(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= kNoAllocMaxDevices) throw Error(RECTV_ERR_ARG, "rectv_shrink_noalloc: device ordinal out of range");
+    std::lock_guard<std::mutex> lk(g_noalloc_mu);
+    if (!g_noalloc_ptr[dev]) {
+        void *p = nullptr;
+        const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+        if (e != cudaSuccess || !p)
+            throw Error(RECTV_ERR_CUDA, std::string("rectv_shrink_noalloc: cudaGetSymbolAddress failed: ") +
+                                            cudaGetErrorString(e));
+        g_noalloc_ptr[dev] = static_cast<double *>(p);
+    }
+    return g_noalloc_ptr[dev];
+}
+
+__global__ void k_noalloc_set_rho(float *dst, float rho) { *dst = rho; }
+
+// Fixed-order FP64 sum of the partials (same order as k_reduce_rho).
+__global__ void k_noalloc_sum3(const double *__restrict__ partials, int nparts, double *out) {
+    __shared__ double sh[3][256];
+    double a = 0, b = 0, c = 0;
+    for (int i = threadIdx.x; i < nparts; i += blockDim.x) {
+        a += partials[3 * i];
+        b += partials[3 * i + 1];
+        c += partials[3 * i + 2];
+    }
+    sh[0][threadIdx.x] = a;
+    sh[1][threadIdx.x] = b;
+    sh[2][threadIdx.x] = c;
+    __syncthreads();
+    for (int o = 128; o > 0; o >>= 1) {
+        if ((int)threadIdx.x < o) {
+            sh[0][threadIdx.x] += sh[0][threadIdx.x + o];
+            sh[1][threadIdx.x] += sh[1][threadIdx.x + o];
+            sh[2][threadIdx.x] += sh[2][threadIdx.x + o];
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        out[0] = sh[0][0];
+        out[1] = sh[1][0];
+        out[2] = sh[2][0];
+    }
+}
+
+}  // namespace
+}  // namespace rectv
+
+extern "C" int rectv_shrink_noalloc(const float *d_u_cur, const float *d_u_old, float *d_psi, float *d_mu, int n,
+                                    int m, int nzp, int nchunks, float rho, float lambda0, float lambda1,
+                                    double *d_sums, void *stream) {
+    return guarded([&] {
+        if (!d_u_cur || !d_u_old || !d_psi || !d_mu || !d_sums)
+            throw rectv::Error(RECTV_ERR_ARG, "rectv_shrink_noalloc: null pointer");
+        if (n < 2 || m < 1 || nzp < 1 || nchunks < 1)
+            throw rectv::Error(RECTV_ERR_ARG, "rectv_shrink_noalloc: n>=2, m>=1, nzp>=1, nchunks>=1 required");
+        if (!(rho > 0.f)) throw rectv::Error(RECTV_ERR_ARG, "rectv_shrink_noalloc: rho must be positive");
+        rectv::TvGeo t{};
+        t.n = n;
+        t.m = m;
+        t.nzp = nzp;
+        t.nchunks = nchunks;
+        t.vol_slab = (long long)n * n * m;
+        t.gp = (long long)(n + 1) * (n + 1) * (m + 1) * (nzp + 1);
+        t.comp_stride = (long long)nchunks * t.gp;
+        t.lambda1 = lambda1;
+        t.sg = (float)(1.0 / (2.0 * std::cbrt(2.0) * ((double)lambda1 / 2.0)));
+        t.sd = (float)(1.0 / (4.0 * std::cbrt(2.0) * ((double)lambda1 / 2.0)));
+        const long long nblocks = (long long)((n + 1 + 31) / 32) * ((n + 1 + 7) / 8) * nchunks * (nzp + 1) * (m + 1);
+        if (nblocks > rectv::kNoAllocMaxBlocks)
+            throw rectv::Error(RECTV_ERR_ARG,
+                               "rectv_shrink_noalloc: problem needs " + std::to_string(nblocks) +
+                                   " thread blocks; the static scratch holds at most " +
+                                   std::to_string(rectv::kNoAllocMaxBlocks) +
+                                   " (ceil((n+1)/32)*ceil((n+1)/8)*nchunks*(nzp+1)*(m+1))");
+        double *scratch = rectv::noalloc_scratch();
+        float *rho_d = reinterpret_cast<float *>(scratch + rectv::kNoAllocRhoSlot);
+        cudaStream_t s = static_cast<cudaStream_t>(stream);
+        rectv::k_noalloc_set_rho<<<1, 1, 0, s>>>(rho_d, rho);
+        LAUNCH_CHECK("k_noalloc_set_rho");
+        const int nparts = rectv::launch_shrink(d_u_cur, d_u_old, d_psi, d_mu, rho_d, lambda0, 0, nchunks, t,
+                                                scratch, s);
+        rectv::k_noalloc_sum3<<<1, 256, 0, s>>>(scratch, nparts, d_sums);
+        LAUNCH_CHECK("k_noalloc_sum3");
+    });
+}
