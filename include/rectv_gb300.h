@@ -163,7 +163,7 @@ int rectv_get_launch_counts(rectv_handle *h, int *kernels, int *fft_execs, int *
  * Its only scratch (FP64 per-block partial sums and the rho value) is a fixed
  * static device array of 1.5 MiB that every GPU loading this library holds
  * until the process exits.  Limit: ceil((n+1)/32)*ceil((n+1)/8)*nchunks*
- * (nzp+1)*(m+1) <= 65536 thread blocks (e.g. n=256, m=16, nzp=8, nchunks=1);
+ * (nzp+1) <= 65536 thread blocks (e.g. n=1024, nzp=8, nchunks=1, any m);
  * larger problems are rejected with RECTV_ERR_ARG.  The first call on a
  * device looks up the array's device address, so make that first call before
  * any stream capture.  All calls share the array, which keeps the last call's

@@ -115,6 +115,9 @@ HostPlan build_plan(const float *theta, int n, int ntheta, int T, int fwd_cap, i
         for (int st = 0; st < c; st += adj_cap)
             p.adj_items.push_back(make_int4(t, (int)(aoff[t] + st), std::min(adj_cap, c - st), split));
     }
+    // heaviest tiles first, so that they do not finish last
+    std::stable_sort(p.adj_items.begin(), p.adj_items.end(),
+                     [](const int4 &a, const int4 &b) { return a.z > b.z; });
     return p;
 }
 

@@ -95,6 +95,7 @@ struct Handle {
     float2 *spec = nullptr;
     float2 *rows = nullptr;
     double *partials = nullptr;
+    double *stage1 = nullptr;
     int nparts_batch = 0;
     double *dot_part = nullptr;
     double *dot_out = nullptr;
@@ -206,6 +207,7 @@ struct Handle {
         partials = dalloc<double>((size_t)3 * nparts_batch * nbatch, owned);
         dot_part = dalloc<double>((size_t)dot_parts(), owned);
         dot_out = dalloc<double>(8, owned);
+        stage1 = dalloc<double>((size_t)3 * reduce_stage1_parts(), owned);
         rho_d = dalloc<float>(1, owned);
         iter_ctr = dalloc<int>(1, owned);
         gd.err = dalloc<int>(1, owned);
@@ -322,7 +324,9 @@ struct Handle {
     void set_geometry(const float *theta_h, const float *phi_h, float center) {
         drop_graphs();
         free_geo();
-        HostPlan hp = build_plan(theta_h, n, ntheta, ug.T, 256, 256);
+        // gather items hold at most one sample table; scatter items are whole
+        // tiles (one block owns each tile, so tiles are stored, never added)
+        HostPlan hp = build_plan(theta_h, n, ntheta, ug.T, table_capacity(), 1 << 30);
         auto up = [&](const void *src, size_t bytes) -> void * {
             void *p = nullptr;
             CUDA_CHECK(cudaMalloc(&p, std::max<size_t>(bytes, 16)));
@@ -432,7 +436,7 @@ struct Handle {
             launch_shrink(U[src], U[old], psi, mu, rho_d, lambda0, bb * dpb, nchunks, tv,
                           partials + (size_t)3 * nparts_batch * bb, stream);
         }
-        launch_reduce_rho(partials, nparts_batch * nbatch, rho_d, stats, iter_ctr, stats_cap, stream);
+        launch_reduce_rho(partials, nparts_batch * nbatch, stage1, rho_d, stats, iter_ctr, stats_cap, stream);
     }
 
     int next_cur(int old) const {
@@ -1074,13 +1078,13 @@ extern "C" int rectv_shrink_noalloc(const float *d_u_cur, const float *d_u_old, 
         t.lambda1 = lambda1;
         t.sg = (float)(1.0 / (2.0 * std::cbrt(2.0) * ((double)lambda1 / 2.0)));
         t.sd = (float)(1.0 / (4.0 * std::cbrt(2.0) * ((double)lambda1 / 2.0)));
-        const long long nblocks = (long long)((n + 1 + 31) / 32) * ((n + 1 + 7) / 8) * nchunks * (nzp + 1) * (m + 1);
+        const long long nblocks = (long long)rectv::shrink_blocks(t, nchunks);
         if (nblocks > rectv::kNoAllocMaxBlocks)
             throw rectv::Error(RECTV_ERR_ARG,
                                "rectv_shrink_noalloc: problem needs " + std::to_string(nblocks) +
                                    " thread blocks; the static scratch holds at most " +
                                    std::to_string(rectv::kNoAllocMaxBlocks) +
-                                   " (ceil((n+1)/32)*ceil((n+1)/8)*nchunks*(nzp+1)*(m+1))");
+                                   " (ceil((n+1)/32)*ceil((n+1)/8)*nchunks*(nzp+1))");
         double *scratch = rectv::noalloc_scratch();
         float *rho_d = reinterpret_cast<float *>(scratch + rectv::kNoAllocRhoSlot);
         cudaStream_t s = static_cast<cudaStream_t>(stream);

@@ -99,6 +99,7 @@ void launch_crop_accum(const float2 *spec, float *u, int zb, float tau, const fl
 size_t gather_fwd_smem(const UsGeo &g);
 size_t scatter_adj_smem(const UsGeo &g);
 void usfft_prepare();  // kernel attributes; call once, outside stream capture
+int table_capacity();  // samples per gather work item
 
 // ---- TV / ADMM kernel launchers (tv_kernels.cu) ----
 struct TvGeo {
@@ -121,8 +122,10 @@ int launch_shrink(const float *u_cur, const float *u_old, float *psi, float *mu,
                   cudaStream_t s);
 int shrink_blocks(const TvGeo &t, int nchunks);
 // sum partials in fixed order, apply the rho rule, append a stats row at *ctr
-void launch_reduce_rho(const double *partials, int nparts, float *rho, double *stats, int *ctr,
+// (two fixed-order stages; stage1 holds 3*reduce_stage1_parts() doubles)
+void launch_reduce_rho(const double *partials, int nparts, double *stage1, float *rho, double *stats, int *ctr,
                        int cap, cudaStream_t s);
+int reduce_stage1_parts();
 // reference-layout gradient / divergence for the operator API and check_adjoints
 // fm points at slab zbase-1 of the extended chunk (zbase = 1 when fm holds
 // the two halo slabs, 0 when it holds the chunk only and flgl = flgr = 0)

@@ -22,28 +22,6 @@ namespace rectv {
 
 namespace {
 
-struct ChunkView {
-    const float *u;     // current iterate, global [z][t][y][x]
-    const float *uold;  // previous outer iterate (halo source)
-    int n, m, nzp, c, nch;
-    long long slab;     // n*n*m
-};
-
-// Value of the extended chunk at voxel coordinates (x,y,t) in [0,n)x[0,n)x[0,m)
-// and chunk-local slice zl in [-1, nzp] (extendf, kernels_operators.cuh:14-19).
-__device__ __forceinline__ float ext_val(const ChunkView &v, int x, int y, int t, int zl) {
-    const long long inplane = ((long long)t * v.n + y) * v.n + x;
-    const long long z0 = (long long)v.c * v.nzp;
-    if (zl < 0) {
-        if (v.c > 0) return v.uold[(z0 - 1) * v.slab + inplane];
-        zl = 0;
-    } else if (zl >= v.nzp) {
-        if (v.c < v.nch - 1) return v.uold[(z0 + v.nzp) * v.slab + inplane];
-        zl = v.nzp - 1;
-    }
-    return v.u[(z0 + zl) * v.slab + inplane];
-}
-
 __device__ __forceinline__ int clampi(int a, int lo, int hi) { return a < lo ? lo : (a > hi ? hi : a); }
 
 template <int NW>
@@ -150,8 +128,10 @@ void launch_graddiv(const float *u_in, const float *u_old, float *u_out, const f
 // End of outer iteration for one chunk (admm.cu:101-117):
 //   h = G u_cur, ho = G u_old (the reference's h2stored),
 //   psi = shrink(h + mu/rho, lambda0/rho), mu += rho h - rho psi,
-//   partial sums of |h-psi|^2, |ho-h|^2 and, for q >= 1, (u_cur-u_old)^2.
-// One thread per dual grid point, blocks of 32x8 over (qx, qy).
+//   sums of |h-psi|^2, |ho-h|^2 and, for q >= 1, (u_cur-u_old)^2.
+// One thread per (qx, qy, qz) marching along qt; the squares of one grid point
+// are summed in FP32 and accumulated across points in FP64; one FP64 partial
+// triple per block.  Blocks of 32x8 over (qx, qy), grid.z over (chunk, qz).
 // ---------------------------------------------------------------------------
 __global__ void __launch_bounds__(256)
     k_shrink(const float *__restrict__ ucur, const float *__restrict__ uold, float *__restrict__ psi,
@@ -159,56 +139,67 @@ __global__ void __launch_bounds__(256)
              int nch_total, double *__restrict__ partials) {
     const int qx = blockIdx.x * blockDim.x + threadIdx.x;
     const int qy = blockIdx.y * blockDim.y + threadIdx.y;
-    const int pl = blockIdx.z;
     const int n = t.n, m = t.m, nzp = t.nzp;
-    const int qt = pl % (m + 1);
-    const int cz = pl / (m + 1);
-    const int qz = cz % (nzp + 1);
-    const int c = c0 + cz / (nzp + 1);
+    const int qz = blockIdx.z % (nzp + 1);
+    const int c = c0 + blockIdx.z / (nzp + 1);
     double a0 = 0.0, a1 = 0.0, a2 = 0.0;
     if (qx <= n && qy <= n) {
-        ChunkView vc{ucur, uold, n, m, nzp, c, nch_total, t.vol_slab};
-        ChunkView vo{uold, uold, n, m, nzp, c, nch_total, t.vol_slab};
+        const long long slab = t.vol_slab, nn = (long long)n * n;
+        const long long zc = (long long)c * nzp;
+        // extended-chunk slabs at z0 = qz-1 and z1 = qz (extendf, kernels_operators.cuh:14-19)
+        auto slab_of = [&](const float *u, int zl) -> const float * {
+            if (zl < 0) return (c > 0) ? uold + (zc - 1) * slab : u + zc * slab;
+            if (zl >= nzp) return (c < nch_total - 1) ? uold + (zc + nzp) * slab : u + (zc + nzp - 1) * slab;
+            return u + (zc + zl) * slab;
+        };
+        const float *c0p = slab_of(ucur, qz - 1), *c1p = slab_of(ucur, qz);
+        const float *o0p = slab_of(uold, qz - 1), *o1p = slab_of(uold, qz);
         const int x0 = clampi(qx - 1, 0, n - 1), x1 = clampi(qx, 0, n - 1);
         const int y0 = clampi(qy - 1, 0, n - 1), y1 = clampi(qy, 0, n - 1);
-        const int t0 = clampi(qt - 1, 0, m - 1), t1 = clampi(qt, 0, m - 1);
-        const int z0 = qz - 1, z1 = qz;
+        const long long p00 = (long long)y0 * n + x0, px = (long long)y0 * n + x1, py = (long long)y1 * n + x0;
+        const bool inner_xyz = (qx >= 1 && qy >= 1 && qz >= 1);
         const float sg = t.sg, sgt = t.sg * t.lambda1;
-        const float fc = ext_val(vc, x0, y0, t0, z0);
-        float h[4] = {sg * (ext_val(vc, x1, y0, t0, z0) - fc), sg * (ext_val(vc, x0, y1, t0, z0) - fc),
-                      sgt * (ext_val(vc, x0, y0, t1, z0) - fc), sg * (ext_val(vc, x0, y0, t0, z1) - fc)};
-        const float fo = ext_val(vo, x0, y0, t0, z0);
-        float ho[4] = {sg * (ext_val(vo, x1, y0, t0, z0) - fo), sg * (ext_val(vo, x0, y1, t0, z0) - fo),
-                       sgt * (ext_val(vo, x0, y0, t1, z0) - fo), sg * (ext_val(vo, x0, y0, t0, z1) - fo)};
         const float rho = *rhop;
-        const long long q = (long long)c * t.gp + (((long long)qz * (m + 1) + qt) * (n + 1) + qy) * (n + 1) + qx;
-        const long long cs = t.comp_stride;
-        float mv[4], ps[4];
-        float za2 = 0.f;
-#pragma unroll
-        for (int i = 0; i < 4; ++i) {
-            mv[i] = mu[i * cs + q];
-            ps[i] = h[i] + mv[i] / rho;  // solve_reg_ker, admm.cu:49-52
-            za2 += ps[i] * ps[i];
-        }
-        const float za = sqrtf(za2);
         const float thr = lambda0 / rho;
+        const long long cs = t.comp_stride;
+        long long q = (long long)c * t.gp + ((long long)qz * (m + 1)) * (n + 1) * (n + 1) + (long long)qy * (n + 1) + qx;
+        const long long st = (long long)(n + 1) * (n + 1);
+        float fc = c0p[p00], fo = o0p[p00];  // values at (x0, y0, t0 = clamp(qt-1) = 0, z0)
+        for (int qt = 0; qt <= m; ++qt) {
+            const long long o0 = (long long)(qt > 0 ? qt - 1 : 0) * nn;  // t0 = clamp(qt-1)
+            const long long o1 = (long long)(qt < m ? qt : m - 1) * nn;  // t1 = clamp(qt)
+            const float fcx = c0p[o0 + px], fcy = c0p[o0 + py], fct = c0p[o1 + p00], fcz = c1p[o0 + p00];
+            const float fox = o0p[o0 + px], foy = o0p[o0 + py], fot = o0p[o1 + p00], foz = o1p[o0 + p00];
+            const float h[4] = {sg * (fcx - fc), sg * (fcy - fc), sgt * (fct - fc), sg * (fcz - fc)};
+            const float ho[4] = {sg * (fox - fo), sg * (foy - fo), sgt * (fot - fo), sg * (foz - fo)};
+            float mv[4], ps[4];
+            float za2 = 0.f;
 #pragma unroll
-        for (int i = 0; i < 4; ++i) {
-            ps[i] = (za <= thr) ? 0.f : ps[i] - thr * ps[i] / za;
-            const float mn = mv[i] + rho * h[i] - rho * ps[i];  // lin4(mu,h2,psi,1,rho,-rho)
-            psi[i * cs + q] = ps[i];
-            mu[i * cs + q] = mn;
-            const double dr = (double)h[i] - (double)ps[i];
-            const double ds = (double)ho[i] - (double)h[i];
-            a0 += dr * dr;
-            a1 += ds * ds;
-        }
-        if (qx >= 1 && qy >= 1 && qt >= 1 && qz >= 1) {
-            const long long vv = ((long long)c * nzp + (qz - 1)) * t.vol_slab +
-                                 ((long long)(qt - 1) * n + (qy - 1)) * n + (qx - 1);
-            const double dd = (double)ucur[vv] - (double)uold[vv];
-            a2 = dd * dd;
+            for (int i = 0; i < 4; ++i) {
+                mv[i] = mu[i * cs + q];
+                ps[i] = h[i] + mv[i] / rho;  // solve_reg_ker, admm.cu:49-52
+                za2 += ps[i] * ps[i];
+            }
+            const float za = sqrtf(za2);
+            float r2 = 0.f, s2 = 0.f;
+#pragma unroll
+            for (int i = 0; i < 4; ++i) {
+                ps[i] = (za <= thr) ? 0.f : ps[i] - thr * ps[i] / za;
+                psi[i * cs + q] = ps[i];
+                mu[i * cs + q] = mv[i] + rho * h[i] - rho * ps[i];  // lin4(mu,h2,psi,1,rho,-rho)
+                const float dr = h[i] - ps[i], ds = ho[i] - h[i];
+                r2 += dr * dr;
+                s2 += ds * ds;
+            }
+            a0 += (double)r2;
+            a1 += (double)s2;
+            if (inner_xyz && qt >= 1) {  // voxel q-1 = (x0, y0, t0, z0) inside the chunk
+                const double dd = (double)fc - (double)fo;
+                a2 += dd * dd;
+            }
+            fc = fct;
+            fo = fot;
+            q += st;
         }
     }
     const long long bid = ((long long)blockIdx.z * gridDim.y + blockIdx.y) * gridDim.x + blockIdx.x;
@@ -216,13 +207,13 @@ __global__ void __launch_bounds__(256)
 }
 
 int shrink_blocks(const TvGeo &t, int nchunks) {
-    return ((t.n + 1 + 31) / 32) * ((t.n + 1 + 7) / 8) * nchunks * (t.nzp + 1) * (t.m + 1);
+    return ((t.n + 1 + 31) / 32) * ((t.n + 1 + 7) / 8) * nchunks * (t.nzp + 1);
 }
 
 int launch_shrink(const float *u_cur, const float *u_old, float *psi, float *mu, const float *rho,
                   float lambda0, int c0, int nchunks_total, const TvGeo &t, double *partials,
                   cudaStream_t s) {
-    dim3 bs(32, 8), gs((t.n + 1 + 31) / 32, (t.n + 1 + 7) / 8, t.nchunks * (t.nzp + 1) * (t.m + 1));
+    dim3 bs(32, 8), gs((t.n + 1 + 31) / 32, (t.n + 1 + 7) / 8, t.nchunks * (t.nzp + 1));
     k_shrink<<<gs, bs, 0, s>>>(u_cur, u_old, psi, mu, rho, lambda0, t, c0, nchunks_total, partials);
     LAUNCH_CHECK("k_shrink");
     return (int)(gs.x * gs.y * gs.z);
@@ -274,9 +265,43 @@ __global__ void k_reduce_rho(const double *__restrict__ partials, int nparts, fl
     }
 }
 
-void launch_reduce_rho(const double *partials, int nparts, float *rho, double *stats, int *ctr,
+// First stage: block b sums its contiguous share of the partials, in order.
+__global__ void k_sum_stage1(const double *__restrict__ partials, int nparts, double *__restrict__ out) {
+    __shared__ double sh[3][256];
+    const int per = (nparts + gridDim.x - 1) / gridDim.x;
+    const int lo = blockIdx.x * per, hi = min(nparts, lo + per);
+    double a = 0, b = 0, c = 0;
+    for (int i = lo + threadIdx.x; i < hi; i += blockDim.x) {
+        a += partials[3 * i];
+        b += partials[3 * i + 1];
+        c += partials[3 * i + 2];
+    }
+    sh[0][threadIdx.x] = a;
+    sh[1][threadIdx.x] = b;
+    sh[2][threadIdx.x] = c;
+    __syncthreads();
+    for (int o = 128; o > 0; o >>= 1) {
+        if ((int)threadIdx.x < o) {
+            sh[0][threadIdx.x] += sh[0][threadIdx.x + o];
+            sh[1][threadIdx.x] += sh[1][threadIdx.x + o];
+            sh[2][threadIdx.x] += sh[2][threadIdx.x + o];
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        out[3 * blockIdx.x] = sh[0][0];
+        out[3 * blockIdx.x + 1] = sh[1][0];
+        out[3 * blockIdx.x + 2] = sh[2][0];
+    }
+}
+
+int reduce_stage1_parts() { return 256; }
+
+void launch_reduce_rho(const double *partials, int nparts, double *stage1, float *rho, double *stats, int *ctr,
                        int cap, cudaStream_t s) {
-    k_reduce_rho<<<1, 256, 0, s>>>(partials, nparts, rho, stats, ctr, cap);
+    k_sum_stage1<<<256, 256, 0, s>>>(partials, nparts, stage1);
+    LAUNCH_CHECK("k_sum_stage1");
+    k_reduce_rho<<<1, 256, 0, s>>>(stage1, 256, rho, stats, ctr, cap);
     LAUNCH_CHECK("k_reduce_rho");
 }
 

@@ -51,6 +51,15 @@ __device__ __forceinline__ void tap_weights(int f, float p0, const UsGeo &g, flo
     }
 }
 
+__device__ __forceinline__ void cp_async8(void *smem, const void *gmem) {
+    const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(sa), "l"(gmem) : "memory");
+}
+
+__device__ __forceinline__ void cp_async_wait_all() {
+    asm volatile("cp.async.commit_group;\ncp.async.wait_group 0;\n" ::: "memory");
+}
+
 }  // namespace
 
 // ---------------------------------------------------------------------------
@@ -88,31 +97,59 @@ void launch_deapod_pad(const float *u, float *spec, int nimg, const float *deapo
 }
 
 // ---------------------------------------------------------------------------
+// Per-sample table built once per block in shared memory, one thread per
+// sample: the 9+9 separable Gaussian weights, the stencil position in the
+// block's tile, the angle/detector indices and a complex factor.
+// ---------------------------------------------------------------------------
+constexpr int kCH = 256;  // samples per table
+constexpr int kThreads = 512;  // threads per gather/scatter block
+constexpr int kWS = 28;   // floats per weight row: ex[9], ey[9], ex_im[9], 1 pad (16-byte rows)
+
+struct EntryTab {
+    float w[kCH][kWS];
+    int cb[kCH];   // gather: float2 offset of the stencil origin in the tile (-1: invalid)
+                   // scatter: packed (dx + 32) | (dy + 32) << 8
+    int th[kCH];
+    int k[kCH];
+    float2 f[kCH];  // gather: (pi/mu)/n (-1)^(k+1) shiftfwd(k); scatter: E(theta, k) of this slice
+};
+
+// ---------------------------------------------------------------------------
 // Forward gather (gather TOMO_FWD, kernels_radonusfft.cuh:81-144, fused with
 // the basis sum of operators.cu:143-152 and shift/fftshift of
 // radonusfft.cu:96-97).  One block per (work item, slice); a work item is a
-// tile of the spectrum and up to `cap` samples whose stencil centre lies in
-// it.  jbase selects a group of MP time samples (m > 16 runs several passes,
-// accumulating into rows).
+// 16x16 tile of the spectrum and up to kCH samples whose stencil origin lies
+// in it.  The block stages the (16+8)^2 cells x MP time samples of its tile,
+// builds the sample table, then each group of MP lanes computes one sample:
+// lane j reads time sample j's complex value per tap (64-bit loads, a
+// 128-byte row per sample), and the group sums K'(theta, j) H_j with
+// shuffles.  jbase selects a group of MP time samples (m > 16 runs several
+// passes, accumulating into rows).
 // ---------------------------------------------------------------------------
 template <int MP, int T>
-__global__ void __launch_bounds__(256)
+__global__ void __launch_bounds__(kThreads)
     k_gather_fwd(const float2 *__restrict__ spec, float2 *__restrict__ rows,
                  const uint32_t *__restrict__ pts, const int4 *__restrict__ items,
                  const float2 *__restrict__ sincos, const float2 *__restrict__ kmat,
                  const float2 *__restrict__ shiftf, UsGeo g, int jbase, int accumulate,
                  int *__restrict__ err) {
     constexpr int TW = T + 2 * kR;
-    constexpr int LPP = 2 * MP;
-    constexpr int GPW = 32 / LPP;
-    extern __shared__ float2 sm[];  // [NC][MP]
+    constexpr int EPW = 32 / MP;  // samples per warp
+    extern __shared__ float4 smraw[];
+    float2 *tile = reinterpret_cast<float2 *>(smraw);  // [TW*TW][MP]
+    EntryTab &tab = *reinterpret_cast<EntryTab *>(tile + TW * TW * MP);
     const int4 it = items[blockIdx.x];
     const int z = blockIdx.y;
     const int tyi = it.x / g.NT, txi = it.x - tyi * g.NT;
     const int P = g.P, half = P / 2;
+    const int count = it.z;
     const float2 *img0 = spec + (long long)z * g.m * g.img_fwd;
 
-    // ---- stage the tile: unit = (row, quad of 4 cells, time sample) ----
+    // ---- stage the tile with asynchronous copies: unit = (row, quad of 4
+    // cells, time sample).  The post-FFT fftshift sign (-1)^(X+Y) of a cell is
+    // (-1)^(column+row) of its tile position, and cells right of the Nyquist
+    // column are read through the Hermitian symmetry of the real-input FFT
+    // (conjugated); both signs are folded into the tap weights. ----
     {
         constexpr int NQ = TW / 4;
         const int nunits = TW * NQ * MP;
@@ -121,48 +158,33 @@ __global__ void __launch_bounds__(256)
             const int rq = u / MP;
             const int row = rq / NQ, q = rq - row * NQ;
             const int jg = jbase + j;
+            float2 *dst0 = tile + (row * TW + 4 * q) * MP + j;
+            if (jg >= g.m) {
+#pragma unroll
+                for (int c = 0; c < 4; ++c) dst0[c * MP] = make_float2(0.f, 0.f);
+                continue;
+            }
             int KY = tyi * T - kR + row;
             KY += (KY < 0) ? P : 0;
             KY -= (KY >= P) ? P : 0;
-            float2 v[4];
+            const int KYm = KY ? P - KY : 0;
+            const float2 *im = img0 + (long long)jg * g.img_fwd;
 #pragma unroll
             for (int c = 0; c < 4; ++c) {
-                float2 w = make_float2(0.f, 0.f);
-                if (jg < g.m) {
-                    int KX = txi * T - kR + 4 * q + c;
-                    KX += (KX < 0) ? P : 0;
-                    KX -= (KX >= P) ? P : 0;
-                    const float2 *im = img0 + (long long)jg * g.img_fwd;
-                    if (KX <= half) {
-                        w = __ldg(im + (long long)KY * g.hp + KX);
-                    } else {  // Hermitian symmetry of the real-input FFT
-                        const int KYm = KY ? P - KY : 0;
-                        w = __ldg(im + (long long)KYm * g.hp + (P - KX));
-                        w.y = -w.y;
-                    }
-                    if ((KX + KY) & 1) {  // post-FFT fftshift (-1)^(X+Y)
-                        w.x = -w.x;
-                        w.y = -w.y;
-                    }
-                }
-                v[c] = w;
+                int KX = txi * T - kR + 4 * q + c;
+                KX += (KX < 0) ? P : 0;
+                KX -= (KX >= P) ? P : 0;
+                const float2 *src = (KX <= half) ? im + (long long)KY * g.hp + KX
+                                                 : im + (long long)KYm * g.hp + (P - KX);
+                cp_async8(dst0 + c * MP, src);
             }
-#pragma unroll
-            for (int c = 0; c < 4; ++c) sm[(row * TW + 4 * q + c) * MP + j] = v[c];
         }
+        cp_async_wait_all();
     }
     __syncthreads();
-
-    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
-    const int grp = lane / LPP, l = lane - grp * LPP, j = l >> 1;
-    const int jg = jbase + j;
-    const float *smf = reinterpret_cast<const float *>(sm);
-    const int count = it.z;
-    const unsigned full = 0xffffffffu;
-    for (int p0 = wid * GPW; p0 < count; p0 += nw * GPW) {
-        const int p = p0 + grp;
-        bool valid = p < count;
-        const uint32_t id = __ldg(pts + it.y + (valid ? p : p0));
+    // ---- sample table ----
+    for (int e = threadIdx.x; e < count; e += blockDim.x) {
+        const uint32_t id = __ldg(pts + it.y + e);
         const int th = id / (uint32_t)g.n;
         const int k = id - th * g.n;
         float x0, y0;
@@ -170,37 +192,86 @@ __global__ void __launch_bounds__(256)
         sample_pos(k, __ldg(sincos + th), g, x0, y0, fx, fy);
         const int lx0 = g.n + fx - txi * T;
         const int ly0 = g.n + fy - tyi * T;
-        if (lx0 < 0 || lx0 >= T || ly0 < 0 || ly0 >= T) {  // host/device bin disagreement
-            if (valid && l == 0) atomicAdd(err, 1);
-            valid = false;
-        }
         float ex[kTaps], ey[kTaps];
         tap_weights(fx, x0, g, ex);
         tap_weights(fy, y0, g, ey);
-        const int cbase = valid ? (ly0 * TW + lx0) : 0;
-        const float *b0 = smf + cbase * LPP + l;
-        float acc = 0.f;
+#pragma unroll
+        for (int i = 0; i < kTaps; ++i) {  // (-1)^(a+b) of the fftshift sign
+            const float sx = (i & 1) ? -ex[i] : ex[i];
+            int KX = txi * T - kR + lx0 + i;  // conjugated columns flip the imaginary weight
+            KX += (KX < 0) ? P : 0;
+            KX -= (KX >= P) ? P : 0;
+            tab.w[e][i] = sx;
+            tab.w[e][kTaps + i] = (i & 1) ? -ey[i] : ey[i];
+            tab.w[e][2 * kTaps + i] = (KX > half) ? -sx : sx;
+        }
+        if (lx0 < 0 || lx0 >= T || ly0 < 0 || ly0 >= T) {  // host/device bin disagreement
+            atomicAdd(err, 1);
+            tab.cb[e] = -1;
+        } else {
+            tab.cb[e] = (ly0 * TW + lx0) * MP;
+        }
+        tab.th[e] = th;
+        tab.k[e] = k;
+        float2 sh = __ldg(shiftf + k);
+        float c = (k & 1) ? g.cw : -g.cw;  // (-1)^(k+1) and (pi/mu)/n
+        if ((lx0 + ly0) & 1) c = -c;        // fftshift sign of the stencil origin
+        tab.f[e] = make_float2(sh.x * c, sh.y * c);
+    }
+    __syncthreads();
+
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    const int grp = lane / MP, j = lane - grp * MP;
+    const int jg = jbase + j;
+    const unsigned full = 0xffffffffu;
+    for (int e0 = wid * EPW; e0 < count; e0 += nw * EPW) {
+        const int e = e0 + grp;
+        bool valid = e < count;
+        const int ee = valid ? e : e0;
+        int cb = tab.cb[ee];
+        if (cb < 0) {
+            valid = false;
+            cb = 0;
+        }
+        float w[kWS];
+        {
+            const float4 *wr = reinterpret_cast<const float4 *>(tab.w[ee]);
+#pragma unroll
+            for (int i = 0; i < kWS / 4; ++i) {
+                const float4 v = wr[i];
+                w[4 * i] = v.x;
+                w[4 * i + 1] = v.y;
+                w[4 * i + 2] = v.z;
+                w[4 * i + 3] = v.w;
+            }
+        }
+        const int th = tab.th[ee];
+        const float2 kv = (jg < g.m) ? __ldg(kmat + (long long)th * g.m + jg) : make_float2(0.f, 0.f);
+        const float2 *b0 = tile + cb + j;
+        float ax = 0.f, ay = 0.f;
 #pragma unroll
         for (int a = 0; a < kTaps; ++a) {
-            float ra = 0.f;
+            float rx = 0.f, ry = 0.f;
 #pragma unroll
-            for (int b = 0; b < kTaps; ++b) ra = fmaf(ex[b], b0[(a * TW + b) * LPP], ra);
-            acc = fmaf(ey[a], ra, acc);
+            for (int b = 0; b < kTaps; ++b) {
+                const float2 v = b0[(a * TW + b) * MP];
+                rx = fmaf(w[b], v.x, rx);
+                ry = fmaf(w[2 * kTaps + b], v.y, ry);
+            }
+            ax = fmaf(w[kTaps + a], rx, ax);
+            ay = fmaf(w[kTaps + a], ry, ay);
         }
-        // time-sample mixing: sum_j K'(theta, j) H_j  (re/im live in lane pairs)
-        const float2 kv = (jg < g.m) ? __ldg(kmat + (long long)th * g.m + jg) : make_float2(0.f, 0.f);
-        const float part = __shfl_xor_sync(full, acc, 1);
-        float val = (l & 1) ? (kv.x * acc + kv.y * part) : (kv.x * acc - kv.y * part);
+        // time-sample mixing: sum_j K'(theta, j) H_j over the group's lanes
+        float px = ax * kv.x - ay * kv.y;
+        float py = ax * kv.y + ay * kv.x;
 #pragma unroll
-        for (int o = 2; o < LPP; o <<= 1) val += __shfl_xor_sync(full, val, o);
-        const float oth = __shfl_xor_sync(full, val, 1);
-        if (valid && l == 0) {
-            float2 sh = __ldg(shiftf + k);
-            const float c = (k & 1) ? g.cw : -g.cw;  // (-1)^(k+1) and (pi/mu)/n
-            sh.x *= c;
-            sh.y *= c;
-            float2 r = cmul(make_float2(val, oth), sh);
-            float2 *dst = rows + ((long long)z * g.ntheta + th) * g.n + k;
+        for (int o = 1; o < MP; o <<= 1) {
+            px += __shfl_xor_sync(full, px, o);
+            py += __shfl_xor_sync(full, py, o);
+        }
+        if (valid && j == 0) {
+            float2 r = cmul(make_float2(px, py), tab.f[ee]);
+            float2 *dst = rows + ((long long)z * g.ntheta + th) * g.n + tab.k[ee];
             if (accumulate) {
                 const float2 o = *dst;
                 r.x += o.x;
@@ -218,16 +289,17 @@ static int mp_for(int m) {
 }
 
 size_t gather_fwd_smem(const UsGeo &g) {
-    return (size_t)(g.T + 2 * kR) * (g.T + 2 * kR) * mp_for(g.m) * sizeof(float2);
+    return (size_t)(g.T + 2 * kR) * (g.T + 2 * kR) * mp_for(g.m) * sizeof(float2) + sizeof(EntryTab);
 }
-size_t scatter_adj_smem(const UsGeo &g) { return (size_t)g.T * g.T * mp_for(g.m) * sizeof(float2); }
+size_t scatter_adj_smem(const UsGeo &g) { return sizeof(EntryTab); }
+int table_capacity() { return kCH; }
 
 template <int MP, int T>
 static void gather_fwd_t(const float2 *spec, float2 *rows, int zb, const GeoDev &gd, const UsGeo &g,
                          int jbase, int accumulate, int *err, cudaStream_t s) {
-    const size_t smem = (size_t)(T + 2 * kR) * (T + 2 * kR) * MP * sizeof(float2);
+    const size_t smem = (size_t)(T + 2 * kR) * (T + 2 * kR) * MP * sizeof(float2) + sizeof(EntryTab);
     dim3 gs(gd.n_fwd_items, zb);
-    k_gather_fwd<MP, T><<<gs, 256, smem, s>>>(spec, rows, gd.fwd_pts, gd.fwd_items, gd.sincos, gd.kmat,
+    k_gather_fwd<MP, T><<<gs, kThreads, smem, s>>>(spec, rows, gd.fwd_pts, gd.fwd_items, gd.sincos, gd.kmat,
                                               gd.shiftfwd, g, jbase, accumulate, err);
     LAUNCH_CHECK("k_gather_fwd");
 }
@@ -336,103 +408,124 @@ void launch_zero_split(float2 *spec, int zb, const GeoDev &gd, const UsGeo &g, c
 // ---------------------------------------------------------------------------
 // Adjoint scatter (gather TOMO_ADJ + wrap TOMO_ADJ, kernels_radonusfft.cuh:
 // 40-64,81-144, fused with shift/fftshift of radonusfft.cu:115-121, the basis
-// weights of operators.cu:171-176 and the pre-IFFT fftshift).  One block per
-// (work item, slice) owns a T x T tile of the periodic P x P grid and
-// accumulates every sample whose stencil touches it in shared memory, then
-// stores the tile once (or adds it, for tiles split over several blocks).
+// weights of operators.cu:171-176 and the pre-IFFT fftshift).
+//
+// One block per (16x16 tile of the periodic grid, slice); thread = cell, with
+// the cell's MP complex time-sample accumulators in registers, so nothing is
+// accumulated in shared memory and no atomics are needed.  The samples whose
+// stencil touches the tile arrive sorted by angle (tables of kCH samples).
+// Along one ray theta the time-sample weights conj(K'(theta, j)) are the same
+// for every sample, so each cell first sums V = sum_k w(k, cell) E(theta, k)
+// over the ray's samples and, when the angle changes, adds
+// conj(K'(theta, j)) V to its MP accumulators.  Warps skip samples whose
+// stencil rows miss their two tile rows.
 // ---------------------------------------------------------------------------
 template <int MP, int T>
-__global__ void __launch_bounds__(256)
+__global__ void __launch_bounds__(T * T)
     k_scatter_adj(const float2 *__restrict__ rowsc, float2 *__restrict__ spec,
                   const uint32_t *__restrict__ pts, const int4 *__restrict__ items,
                   const float2 *__restrict__ sincos, const float2 *__restrict__ kmat,
                   const float2 *__restrict__ shifta, UsGeo g, int jbase) {
-    constexpr int LPP = 2 * MP;
-    constexpr int GPW = 32 / LPP;
-    extern __shared__ float2 acc[];  // [T*T][MP]
-    float *accf = reinterpret_cast<float *>(acc);
-    for (int i = threadIdx.x; i < T * T * LPP; i += blockDim.x) accf[i] = 0.f;
-    __syncthreads();
+    static_assert(T == 16, "one thread per cell of a 16x16 tile, 2 rows per warp");
+    extern __shared__ float4 smraw[];
+    EntryTab &tab = *reinterpret_cast<EntryTab *>(smraw);
     const int4 it = items[blockIdx.x];
     const int z = blockIdx.y;
     const int tyi = it.x / g.NT, txi = it.x - tyi * g.NT;
     const int P = g.P, half = P / 2, hn = g.n / 2 + 1;
-    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
-    const int grp = lane / LPP, l = lane - grp * LPP, j = l >> 1, comp = l & 1;
-    const int jg = jbase + j;
-    const int count = it.z;
+    const int tid = threadIdx.x;
+    const int ly = tid / T, lx = tid - ly * T;
+    const int wrow = (tid >> 5) * 2;  // first tile row of this warp
     const float2 *rz = rowsc + (long long)z * g.ntheta * hn;
-    for (int p0 = wid * GPW; p0 < count; p0 += nw * GPW) {
-        const int p = p0 + grp;
-        const bool valid = p < count;
-        const uint32_t id = __ldg(pts + it.y + (valid ? p : p0));
-        const int th = id / (uint32_t)g.n;
-        const int k = id - th * g.n;
-        float x0, y0;
-        int fx, fy;
-        sample_pos(k, __ldg(sincos + th), g, x0, y0, fx, fy);
-        int dx = g.n + fx - kR - txi * T;
-        int dy = g.n + fy - kR - tyi * T;
-        dx += (dx < -half) ? P : 0;
-        dx -= (dx > half) ? P : 0;
-        dy += (dy < -half) ? P : 0;
-        dy -= (dy > half) ? P : 0;
-        // E = (-1)^(k+1) shiftadj(k) FFT(row)(k) (pi/mu)/n  (Hermitian row spectrum)
-        float2 R = (k <= g.n / 2) ? __ldg(rz + (long long)th * hn + k)
-                                  : __ldg(rz + (long long)th * hn + (g.n - k));
-        if (k > g.n / 2) R.y = -R.y;
-        const float2 S = __ldg(shifta + k);
-        float2 E = cmul(R, S);
-        const float c = (k & 1) ? g.cw : -g.cw;
-        E.x *= c;
-        E.y *= c;
-        const float2 kv = (jg < g.m) ? __ldg(kmat + (long long)th * g.m + jg) : make_float2(0.f, 0.f);
-        float qv = comp ? (kv.x * E.y - kv.y * E.x) : (kv.x * E.x + kv.y * E.y);  // conj(K') E
-        if (!valid) qv = 0.f;
-        float ex[kTaps], ey[kTaps];
-        tap_weights(fx, x0, g, ex);
-        tap_weights(fy, y0, g, ey);
+    float ar[MP], ai[MP];
 #pragma unroll
-        for (int a = 0; a < kTaps; ++a) {
-            const int ly = dy + a;
-            if ((unsigned)ly < (unsigned)T) {
-                const float wa = ey[a] * qv;
+    for (int j = 0; j < MP; ++j) ar[j] = ai[j] = 0.f;
+    float vr = 0.f, vi = 0.f;
+    int cur = -1;
+    auto mix = [&](int th) {  // acc_j += conj(K'(th, j)) V
+        if (vr != 0.f || vi != 0.f) {
+            const float2 *krow = kmat + (long long)th * g.m + jbase;
 #pragma unroll
-                for (int b = 0; b < kTaps; ++b) {
-                    const int lx = dx + b;
-                    if ((unsigned)lx < (unsigned)T) atomicAdd(&accf[(ly * T + lx) * LPP + l], ex[b] * wa);
-                }
+            for (int j = 0; j < MP; ++j) {
+                const float2 kv = (jbase + j < g.m) ? __ldg(krow + j) : make_float2(0.f, 0.f);
+                ar[j] = fmaf(kv.x, vr, fmaf(kv.y, vi, ar[j]));
+                ai[j] = fmaf(kv.x, vi, fmaf(-kv.y, vr, ai[j]));
+            }
+        }
+        vr = 0.f;
+        vi = 0.f;
+    };
+    for (int c0 = 0; c0 < it.z; c0 += kCH) {
+        const int cnt = min(kCH, it.z - c0);
+        __syncthreads();  // previous table consumed
+        for (int e = tid; e < cnt; e += blockDim.x) {
+            const uint32_t id = __ldg(pts + it.y + c0 + e);
+            const int th = id / (uint32_t)g.n;
+            const int k = id - th * g.n;
+            float x0, y0;
+            int fx, fy;
+            sample_pos(k, __ldg(sincos + th), g, x0, y0, fx, fy);
+            int dx = g.n + fx - kR - txi * T;
+            int dy = g.n + fy - kR - tyi * T;
+            dx += (dx < -half) ? P : 0;
+            dx -= (dx > half) ? P : 0;
+            dy += (dy < -half) ? P : 0;
+            dy -= (dy > half) ? P : 0;
+            float ex[kTaps], ey[kTaps];
+            tap_weights(fx, x0, g, ex);
+            tap_weights(fy, y0, g, ey);
+#pragma unroll
+            for (int i = 0; i < kTaps; ++i) {
+                tab.w[e][i] = ex[i];
+                tab.w[e][kTaps + i] = ey[i];
+            }
+            // stencils of listed samples start within [-2r, T) of the tile
+            tab.cb[e] = ((dx + 32) & 0xff) | (((dy + 32) & 0xff) << 8);
+            tab.th[e] = th;
+            // E = (-1)^(k+1) shiftadj(k) FFT(row)(k) (pi/mu)/n  (Hermitian row spectrum)
+            float2 R = (k <= g.n / 2) ? __ldg(rz + (long long)th * hn + k)
+                                      : __ldg(rz + (long long)th * hn + (g.n - k));
+            if (k > g.n / 2) R.y = -R.y;
+            const float2 E = cmul(R, __ldg(shifta + k));
+            const float c = (k & 1) ? g.cw : -g.cw;
+            tab.f[e] = make_float2(E.x * c, E.y * c);
+        }
+        __syncthreads();
+        for (int e = 0; e < cnt; ++e) {
+            const int th = tab.th[e];
+            if (th != cur) {  // ray boundary (same for every thread)
+                if (cur >= 0) mix(cur);
+                cur = th;
+            }
+            const int pk = tab.cb[e];
+            const int dy = ((pk >> 8) & 0xff) - 32;
+            if ((unsigned)(wrow + 1 - dy) > 9u) continue;  // stencil rows miss this warp's rows
+            const int dx = (pk & 0xff) - 32;
+            const int a = ly - dy, b = lx - dx;
+            if ((unsigned)a < (unsigned)kTaps && (unsigned)b < (unsigned)kTaps) {
+                const float w = tab.w[e][b] * tab.w[e][kTaps + a];
+                const float2 E = tab.f[e];
+                vr = fmaf(w, E.x, vr);
+                vi = fmaf(w, E.y, vi);
             }
         }
     }
-    __syncthreads();
-    // ---- flush: unit = (row, quad, time sample); pre-IFFT fftshift sign ----
-    constexpr int NQ = T / 4;
-    const int nunits = T * NQ * MP;
-    const int split = it.w;
-    for (int u = threadIdx.x; u < nunits; u += blockDim.x) {
-        const int jj = u % MP;
-        const int rq = u / MP;
-        const int row = rq / NQ, q = rq - row * NQ;
-        const int jgg = jbase + jj;
-        if (jgg >= g.m) continue;
-        const int KY = tyi * T + row;
-        if (KY >= P) continue;  // partial last tile row
-        float2 *dst = spec + ((long long)z * g.m + jgg) * g.img_adj + (long long)KY * P + txi * T + 4 * q;
+    if (cur >= 0) mix(cur);
+    // ---- store the cell (pre-IFFT fftshift sign); split tiles add ----
+    const int KY = tyi * T + ly, KX = txi * T + lx;
+    if (KY < P && KX < P) {
+        const float sg = ((KX + KY) & 1) ? -1.f : 1.f;
+        float2 *dst = spec + ((long long)z * g.m + jbase) * g.img_adj + (long long)KY * P + KX;
 #pragma unroll
-        for (int c = 0; c < 4; ++c) {
-            const int KX = txi * T + 4 * q + c;
-            if (KX >= P) break;
-            float2 v = acc[(row * T + 4 * q + c) * MP + jj];
-            if ((KX + KY) & 1) {
-                v.x = -v.x;
-                v.y = -v.y;
-            }
-            if (split) {
-                atomicAdd(&dst[c].x, v.x);
-                atomicAdd(&dst[c].y, v.y);
+        for (int j = 0; j < MP; ++j) {
+            if (jbase + j >= g.m) break;
+            const float2 v = make_float2(sg * ar[j], sg * ai[j]);
+            float2 *d = dst + (long long)j * g.img_adj;
+            if (it.w) {
+                atomicAdd(&d->x, v.x);
+                atomicAdd(&d->y, v.y);
             } else {
-                dst[c] = v;
+                *d = v;
             }
         }
     }
@@ -441,9 +534,9 @@ __global__ void __launch_bounds__(256)
 template <int MP, int T>
 static void scatter_adj_t(const float2 *rowsc, float2 *spec, int zb, const GeoDev &gd,
                           const UsGeo &g, int jbase, cudaStream_t s) {
-    const size_t smem = (size_t)T * T * MP * sizeof(float2);
+    const size_t smem = sizeof(EntryTab);
     dim3 gs(gd.n_adj_items, zb);
-    k_scatter_adj<MP, T><<<gs, 256, smem, s>>>(rowsc, spec, gd.adj_pts, gd.adj_items, gd.sincos, gd.kmat,
+    k_scatter_adj<MP, T><<<gs, T * T, smem, s>>>(rowsc, spec, gd.adj_pts, gd.adj_items, gd.sincos, gd.kmat,
                                                gd.shiftadj, g, jbase);
     LAUNCH_CHECK("k_scatter_adj");
 }
@@ -491,8 +584,8 @@ void launch_crop_accum(const float2 *spec, float *u, int zb, float tau, const fl
 
 template <int MP, int T>
 static void set_attrs() {
-    const int fs = (int)((T + 2 * kR) * (T + 2 * kR) * MP * sizeof(float2));
-    const int as = (int)(T * T * MP * sizeof(float2));
+    const int fs = (int)((T + 2 * kR) * (T + 2 * kR) * MP * sizeof(float2) + sizeof(EntryTab));
+    const int as = (int)sizeof(EntryTab);
     CUDA_CHECK(cudaFuncSetAttribute(k_gather_fwd<MP, T>, cudaFuncAttributeMaxDynamicSharedMemorySize, fs));
     CUDA_CHECK(cudaFuncSetAttribute(k_scatter_adj<MP, T>, cudaFuncAttributeMaxDynamicSharedMemorySize, as));
 }

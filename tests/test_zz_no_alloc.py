@@ -72,6 +72,6 @@ def test_shrink_noalloc_rejects_oversize(lib_built, torch_cuda):
     from rectv_gpu_gb300 import _lib
     lib = _lib.load()
     dummy = ctypes.c_void_p(1)
-    rc = lib.rectv_shrink_noalloc(dummy, dummy, dummy, dummy, 1024, 16, 16, 4, 0.5, 1e-3, 4.0, dummy, None)
+    rc = lib.rectv_shrink_noalloc(dummy, dummy, dummy, dummy, 2048, 16, 16, 4, 0.5, 1e-3, 4.0, dummy, None)
     assert rc == 1
     assert "at most 65536" in lib.rectv_last_error().decode()
