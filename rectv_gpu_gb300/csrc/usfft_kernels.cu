@@ -114,6 +114,20 @@ struct EntryTab {
     float2 f[kCH];  // gather: (pi/mu)/n (-1)^(k+1) shiftfwd(k); scatter: E(theta, k) of this slice
 };
 
+
+// Scatter block's shared memory: sample table, per-ray grids of one batch of
+// rays, and the ray index of each table row.
+constexpr int kSegBatch = 16;
+
+template <int T>
+struct ScatterSmem {
+    EntryTab tab;
+    float2 v[kSegBatch][T * T];
+    int seg_of[kCH];     // ray (segment) index of each table row
+    int seg_first[kCH];  // first table row of each segment
+    int wsum[8];
+};
+
 // ---------------------------------------------------------------------------
 // Forward gather (gather TOMO_FWD, kernels_radonusfft.cuh:81-144, fused with
 // the basis sum of operators.cu:143-152 and shift/fftshift of
@@ -145,43 +159,37 @@ __global__ void __launch_bounds__(kThreads)
     const int count = it.z;
     const float2 *img0 = spec + (long long)z * g.m * g.img_fwd;
 
-    // ---- stage the tile with asynchronous copies: unit = (row, quad of 4
-    // cells, time sample).  The post-FFT fftshift sign (-1)^(X+Y) of a cell is
-    // (-1)^(column+row) of its tile position, and cells right of the Nyquist
-    // column are read through the Hermitian symmetry of the real-input FFT
-    // (conjugated); both signs are folded into the tap weights. ----
+    // ---- stage the tile with asynchronous copies, one time-sample plane at
+    // a time with consecutive threads on consecutive cells (coalesced reads).
+    // Cell c, time sample j sits at float2 c*MP + (j ^ (column & (MP-1))): the
+    // XOR swizzle keeps both these stores and the compute loop's 128-byte rows
+    // free of bank conflicts.  The post-FFT fftshift sign (-1)^(X+Y) of a cell
+    // is (-1)^(column+row) of its tile position, and cells right of the
+    // Nyquist column are read through the Hermitian symmetry of the real-input
+    // FFT (conjugated); both signs are folded into the tap weights. ----
     {
-        constexpr int NQ = TW / 4;
-        const int nunits = TW * NQ * MP;
-        for (int u = threadIdx.x; u < nunits; u += blockDim.x) {
-            const int j = u % MP;
-            const int rq = u / MP;
-            const int row = rq / NQ, q = rq - row * NQ;
-            const int jg = jbase + j;
-            float2 *dst0 = tile + (row * TW + 4 * q) * MP + j;
-            if (jg >= g.m) {
-#pragma unroll
-                for (int c = 0; c < 4; ++c) dst0[c * MP] = make_float2(0.f, 0.f);
-                continue;
-            }
+        constexpr int NC = TW * TW;
+        for (int cell = threadIdx.x; cell < NC; cell += blockDim.x) {
+            const int row = cell / TW, col = cell - row * TW;
             int KY = tyi * T - kR + row;
             KY += (KY < 0) ? P : 0;
             KY -= (KY >= P) ? P : 0;
-            const int KYm = KY ? P - KY : 0;
-            const float2 *im = img0 + (long long)jg * g.img_fwd;
-#pragma unroll
-            for (int c = 0; c < 4; ++c) {
-                int KX = txi * T - kR + 4 * q + c;
-                KX += (KX < 0) ? P : 0;
-                KX -= (KX >= P) ? P : 0;
-                const float2 *src = (KX <= half) ? im + (long long)KY * g.hp + KX
-                                                 : im + (long long)KYm * g.hp + (P - KX);
-                cp_async8(dst0 + c * MP, src);
+            int KX = txi * T - kR + col;
+            KX += (KX < 0) ? P : 0;
+            KX -= (KX >= P) ? P : 0;
+            const long long so = (KX <= half) ? (long long)KY * g.hp + KX
+                                              : (long long)(KY ? P - KY : 0) * g.hp + (P - KX);
+            const float2 *src = img0 + (long long)jbase * g.img_fwd + so;
+            float2 *dst = tile + cell * MP;
+            const int sw = col & (MP - 1);
+#pragma unroll 4
+            for (int j = 0; j < MP; ++j) {
+                if (jbase + j < g.m) cp_async8(dst + (j ^ sw), src + (long long)j * g.img_fwd);
+                else dst[j ^ sw] = make_float2(0.f, 0.f);
             }
         }
         cp_async_wait_all();
     }
-    __syncthreads();
     // ---- sample table ----
     for (int e = threadIdx.x; e < count; e += blockDim.x) {
         const uint32_t id = __ldg(pts + it.y + e);
@@ -209,7 +217,7 @@ __global__ void __launch_bounds__(kThreads)
             atomicAdd(err, 1);
             tab.cb[e] = -1;
         } else {
-            tab.cb[e] = (ly0 * TW + lx0) * MP;
+            tab.cb[e] = ((ly0 * TW + lx0) * MP) | (lx0 << 20);
         }
         tab.th[e] = th;
         tab.k[e] = k;
@@ -229,9 +237,12 @@ __global__ void __launch_bounds__(kThreads)
         bool valid = e < count;
         const int ee = valid ? e : e0;
         int cb = tab.cb[ee];
-        if (cb < 0) {
+        int lx0 = cb >> 20;
+        cb &= (1 << 20) - 1;
+        if (tab.cb[ee] < 0) {
             valid = false;
             cb = 0;
+            lx0 = 0;
         }
         float w[kWS];
         {
@@ -247,14 +258,16 @@ __global__ void __launch_bounds__(kThreads)
         }
         const int th = tab.th[ee];
         const float2 kv = (jg < g.m) ? __ldg(kmat + (long long)th * g.m + jg) : make_float2(0.f, 0.f);
-        const float2 *b0 = tile + cb + j;
+        const float2 *bcol[kTaps];  // per tap column: swizzled slot of time sample j
+#pragma unroll
+        for (int b = 0; b < kTaps; ++b) bcol[b] = tile + cb + b * MP + (j ^ ((lx0 + b) & (MP - 1)));
         float ax = 0.f, ay = 0.f;
 #pragma unroll
         for (int a = 0; a < kTaps; ++a) {
             float rx = 0.f, ry = 0.f;
 #pragma unroll
             for (int b = 0; b < kTaps; ++b) {
-                const float2 v = b0[(a * TW + b) * MP];
+                const float2 v = bcol[b][a * TW * MP];
                 rx = fmaf(w[b], v.x, rx);
                 ry = fmaf(w[2 * kTaps + b], v.y, ry);
             }
@@ -291,7 +304,7 @@ static int mp_for(int m) {
 size_t gather_fwd_smem(const UsGeo &g) {
     return (size_t)(g.T + 2 * kR) * (g.T + 2 * kR) * mp_for(g.m) * sizeof(float2) + sizeof(EntryTab);
 }
-size_t scatter_adj_smem(const UsGeo &g) { return sizeof(EntryTab); }
+size_t scatter_adj_smem(const UsGeo &g) { return sizeof(ScatterSmem<16>); }
 int table_capacity() { return kCH; }
 
 template <int MP, int T>
@@ -410,15 +423,15 @@ void launch_zero_split(float2 *spec, int zb, const GeoDev &gd, const UsGeo &g, c
 // 40-64,81-144, fused with shift/fftshift of radonusfft.cu:115-121, the basis
 // weights of operators.cu:171-176 and the pre-IFFT fftshift).
 //
-// One block per (16x16 tile of the periodic grid, slice); thread = cell, with
-// the cell's MP complex time-sample accumulators in registers, so nothing is
-// accumulated in shared memory and no atomics are needed.  The samples whose
-// stencil touches the tile arrive sorted by angle (tables of kCH samples).
-// Along one ray theta the time-sample weights conj(K'(theta, j)) are the same
-// for every sample, so each cell first sums V = sum_k w(k, cell) E(theta, k)
-// over the ray's samples and, when the angle changes, adds
-// conj(K'(theta, j)) V to its MP accumulators.  Warps skip samples whose
-// stencil rows miss their two tile rows.
+// One block per (16x16 tile of the periodic grid, slice).  The samples whose
+// stencil touches the tile arrive sorted by angle.  Along one ray theta the
+// time-sample weights conj(K'(theta, j)) are the same for every sample, so the
+// block works per ray ("segment"), in batches of kSegBatch rays:
+//  1. a warp per sample, lanes on its 81 taps, adds w E(theta, k) into the
+//     ray's single-complex grid V_ray (shared memory);
+//  2. thread = cell adds conj(K'(theta, j)) V_ray(cell) to the cell's MP
+//     complex time-sample accumulators, held in registers.
+// The tile is stored once at the end (added, for a tile split over blocks).
 // ---------------------------------------------------------------------------
 template <int MP, int T>
 __global__ void __launch_bounds__(T * T)
@@ -426,35 +439,28 @@ __global__ void __launch_bounds__(T * T)
                   const uint32_t *__restrict__ pts, const int4 *__restrict__ items,
                   const float2 *__restrict__ sincos, const float2 *__restrict__ kmat,
                   const float2 *__restrict__ shifta, UsGeo g, int jbase) {
-    static_assert(T == 16, "one thread per cell of a 16x16 tile, 2 rows per warp");
+    static_assert(T == 16, "one thread per cell of a 16x16 tile");
     extern __shared__ float4 smraw[];
-    EntryTab &tab = *reinterpret_cast<EntryTab *>(smraw);
+    ScatterSmem<T> &sm = *reinterpret_cast<ScatterSmem<T> *>(smraw);
+    EntryTab &tab = sm.tab;
     const int4 it = items[blockIdx.x];
     const int z = blockIdx.y;
     const int tyi = it.x / g.NT, txi = it.x - tyi * g.NT;
     const int P = g.P, half = P / 2, hn = g.n / 2 + 1;
-    const int tid = threadIdx.x;
-    const int ly = tid / T, lx = tid - ly * T;
-    const int wrow = (tid >> 5) * 2;  // first tile row of this warp
+    const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+    constexpr int NW = T * T / 32;
     const float2 *rz = rowsc + (long long)z * g.ntheta * hn;
+    // this lane's taps t = lane, lane+32, lane+64 (< 81): row a = t/9, column b = t%9
+    int ta[3], tb[3];
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+        const int t = lane + 32 * i;
+        ta[i] = (t < kTaps * kTaps) ? t / kTaps : 1000;
+        tb[i] = t - (t / kTaps) * kTaps;
+    }
     float ar[MP], ai[MP];
 #pragma unroll
     for (int j = 0; j < MP; ++j) ar[j] = ai[j] = 0.f;
-    float vr = 0.f, vi = 0.f;
-    int cur = -1;
-    auto mix = [&](int th) {  // acc_j += conj(K'(th, j)) V
-        if (vr != 0.f || vi != 0.f) {
-            const float2 *krow = kmat + (long long)th * g.m + jbase;
-#pragma unroll
-            for (int j = 0; j < MP; ++j) {
-                const float2 kv = (jbase + j < g.m) ? __ldg(krow + j) : make_float2(0.f, 0.f);
-                ar[j] = fmaf(kv.x, vr, fmaf(kv.y, vi, ar[j]));
-                ai[j] = fmaf(kv.x, vi, fmaf(-kv.y, vr, ai[j]));
-            }
-        }
-        vr = 0.f;
-        vi = 0.f;
-    };
     for (int c0 = 0; c0 < it.z; c0 += kCH) {
         const int cnt = min(kCH, it.z - c0);
         __syncthreads();  // previous table consumed
@@ -491,27 +497,72 @@ __global__ void __launch_bounds__(T * T)
             tab.f[e] = make_float2(E.x * c, E.y * c);
         }
         __syncthreads();
-        for (int e = 0; e < cnt; ++e) {
-            const int th = tab.th[e];
-            if (th != cur) {  // ray boundary (same for every thread)
-                if (cur >= 0) mix(cur);
-                cur = th;
-            }
-            const int pk = tab.cb[e];
-            const int dy = ((pk >> 8) & 0xff) - 32;
-            if ((unsigned)(wrow + 1 - dy) > 9u) continue;  // stencil rows miss this warp's rows
-            const int dx = (pk & 0xff) - 32;
-            const int a = ly - dy, b = lx - dx;
-            if ((unsigned)a < (unsigned)kTaps && (unsigned)b < (unsigned)kTaps) {
-                const float w = tab.w[e][b] * tab.w[e][kTaps + a];
+        // ---- segment index of each row: block-wide inclusive scan of ray starts ----
+        int flag = 0;
+        if (tid < cnt) flag = (tid == 0 || tab.th[tid] != tab.th[tid - 1]) ? 1 : 0;
+        int incl = flag;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int y = __shfl_up_sync(0xffffffffu, incl, o);
+            if (lane >= o) incl += y;
+        }
+        if (lane == 31) sm.wsum[wid] = incl;
+        __syncthreads();
+        int base = 0, nseg = 0;
+#pragma unroll
+        for (int w = 0; w < NW; ++w) {
+            const int v = sm.wsum[w];
+            base += (w < wid) ? v : 0;
+            nseg += v;
+        }
+        incl += base;
+        if (tid < cnt) {
+            sm.seg_of[tid] = incl - 1;
+            if (flag) sm.seg_first[incl - 1] = tid;
+        }
+        for (int sb = 0; sb < nseg; sb += kSegBatch) {
+            const int nb = min(kSegBatch, nseg - sb);
+            __syncthreads();  // seg tables written; previous batch mixed
+            for (int s = 0; s < nb; ++s) sm.v[s][tid] = make_float2(0.f, 0.f);
+            const int e_lo = sm.seg_first[sb];
+            const int e_hi = (sb + nb < nseg) ? sm.seg_first[sb + nb] : cnt;
+            __syncthreads();
+            // ---- 1. rays' grids: warp per sample, lanes on taps ----
+            for (int e = e_lo + wid; e < e_hi; e += NW) {
+                const int pk = tab.cb[e];
+                const int dx = (pk & 0xff) - 32, dy = ((pk >> 8) & 0xff) - 32;
                 const float2 E = tab.f[e];
-                vr = fmaf(w, E.x, vr);
-                vi = fmaf(w, E.y, vi);
+                float *vs = reinterpret_cast<float *>(sm.v[sm.seg_of[e] - sb]);
+#pragma unroll
+                for (int i = 0; i < 3; ++i) {
+                    const int cy = dy + ta[i], cx = dx + tb[i];
+                    if ((unsigned)cy < (unsigned)T && (unsigned)cx < (unsigned)T) {
+                        const float w = tab.w[e][tb[i]] * tab.w[e][kTaps + ta[i]];
+                        const unsigned sa = (unsigned)__cvta_generic_to_shared(vs + 2 * (cy * T + cx));
+                        asm volatile("red.shared.add.f32 [%0], %1;\n" ::"r"(sa), "f"(w * E.x) : "memory");
+                        asm volatile("red.shared.add.f32 [%0+4], %1;\n" ::"r"(sa), "f"(w * E.y) : "memory");
+                    }
+                }
+            }
+            __syncthreads();
+            // ---- 2. thread = cell: acc_j += conj(K'(theta, j)) V_ray(cell) ----
+            for (int s = 0; s < nb; ++s) {
+                const float2 v = sm.v[s][tid];
+                if (v.x != 0.f || v.y != 0.f) {
+                    const int th = tab.th[sm.seg_first[sb + s]];
+                    const float2 *krow = kmat + (long long)th * g.m + jbase;
+#pragma unroll
+                    for (int j = 0; j < MP; ++j) {
+                        const float2 kv = (jbase + j < g.m) ? __ldg(krow + j) : make_float2(0.f, 0.f);
+                        ar[j] = fmaf(kv.x, v.x, fmaf(kv.y, v.y, ar[j]));
+                        ai[j] = fmaf(kv.x, v.y, fmaf(-kv.y, v.x, ai[j]));
+                    }
+                }
             }
         }
     }
-    if (cur >= 0) mix(cur);
     // ---- store the cell (pre-IFFT fftshift sign); split tiles add ----
+    const int ly = tid / T, lx = tid - (tid / T) * T;
     const int KY = tyi * T + ly, KX = txi * T + lx;
     if (KY < P && KX < P) {
         const float sg = ((KX + KY) & 1) ? -1.f : 1.f;
@@ -534,7 +585,7 @@ __global__ void __launch_bounds__(T * T)
 template <int MP, int T>
 static void scatter_adj_t(const float2 *rowsc, float2 *spec, int zb, const GeoDev &gd,
                           const UsGeo &g, int jbase, cudaStream_t s) {
-    const size_t smem = sizeof(EntryTab);
+    const size_t smem = sizeof(ScatterSmem<T>);
     dim3 gs(gd.n_adj_items, zb);
     k_scatter_adj<MP, T><<<gs, T * T, smem, s>>>(rowsc, spec, gd.adj_pts, gd.adj_items, gd.sincos, gd.kmat,
                                                gd.shiftadj, g, jbase);
@@ -585,7 +636,7 @@ void launch_crop_accum(const float2 *spec, float *u, int zb, float tau, const fl
 template <int MP, int T>
 static void set_attrs() {
     const int fs = (int)((T + 2 * kR) * (T + 2 * kR) * MP * sizeof(float2) + sizeof(EntryTab));
-    const int as = (int)sizeof(EntryTab);
+    const int as = (int)sizeof(ScatterSmem<T>);
     CUDA_CHECK(cudaFuncSetAttribute(k_gather_fwd<MP, T>, cudaFuncAttributeMaxDynamicSharedMemorySize, fs));
     CUDA_CHECK(cudaFuncSetAttribute(k_scatter_adj<MP, T>, cudaFuncAttributeMaxDynamicSharedMemorySize, as));
 }
