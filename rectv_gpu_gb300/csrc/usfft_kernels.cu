@@ -122,7 +122,8 @@ constexpr int kSegBatch = 16;
 template <int T>
 struct ScatterSmem {
     EntryTab tab;
-    float2 v[kSegBatch][T * T];
+    float v[kSegBatch][2][T * T];  // per-ray grids, real and imaginary planes
+    float4 kr[kSegBatch][8];       // per-ray mixing rows K'(theta, jbase + j), j < 16
     int seg_of[kCH];     // ray (segment) index of each table row
     int seg_first[kCH];  // first table row of each segment
     int wsum[8];
@@ -434,7 +435,7 @@ void launch_zero_split(float2 *spec, int zb, const GeoDev &gd, const UsGeo &g, c
 // The tile is stored once at the end (added, for a tile split over blocks).
 // ---------------------------------------------------------------------------
 template <int MP, int T>
-__global__ void __launch_bounds__(T * T)
+__global__ void __launch_bounds__(T * T, 3)
     k_scatter_adj(const float2 *__restrict__ rowsc, float2 *__restrict__ spec,
                   const uint32_t *__restrict__ pts, const int4 *__restrict__ items,
                   const float2 *__restrict__ sincos, const float2 *__restrict__ kmat,
@@ -523,7 +524,17 @@ __global__ void __launch_bounds__(T * T)
         for (int sb = 0; sb < nseg; sb += kSegBatch) {
             const int nb = min(kSegBatch, nseg - sb);
             __syncthreads();  // seg tables written; previous batch mixed
-            for (int s = 0; s < nb; ++s) sm.v[s][tid] = make_float2(0.f, 0.f);
+            for (int s = 0; s < nb; ++s) {
+                sm.v[s][0][tid] = 0.f;
+                sm.v[s][1][tid] = 0.f;
+            }
+            if (tid < nb * 16) {  // stage the batch's mixing rows (zero beyond m)
+                const int s = tid >> 4, j = tid & 15;
+                const int th = tab.th[sm.seg_first[sb + s]];
+                const float2 kv =
+                    (jbase + j < g.m) ? __ldg(kmat + (long long)th * g.m + jbase + j) : make_float2(0.f, 0.f);
+                reinterpret_cast<float2 *>(sm.kr[s])[j] = kv;
+            }
             const int e_lo = sm.seg_first[sb];
             const int e_hi = (sb + nb < nseg) ? sm.seg_first[sb + nb] : cnt;
             __syncthreads();
@@ -532,30 +543,32 @@ __global__ void __launch_bounds__(T * T)
                 const int pk = tab.cb[e];
                 const int dx = (pk & 0xff) - 32, dy = ((pk >> 8) & 0xff) - 32;
                 const float2 E = tab.f[e];
-                float *vs = reinterpret_cast<float *>(sm.v[sm.seg_of[e] - sb]);
+                float *vs = sm.v[sm.seg_of[e] - sb][0];
 #pragma unroll
                 for (int i = 0; i < 3; ++i) {
                     const int cy = dy + ta[i], cx = dx + tb[i];
                     if ((unsigned)cy < (unsigned)T && (unsigned)cx < (unsigned)T) {
                         const float w = tab.w[e][tb[i]] * tab.w[e][kTaps + ta[i]];
-                        const unsigned sa = (unsigned)__cvta_generic_to_shared(vs + 2 * (cy * T + cx));
+                        const unsigned sa = (unsigned)__cvta_generic_to_shared(vs + cy * T + cx);
                         asm volatile("red.shared.add.f32 [%0], %1;\n" ::"r"(sa), "f"(w * E.x) : "memory");
-                        asm volatile("red.shared.add.f32 [%0+4], %1;\n" ::"r"(sa), "f"(w * E.y) : "memory");
+                        asm volatile("red.shared.add.f32 [%0+1024], %1;\n" ::"r"(sa), "f"(w * E.y) : "memory");
                     }
                 }
             }
             __syncthreads();
             // ---- 2. thread = cell: acc_j += conj(K'(theta, j)) V_ray(cell) ----
             for (int s = 0; s < nb; ++s) {
-                const float2 v = sm.v[s][tid];
+                const float2 v = make_float2(sm.v[s][0][tid], sm.v[s][1][tid]);
                 if (v.x != 0.f || v.y != 0.f) {
-                    const int th = tab.th[sm.seg_first[sb + s]];
-                    const float2 *krow = kmat + (long long)th * g.m + jbase;
 #pragma unroll
-                    for (int j = 0; j < MP; ++j) {
-                        const float2 kv = (jbase + j < g.m) ? __ldg(krow + j) : make_float2(0.f, 0.f);
-                        ar[j] = fmaf(kv.x, v.x, fmaf(kv.y, v.y, ar[j]));
-                        ai[j] = fmaf(kv.x, v.y, fmaf(-kv.y, v.x, ai[j]));
+                    for (int jj = 0; jj < (MP + 1) / 2; ++jj) {
+                        const float4 kv = sm.kr[s][jj];
+                        ar[2 * jj] = fmaf(kv.x, v.x, fmaf(kv.y, v.y, ar[2 * jj]));
+                        ai[2 * jj] = fmaf(kv.x, v.y, fmaf(-kv.y, v.x, ai[2 * jj]));
+                        if (2 * jj + 1 < MP) {
+                            ar[2 * jj + 1] = fmaf(kv.z, v.x, fmaf(kv.w, v.y, ar[2 * jj + 1]));
+                            ai[2 * jj + 1] = fmaf(kv.z, v.y, fmaf(-kv.w, v.x, ai[2 * jj + 1]));
+                        }
                     }
                 }
             }
