@@ -63,6 +63,24 @@ def ncu_traffic(kernel, wl):
 
 
 # ---------------------------------------------------------------------------
+# multi-rank aggregation (independent replicas, one per GPU)
+# ---------------------------------------------------------------------------
+def max_over_ranks(x, dist, device):
+    """Largest value of x over all ranks (x unchanged without a process group)."""
+    if dist is None:
+        return float(x)
+    import torch
+    t = torch.tensor([float(x)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def whole_job_rate(steps, world, ms):
+    """Units all ranks processed (each rank: `steps` iterations) per second."""
+    return world * steps / (ms * 1e-3)
+
+
+# ---------------------------------------------------------------------------
 # clocks sampled during the timed region
 # ---------------------------------------------------------------------------
 class ClockSampler:
@@ -296,11 +314,8 @@ def run_ours(args, rank, world, local_rank):
     e1.record(stream)
     torch.cuda.synchronize()
     clocks = sampler.stop()
-    ms = e0.elapsed_time(e1)
+    ms = max_over_ranks(e0.elapsed_time(e1), dist, dev)
     if dist:
-        t = torch.tensor([ms], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
         dist.barrier()
     hist = obj.history()
 
@@ -334,7 +349,13 @@ def run_ours(args, rank, world, local_rank):
     _lib.check(lib.rectv_kernel_cost(obj._h, dom, ctypes.byref(bytes_), ctypes.byref(flops)))
     peak, peak_kind = measured_peaks()
     achieved = bytes_.value / (ktimes[dom] * 1e-3) / 1e9
-    roofline = {"bound": "hbm", "kernel": KERNEL_NAMES[dom], "achieved": achieved, "peak": peak,
+    limiter = {
+        "k_scatter_adj": "FP32 issue and shared-memory latency (per-ray shared reductions, 16-way "
+                         "time-sample mixing in registers); DRAM traffic ~= algorithmic bytes",
+        "k_gather_fwd": "shared-memory bandwidth (81 taps x 16 time samples x 8 B per polar sample)",
+        "k_graddiv": "HBM bandwidth", "k_shrink": "HBM bandwidth"}[KERNEL_NAMES[dom]]
+    roofline = {"bound": "hbm", "limiter": limiter, "kernel": KERNEL_NAMES[dom], "achieved": achieved,
+                "peak": peak,
                 "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / peak,
                 "traffic": ncu_traffic(KERNEL_NAMES[dom], workload_name(w)),
                 "algorithmic_bytes": bytes_.value, "fp32_tflops": flops.value / (ktimes[dom] * 1e-3) / 1e12,
@@ -354,11 +375,7 @@ def run_ours(args, rank, world, local_rank):
     obj.run(f_h.data_ptr(), g_h.data_ptr(), th_h.data_ptr(), ph_h.data_ptr(), center, lam0, lam1, args.steps,
             titer)
     t1 = time.perf_counter()
-    e2e_s = t1 - t0
-    if dist:
-        t = torch.tensor([e2e_s], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_s = float(t.item())
+    e2e_s = max_over_ranks(t1 - t0, dist, dev)
     h2d = g_h.numel() * 4 + th_h.numel() * 4 + ph_h.numel() * 4
     d2h = f_h.numel() * 4
     finite = bool(np.isfinite(f_h[:, :, ::64, ::64].numpy()).all())
@@ -368,7 +385,7 @@ def run_ours(args, rank, world, local_rank):
         v, s, sample, workers = cpu_sample(w)
         cpu = {"value": v, "unit": "iter/s", "cores": workers, "kind": "port", "sample": sample}
 
-    value = world * args.steps / (ms * 1e-3)
+    value = whole_job_rate(args.steps, world, ms)
     voxels = float(n) * n * m * nz
     line = {
         "metric": METRIC, "value": value, "unit": "iter/s", "n_gpus": world, "steps": args.steps,
@@ -380,7 +397,7 @@ def run_ours(args, rank, world, local_rank):
                    "l2": "inputs larger than L2 (iterate 4.3 GB, dual variables 2x19 GB)",
                    "parallelism": "replicas" if world > 1 else "single"},
         "voxel_updates_per_s": value * voxels,
-        "e2e": {"value": world * args.steps / e2e_s, "unit": "iter/s", "h2d_bytes_per_step": h2d / args.steps,
+        "e2e": {"value": whole_job_rate(args.steps, world, e2e_s * 1e3), "unit": "iter/s", "h2d_bytes_per_step": h2d / args.steps,
                 "d2h_bytes_per_step": d2h / args.steps, "seconds": e2e_s, "api": "rectv_run (C ABI)"},
         "roofline": roofline,
         "cpu_baseline": cpu,

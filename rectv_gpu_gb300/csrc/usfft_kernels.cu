@@ -535,15 +535,16 @@ __global__ void __launch_bounds__(T * T, 3)
                     (jbase + j < g.m) ? __ldg(kmat + (long long)th * g.m + jbase + j) : make_float2(0.f, 0.f);
                 reinterpret_cast<float2 *>(sm.kr[s])[j] = kv;
             }
-            const int e_lo = sm.seg_first[sb];
-            const int e_hi = (sb + nb < nseg) ? sm.seg_first[sb + nb] : cnt;
             __syncthreads();
-            // ---- 1. rays' grids: warp per sample, lanes on taps ----
-            for (int e = e_lo + wid; e < e_hi; e += NW) {
+            // ---- 1. rays' grids: a warp per ray (its samples in order, so the
+            // sums are reproducible), lanes on the taps of one sample ----
+            for (int s = wid; s < nb; s += NW)
+            for (int e = sm.seg_first[sb + s], e_end = (sb + s + 1 < nseg) ? sm.seg_first[sb + s + 1] : cnt;
+                 e < e_end; ++e) {
                 const int pk = tab.cb[e];
                 const int dx = (pk & 0xff) - 32, dy = ((pk >> 8) & 0xff) - 32;
                 const float2 E = tab.f[e];
-                float *vs = sm.v[sm.seg_of[e] - sb][0];
+                float *vs = sm.v[s][0];
 #pragma unroll
                 for (int i = 0; i < 3; ++i) {
                     const int cy = dy + ta[i], cx = dx + tb[i];
