@@ -143,6 +143,39 @@ int rectv_kernel_cost(rectv_handle *h, int which, double *bytes, double *flops);
 int rectv_get_launch_counts(rectv_handle *h, int *kernels, int *fft_execs, int *batch_slices);
 
 /* ---------------------------------------------------------------------------
+ * Filtered backprojection and warm start (no counterpart run by the
+ * reference: its ramp filter applyfilter and mask circ,
+ * kernels_radonusfft.cuh:146-189, and the filter flag of radonusfft::adjR,
+ * radonusfft.cu:106, are never used).
+ * ------------------------------------------------------------------------- */
+
+/* Static filtered backprojection of every slice: frec [nz][n][n] (host) =
+ * circ(pi/4 * R*(applyfilter(g))) with g [nz][ntheta][n], theta [ntheta] host
+ * float32 and the rotation centre as in rectv_run.  Uses the handle's buffers
+ * (not its reconstruction state). */
+int rectv_fbp(rectv_handle *h, float *frec, const float *g, const float *theta, float center);
+
+/* rectv_run starting from finit [nz][m][n][n] (host) instead of zero. */
+int rectv_run_init(rectv_handle *h, float *fres, const float *g, const float *theta, const float *phi,
+                   const float *finit, float center, float lambda0, float lambda1, int niter, int titer);
+
+/* ---------------------------------------------------------------------------
+ * Data ingest: the step before the solver.  Replaces the preprocessing of
+ * examples/tao/tao.py:34-41 (flat/dark normalisation, -log, projection ->
+ * sinogram transpose):
+ *   out[z][theta][x] = -log((data[theta][z][x] - mean_f dark[f][z][x]) /
+ *                           (1e-3 + mean_f flat[f][z][x] - mean_f dark[f][z][x]))
+ * Host pointers; data [ntheta][nz][n], dark [ndark][nz][n], flat [nflat][nz][n]
+ * of element type dtype; out float32 [nz][ntheta][n] (the layout rectv_run
+ * takes).  Uses temporary device memory; non-positive ratios give NaN/inf as
+ * in the NumPy original.
+ * ------------------------------------------------------------------------- */
+enum { RECTV_DTYPE_F32 = 0, RECTV_DTYPE_U16 = 1 };
+
+int rectv_preprocess(float *out, const void *data, const void *dark, const void *flat, int dtype, int ntheta,
+                     int nz, int n, int ndark, int nflat);
+
+/* ---------------------------------------------------------------------------
  * Allocation-free entry point (no counterpart in the reference).
  *
  * For callers that cannot let a library allocate device memory -- an

@@ -342,7 +342,7 @@ def solver_admm(ops, fm, g, psi, mu, lambda0, lambda1, rho, flgl, flgr, titer):
 
 
 def run(data, theta, phi, center, lambda0, lambda1, niter, titer, nzp, return_history=False,
-        callback=None):
+        callback=None, init=None):
     """rectv::run (rectv.cu:102-252) with the wrapper's conventions applied by the caller.
 
     ``lambda0`` here is the value passed to ``run`` (Solver.recon multiplies
@@ -357,6 +357,9 @@ def run(data, theta, phi, center, lambda0, lambda1, niter, titer, nzp, return_hi
     nchunks = nz // nzp
     ops = Operators(n, ntheta, m, theta, phi, center)
     f = np.zeros((nz, m, n, n))
+    if init is not None:  # extension: warm start instead of rectv.cu:119-120's zero
+        nzc = nchunks * nzp
+        f[:nzc] = np.asarray(init, dtype=np.float64)[:nzc]
     fn = np.zeros((nz, m, n, n))
     gp = (nzp + 1, m + 1, n + 1, n + 1, 4)
     psi = [np.zeros(gp) for _ in range(nchunks)]
@@ -420,3 +423,43 @@ def check_adjoints(data, theta, phi, lambda1, center):
     res[4] = np.sum(h2.ravel()[:npts] ** 2)
     res[5] = np.sum(fn * fn)
     return res
+
+
+# ---------------------------------------------------------------------------
+# Data ingest (the step before the path)
+# ---------------------------------------------------------------------------
+
+def preprocess(data, dark, flat):
+    """Flat/dark normalisation, -log and projection -> sinogram transpose of
+    the reference's tao example (examples/tao/tao.py:41), in float64."""
+    data = np.asarray(data, dtype=np.float64)
+    dm = np.mean(np.asarray(dark, dtype=np.float64), axis=0)
+    fm = np.mean(np.asarray(flat, dtype=np.float64), axis=0)
+    with np.errstate(invalid="ignore", divide="ignore"):
+        return -np.log((data - dm) / (1e-3 + fm - dm)).swapaxes(0, 1)
+
+
+# ---------------------------------------------------------------------------
+# Filtered backprojection with the reference's unused filter and mask
+# ---------------------------------------------------------------------------
+
+def fbp(data, theta, center):
+    """circ(pi/4 * adjR(applyfilter(g))) per slice: adjR (radonusfft.cu:
+    106-135) with applyfilter (kernels_radonusfft.cuh:173-189) applied to the
+    centred row spectrum right after the row FFT's fftshift, and circ with
+    r = 0 (kernels_radonusfft.cuh:146-159).  data [nz, ntheta, n] ->
+    [nz, n, n] float64."""
+    data = np.asarray(data, dtype=np.float64)
+    nz, ntheta, n = data.shape
+    R = USFFT(n, theta, center)
+    k = np.arange(n)
+    rho = (k - n // 2) / float(n)
+    with np.errstate(invalid="ignore", divide="ignore"):
+        w = np.where(rho == 0, 0.0, np.abs(rho) * n * 4 * np.sin(rho) / rho)
+    g = data.astype(np.complex128) * R.mod1
+    g = np.fft.fft(g, axis=-1) * R.mod1 * w
+    g = np.fft.ifft(g * R.mod1, axis=-1) * R.mod1  # back to s; adj transforms again
+    f = R.adj(g).real * (PI_USFFT / 4)
+    x = (np.arange(n) - n // 2) / float(n)
+    mask = (4 * x[None, :] ** 2 + 4 * x[:, None] ** 2) < 1
+    return f * mask[None]

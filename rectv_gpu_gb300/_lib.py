@@ -42,6 +42,9 @@ SIGNATURES = {
     "rectv_kernel_cost": (_I, [_P, _I, _P, _P]),
     "rectv_get_launch_counts": (_I, [_P, _IP, _IP, _IP]),
     "rectv_shrink_noalloc": (_I, [_P, _P, _P, _P, _I, _I, _I, _I, _F, _F, _F, _P, _P]),
+    "rectv_preprocess": (_I, [_P, _P, _P, _P, _I, _I, _I, _I, _I, _I]),
+    "rectv_fbp": (_I, [_P, _P, _P, _P, _F]),
+    "rectv_run_init": (_I, [_P, _P, _P, _P, _P, _P, _F, _F, _F, _I, _I]),
 }
 
 _lib = None

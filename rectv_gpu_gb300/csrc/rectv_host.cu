@@ -348,9 +348,13 @@ struct Handle {
 
         // K'(theta, j) = ntheta/sqrt(m) sum_i phi_i(theta) conj(phi_i(t_j)),
         // t_j = j*ntheta/m: decphi/mulphi/recphi (kernels_operators.cuh:99-149)
-        std::vector<float2> kmat((size_t)ntheta * m);
+        // phi_h == nullptr: the plain (static) Radon transform into time sample 0,
+        // K'(theta, 0) = 1, K'(theta, j > 0) = 0 (filtered backprojection)
+        std::vector<float2> kmat((size_t)ntheta * m, make_float2(0.f, 0.f));
         const double cphi = (double)ntheta / std::sqrt((double)m);
-        for (int th = 0; th < ntheta; ++th)
+        if (!phi_h)
+            for (int th = 0; th < ntheta; ++th) kmat[(size_t)th * m] = make_float2(1.f, 0.f);
+        for (int th = 0; phi_h && th < ntheta; ++th)
             for (int j = 0; j < m; ++j) {
                 const int tj = (int)(((long long)j * ntheta) / m);
                 std::complex<double> acc(0.0, 0.0);
@@ -402,10 +406,11 @@ struct Handle {
     }
 
     // u += tau R_apr^T h
-    void adjoint(const float *h, float *u, float tau) {
+    void adjoint(const float *h, float *u, float tau, const float *row_filter = nullptr) {
         launch_adj_prep(h, reinterpret_cast<float *>(rows), zb, ug, stream);
         CUFFT_CHECK(cufftExecR2C(p_rows_r2c, reinterpret_cast<cufftReal *>(rows),
                                  reinterpret_cast<cufftComplex *>(rows)));
+        if (row_filter) launch_filter_rows(rows, row_filter, (long long)zb * ntheta, n, stream);
         launch_zero_split(spec, zb, gd, ug, stream);
         launch_scatter_adj(rows, spec, zb, gd, ug, stream);
         const int nimg = zb * m;
@@ -472,17 +477,21 @@ struct Handle {
     }
 
     void setup(const float *theta_h, const float *phi_h, float center, float lambda0_, float lambda1_,
-               int titer_) {
+               int titer_, const float *init = nullptr, cudaMemcpyKind init_kind = cudaMemcpyHostToDevice) {
         check_live();
         if (titer_ < 0) throw Error(RECTV_ERR_ARG, "rectv: titer must be >= 0");
+        if (!phi_h) throw Error(RECTV_ERR_ARG, "rectv: phi is required");
         set_geometry(theta_h, phi_h, center);
         lambda0 = lambda0_;
         set_lambda1(lambda1_);
         titer = titer_;
         drop_graphs();
-        // initial guess and ADMM state (rectv.cu:119-125)
+        // initial guess (zero, as rectv.cu:119-120, unless given) and ADMM state (rectv.cu:121-125)
         cur = 0;
-        CUDA_CHECK(cudaMemsetAsync(U[0], 0, sizeof(float) * (size_t)nzc * slab, stream));
+        if (init)
+            CUDA_CHECK(cudaMemcpyAsync(U[0], init, sizeof(float) * (size_t)nzc * slab, init_kind, stream));
+        else
+            CUDA_CHECK(cudaMemsetAsync(U[0], 0, sizeof(float) * (size_t)nzc * slab, stream));
         CUDA_CHECK(cudaMemsetAsync(psi, 0, sizeof(float) * (size_t)4 * nchunks * gp, stream));
         CUDA_CHECK(cudaMemsetAsync(mu, 0, sizeof(float) * (size_t)4 * nchunks * gp, stream));
         const float rho0 = 0.5f;
@@ -617,6 +626,43 @@ struct Handle {
     }
 
     void launch_axpy(float *y, const float *x, float a, long long count);
+
+    // ---- filtered backprojection (static object), per slice ----
+    // frec[z] = circ( pi/4 * R^T( applyfilter(g[z]) ) ): the USFFT adjoint with
+    // the reference's ramp filter (kernels_radonusfft.cuh:173-189) on the
+    // centred row spectrum and its circular mask (kernels_radonusfft.cuh:
+    // 146-159, r = 0).  pi/4 makes R^T W R the identity on band-limited,
+    // zero-mean objects for this operator's 1/sqrt(n ntheta) normalisation.
+    void fbp(float *frec_h, const float *g_h, const float *theta_h, float center) {
+        check_live();
+        session = false;
+        drop_graphs();
+        set_geometry(theta_h, nullptr, center);
+        std::vector<float> w(n / 2 + 1);
+        for (int k = 0; k <= n / 2; ++k) {
+            const float rho = (float)(k - n / 2) / (float)n;
+            w[k] = (rho == 0.f) ? 0.f : (float)(std::fabs((double)rho) * n * 4 * std::sin((double)rho) / rho);
+        }
+        float *w_d = nullptr;
+        CUDA_CHECK(cudaMalloc(&w_d, w.size() * sizeof(float)));
+        geo_owned.push_back(w_d);
+        CUDA_CHECK(cudaMemcpyAsync(w_d, w.data(), w.size() * sizeof(float), cudaMemcpyHostToDevice, stream));
+        const float scale = (float)(kPiUsfft / 4.0);
+        float *tmp = U[2], *out = U[1];
+        for (int z0 = 0; z0 < nz; z0 += zb) {
+            const int nb = std::min(zb, nz - z0);
+            CUDA_CHECK(cudaMemsetAsync(h1, 0, sizeof(float) * (size_t)zb * ntheta * n, stream));
+            CUDA_CHECK(cudaMemcpyAsync(h1, g_h + (size_t)z0 * ntheta * n, sizeof(float) * (size_t)nb * ntheta * n,
+                                       cudaMemcpyHostToDevice, stream));
+            CUDA_CHECK(cudaMemsetAsync(tmp, 0, sizeof(float) * (size_t)zb * slab, stream));
+            adjoint(h1, tmp, scale, w_d);
+            launch_fbp_mask(tmp, out, nb, n, m, 0.f, stream);
+            CUDA_CHECK(cudaMemcpyAsync(frec_h + (size_t)z0 * n * n, out, sizeof(float) * (size_t)nb * n * n,
+                                       cudaMemcpyDeviceToHost, stream));
+            CUDA_CHECK(cudaStreamSynchronize(stream));
+        }
+        free_geo();  // the FBP geometry is not the reconstruction's
+    }
 
     // ---- instrumentation ----
     int jgroups() const { return (m + 15) / 16; }
@@ -956,6 +1002,36 @@ int rectv_op_divergent(rectv_handle *h, float *d_fn, const float *d_h2, float la
 }  // extern "C"
 
 extern "C" {
+
+int rectv_fbp(rectv_handle *h, float *frec, const float *g, const float *theta, float center) {
+    return guarded([&] {
+        rectv::Handle *H = live(h);
+        if (!frec || !g || !theta) throw rectv::Error(RECTV_ERR_ARG, "rectv_fbp: null pointer");
+        H->fbp(frec, g, theta, center);
+    });
+}
+
+int rectv_run_init(rectv_handle *h, float *fres, const float *g, const float *theta, const float *phi,
+                   const float *finit, float center, float lambda0, float lambda1, int niter, int titer) {
+    return guarded([&] {
+        rectv::Handle *H = live(h);
+        if (!fres || !g || !theta || !phi) throw rectv::Error(RECTV_ERR_ARG, "rectv_run_init: null pointer");
+        CUDA_CHECK(cudaMemcpyAsync(H->gdata, g, sizeof(float) * (size_t)H->nz * H->ntheta * H->n,
+                                   cudaMemcpyHostToDevice, H->stream));
+        H->setup(theta, phi, center, lambda0, lambda1, titer, finit);
+        H->iterate(niter);
+        const size_t nf = (size_t)H->nzc * H->slab;
+        CUDA_CHECK(cudaMemcpyAsync(fres, H->U[H->cur], sizeof(float) * nf, cudaMemcpyDeviceToHost, H->stream));
+        CUDA_CHECK(cudaStreamSynchronize(H->stream));
+        const size_t total = (size_t)H->nz * H->slab;
+        if (total > nf) std::memset(fres + nf, 0, sizeof(float) * (total - nf));
+    });
+}
+
+int rectv_preprocess(float *out, const void *data, const void *dark, const void *flat, int dtype, int ntheta, int nz,
+                     int n, int ndark, int nflat) {
+    return guarded([&] { rectv::preprocess(out, data, dark, flat, dtype, ntheta, nz, n, ndark, nflat); });
+}
 
 int rectv_launch_kernel(rectv_handle *h, int which, int reps) {
     return guarded([&] { live(h)->launch_kernel(which, reps); });

@@ -137,4 +137,12 @@ void launch_dot(const float *a, const float *b, long long count, double *partial
                 double *out, cudaStream_t s);
 int dot_parts();
 
+// ---- filtered backprojection helpers (io_kernels.cu) ----
+void launch_filter_rows(float2 *rowsc, const float *w, long long nrows, int n, cudaStream_t s);
+void launch_fbp_mask(const float *u, float *out, int nslices, int n, int m, float r, cudaStream_t s);
+
+// ---- data ingest (io_kernels.cu) ----
+void preprocess(float *out, const void *data, const void *dark, const void *flat, int dtype, int ntheta, int nz,
+                int n, int ndark, int nflat);
+
 }  // namespace rectv

@@ -86,6 +86,16 @@ class rectv:
             self._h = None
 
     # -- extensions --
+    def run_init(self, fres, g, theta, phi, finit, center, lambda0, lambda1, niter, titer):
+        """run starting from the host array at address finit [nz][m][n][n]."""
+        _lib.check(_lib.load().rectv_run_init(self._h, _addr(fres), _addr(g), _addr(theta), _addr(phi),
+                                              _addr(finit), float(center), float(lambda0), float(lambda1),
+                                              int(niter), int(titer)))
+
+    def fbp_run(self, frec, g, theta, center):
+        """Filtered backprojection into the host array at address frec [nz][n][n]."""
+        _lib.check(_lib.load().rectv_fbp(self._h, _addr(frec), _addr(g), _addr(theta), float(center)))
+
     def set_verbose(self, verbose):
         _lib.check(_lib.load().rectv_set_verbose(self._h, int(bool(verbose))))
 

@@ -74,13 +74,18 @@ class Solver(rectv):
         """Free GPU memory due at interruptions or with-block exit."""
         self.free()
 
-    def recon(self, data, theta, phi, rot_center=None, lambda0=1e-3, lambda1=1, niter=1, titer=1):
+    def recon(self, data, theta, phi, rot_center=None, lambda0=1e-3, lambda1=1, niter=1, titer=1, *,
+              init=None):
         """Reconstruct with the time-resolved method (solver.py:45-84).
 
         data : float [nz, ntheta, n] projections; theta : float [ntheta];
         phi : float [m, 2*ntheta] temporal basis; rot_center defaults to n/2;
         lambda0, lambda1 regularisation; niter outer ADMM iterations, titer
         inner iterations.  Returns float32 [nz, m, n, n].
+
+        init (keyword, extension): None starts from zero like the reference;
+        'fbp' starts from the filtered backprojection of every slice (the same
+        image at every time sample); an array [nz, m, n, n] starts from it.
         """
         # equivalent problem: lambda0 is applied as lambda0*lambda1 (solver.py:76)
         lambda0 *= lambda1
@@ -90,9 +95,31 @@ class Solver(rectv):
         theta = _f32(theta, (self.ntheta,), "theta")
         phi = _f32(phi, (self.m, 2 * self.ntheta), "phi")
         rtv = np.zeros([self.nz, self.m, self.n, self.n], dtype="float32")
-        self.run(getp(rtv), getp(data), getp(theta), getp(phi), rot_center, lambda0, lambda1,
-                 niter, titer)
+        if init is None:
+            self.run(getp(rtv), getp(data), getp(theta), getp(phi), rot_center, lambda0, lambda1,
+                     niter, titer)
+            return rtv
+        if isinstance(init, str):
+            if init != "fbp":
+                raise ValueError("init must be None, 'fbp' or an array")
+            f0 = self.fbp(data, theta, rot_center)
+            init = np.ascontiguousarray(np.broadcast_to(f0[:, None], rtv.shape))
+        init = _f32(init, rtv.shape, "init")
+        self.run_init(getp(rtv), getp(data), getp(theta), getp(phi), getp(init), rot_center, lambda0,
+                      lambda1, niter, titer)
         return rtv
+
+    def fbp(self, data, theta, rot_center=None):
+        """Filtered backprojection of every slice (static object): float32
+        [nz, n, n], with the reference's ramp filter and circular mask
+        (applyfilter, circ: kernels_radonusfft.cuh:146-189)."""
+        if rot_center is None:
+            rot_center = self.n / 2
+        data = _f32(data, (self.nz, self.ntheta, self.n), "data")
+        theta = _f32(theta, (self.ntheta,), "theta")
+        out = np.zeros([self.nz, self.n, self.n], dtype="float32")
+        self.fbp_run(getp(out), getp(data), getp(theta), rot_center)
+        return out
 
     def adjoint_tests(self, data, theta, phi, lambda1, rot_center=None):
         """Adjoint test values (solver.py:86-93); see rectv_check_adjoints."""

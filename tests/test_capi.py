@@ -50,8 +50,10 @@ def test_solver_signature_matches_reference():
     import inspect
     from rectv_gpu_gb300 import Solver
     sig = inspect.signature(Solver.recon)
-    assert list(sig.parameters) == ["self", "data", "theta", "phi", "rot_center", "lambda0", "lambda1",
-                                    "niter", "titer"]
+    positional = [k for k, v in sig.parameters.items() if v.kind != inspect.Parameter.KEYWORD_ONLY]
+    assert positional == ["self", "data", "theta", "phi", "rot_center", "lambda0", "lambda1", "niter", "titer"]
+    extras = [k for k, v in sig.parameters.items() if v.kind == inspect.Parameter.KEYWORD_ONLY]
+    assert extras == ["init"] and sig.parameters["init"].default is None
     d = {k: v.default for k, v in sig.parameters.items()}
     assert d["rot_center"] is None and d["lambda0"] == 1e-3 and d["lambda1"] == 1
     assert d["niter"] == 1 and d["titer"] == 1
