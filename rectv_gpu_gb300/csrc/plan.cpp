@@ -29,7 +29,7 @@ inline int wrapi(int a, int m) {
 }
 }  // namespace
 
-HostPlan build_plan(const float *theta, int n, int ntheta, int T, int fwd_cap, int adj_cap) {
+HostPlan build_plan(const float *theta, int n, int ntheta, int T, int fwd_cap, int adj_cap, float tc_min_spr) {
     HostPlan p;
     const int P = 2 * n;
     const int NT = (P + T - 1) / T;
@@ -98,10 +98,30 @@ HostPlan build_plan(const float *theta, int n, int ntheta, int T, int fwd_cap, i
                     if (tl[i] >= 0) p.adj_pts[apos[tl[i]]++] = id;
             }
     }
+    // forward items: whole rays (runs of equal theta) of one tile, at most
+    // fwd_cap samples; rays with several samples each go to the tensor cores
     for (int t = 0; t < ntiles; ++t) {
-        const int c = fcnt[t];
-        for (int st = 0; st < c; st += fwd_cap)
-            p.fwd_items.push_back(make_int4(t, (int)(foff[t] + st), std::min(fwd_cap, c - st), 0));
+        long long i = foff[t];
+        const long long e = foff[t + 1];
+        while (i < e) {
+            long long j = i;
+            int nrays = 0;
+            while (j < e) {
+                const uint32_t th = p.fwd_pts[j] / (uint32_t)n;
+                long long r = j;
+                while (r < e && p.fwd_pts[r] / (uint32_t)n == th) ++r;
+                if (r - i > fwd_cap) break;
+                j = r;
+                ++nrays;
+            }
+            if (nrays == 0) throw Error(1, "ray longer than a gather work item");
+            const int cnt = (int)(j - i);
+            if (tc_min_spr >= 0.f && cnt >= tc_min_spr * nrays)
+                p.fwd_tc_items.push_back(make_int4(t, (int)i, cnt, nrays));
+            else
+                p.fwd_items.push_back(make_int4(t, (int)i, cnt, 0));
+            i = j;
+        }
     }
     for (int t = 0; t < ntiles; ++t) {
         const int c = acnt[t];

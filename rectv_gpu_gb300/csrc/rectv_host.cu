@@ -108,6 +108,7 @@ struct Handle {
 
     // cuFFT
     cufftHandle p_r2c2d = 0, p_c2c2d = 0, p_rows_c2c = 0, p_rows_r2c = 0;
+    CUtensorMap spec_tmap;  // TMA boxes of the forward spectra (tensor-core gather)
     bool plans_made = false;
     int img_per_fft = 0;
     void *fft_work = nullptr;
@@ -151,13 +152,16 @@ struct Handle {
     void init() {
         CUDA_CHECK(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
         usfft_prepare();
+        gather_tc_prepare();
         const int P = 2 * n;
         ug.n = n;
         ug.ntheta = ntheta;
         ug.m = m;
         ug.P = P;
         ug.hp = P / 2 + 1;
-        ug.img_fwd = (long long)P * ug.hp;
+        ug.qp = n + 2 * kHalo + (n & 1);
+        ug.qoff = (long long)kHalo * ug.qp + kHalo;
+        ug.img_fwd = (long long)(P + 2 * kHalo) * ug.qp;
         ug.img_adj = (long long)P * P;
         ug.tn = (float)(2 * n);
         ug.inv2n = (float)(1.0 / (2.0 * n));
@@ -190,9 +194,10 @@ struct Handle {
         mu = dalloc<float>((size_t)4 * nchunks * gp, owned);
         h1 = dalloc<float>((size_t)zb * ntheta * n, owned);
         // spectra; also the float4 gradient scratch of check_adjoints
-        const size_t spec_elems =
-            std::max<size_t>((size_t)zb * m * (size_t)ug.img_adj, (size_t)2 * (n + 1) * (n + 1) * (m + 1) * (nzp + 1));
+        const size_t spec_elems = std::max<size_t>(
+            (size_t)zb * m * (size_t)std::max(ug.img_adj, ug.img_fwd), (size_t)2 * (n + 1) * (n + 1) * (m + 1) * (nzp + 1));
         spec = dalloc<float2>(spec_elems, owned);
+        make_spec_tensor_map(&spec_tmap, spec, zb * m, ug);
         rows = dalloc<float2>((size_t)zb * ntheta * (size_t)std::max(n, n / 2 + 1), owned);
 
         tv.n = n;
@@ -244,11 +249,12 @@ struct Handle {
         CUFFT_CHECK(cufftCreate(&p_rows_r2c));
         plans_made = true;
         for (cufftHandle h : {p_r2c2d, p_c2c2d, p_rows_c2c, p_rows_r2c}) CUFFT_CHECK(cufftSetAutoAllocation(h, 0));
-        {  // 2D R2C in place: real rows of P+2 floats -> P/2+1 complex
+        {  // 2D R2C in place inside the padded forward images: real rows of
+           // 2 qp floats -> P/2+1 complex of a qp-complex row
             int nn[2] = {P, P};
-            int inem[2] = {P, P + 2};
-            int onem[2] = {P, P / 2 + 1};
-            CUFFT_CHECK(cufftMakePlanMany(p_r2c2d, 2, nn, inem, 1, P * (P + 2), onem, 1, P * (P / 2 + 1),
+            int inem[2] = {P, 2 * ug.qp};
+            int onem[2] = {P, ug.qp};
+            CUFFT_CHECK(cufftMakePlanMany(p_r2c2d, 2, nn, inem, 1, (int)(2 * ug.img_fwd), onem, 1, (int)ug.img_fwd,
                                           CUFFT_R2C, per, &w1));
             ws = std::max(ws, w1);
         }
@@ -316,6 +322,9 @@ struct Handle {
         session = false;
     }
 
+    // 16 time samples per gather pass (the tensor-core gather's K)
+    bool mp16() const { return m > 8; }
+
     void check_live() const {
         if (freed) throw Error(RECTV_ERR_STATE, "rectv: object was freed");
     }
@@ -326,7 +335,16 @@ struct Handle {
         free_geo();
         // gather items hold at most one sample table; scatter items are whole
         // tiles (one block owns each tile, so tiles are stored, never added)
-        HostPlan hp = build_plan(theta_h, n, ntheta, ug.T, table_capacity(), 1 << 30);
+        // forward items with >= 2 samples per ray use the tensor-core gather
+        // (time samples are mixed once per ray); RECTV_GATHER=direct|tc forces
+        // one kernel (A/B comparisons).  Below 9 time samples the direct
+        // kernel's shared-memory rows are short and it stays the only one.
+        float tc_min_spr = (mp16() ? 2.0f : -1.0f);
+        if (const char *e = std::getenv("RECTV_GATHER")) {
+            if (!std::strcmp(e, "direct")) tc_min_spr = -1.0f;
+            if (!std::strcmp(e, "tc") && mp16()) tc_min_spr = 0.0f;
+        }
+        HostPlan hp = build_plan(theta_h, n, ntheta, ug.T, table_capacity(), 1 << 30, tc_min_spr);
         auto up = [&](const void *src, size_t bytes) -> void * {
             void *p = nullptr;
             CUDA_CHECK(cudaMalloc(&p, std::max<size_t>(bytes, 16)));
@@ -338,6 +356,8 @@ struct Handle {
         gd.fwd_pts = (uint32_t *)up(hp.fwd_pts.data(), hp.fwd_pts.size() * 4);
         gd.fwd_items = (int4 *)up(hp.fwd_items.data(), hp.fwd_items.size() * sizeof(int4));
         gd.n_fwd_items = (int)hp.fwd_items.size();
+        gd.fwd_tc_items = (int4 *)up(hp.fwd_tc_items.data(), hp.fwd_tc_items.size() * sizeof(int4));
+        gd.n_fwd_tc_items = (int)hp.fwd_tc_items.size();
         gd.adj_pts = (uint32_t *)up(hp.adj_pts.data(), hp.adj_pts.size() * 4);
         gd.adj_items = (int4 *)up(hp.adj_items.data(), hp.adj_items.size() * sizeof(int4));
         gd.n_adj_items = (int)hp.adj_items.size();
@@ -396,10 +416,11 @@ struct Handle {
         launch_deapod_pad(u, reinterpret_cast<float *>(spec), zb * m, gd.deapod, ug, stream);
         const int nimg = zb * m;
         for (int i = 0; i < nimg; i += img_per_fft) {
-            cufftComplex *p = reinterpret_cast<cufftComplex *>(spec + (size_t)i * ug.img_fwd);
+            cufftComplex *p = reinterpret_cast<cufftComplex *>(spec + (size_t)i * ug.img_fwd + ug.qoff);
             CUFFT_CHECK(cufftExecR2C(p_r2c2d, reinterpret_cast<cufftReal *>(p), p));
         }
-        launch_gather_fwd(spec, rows, zb, gd, ug, stream);
+        launch_spec_halo(spec, nimg, ug, stream);
+        launch_gather_fwd(spec, rows, zb, gd, ug, &spec_tmap, stream);
         CUFFT_CHECK(cufftExecC2C(p_rows_c2c, reinterpret_cast<cufftComplex *>(rows),
                                  reinterpret_cast<cufftComplex *>(rows), CUFFT_INVERSE));
         launch_finish_fwd(rows, gb, out, zb, tau, residual, ug, stream);
@@ -584,7 +605,7 @@ struct Handle {
         int errs = 0;
         CUDA_CHECK(cudaMemcpyAsync(&errs, gd.err, sizeof(int), cudaMemcpyDeviceToHost, stream));
         CUDA_CHECK(cudaStreamSynchronize(stream));
-        if (errs) throw Error(RECTV_ERR_STATE, "rectv: internal plan/stencil mismatch");
+        if (errs) throw Error(RECTV_ERR_STATE, "rectv: internal kernel error (plan/stencil mismatch or tensor-core wait timeout)");
     }
 
     // ---- operator API helpers: any number of slices via zero-padded batches ----
@@ -704,7 +725,7 @@ struct Handle {
         if (!session) throw Error(RECTV_ERR_STATE, "rectv_launch_kernel: needs a set-up session");
         for (int r = 0; r < reps; ++r) {
             switch (which) {
-                case 0: launch_gather_fwd(spec, rows, zb, gd, ug, stream); break;
+                case 0: launch_gather_fwd(spec, rows, zb, gd, ug, &spec_tmap, stream); break;
                 case 1: launch_scatter_adj(rows, spec, zb, gd, ug, stream); break;
                 case 2: launch_graddiv(U[cur], U[cur], U[(cur + 1) % 3], psi, mu, rho_d, 0, nchunks, tv, stream); break;
                 case 3:  // overwrites the session's dual variables

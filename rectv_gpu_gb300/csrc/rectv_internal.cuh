@@ -10,6 +10,7 @@
 //           complex in-place R2C (adjoint)
 #pragma once
 
+#include <cuda.h>
 #include <cuda_runtime.h>
 #include <cufft.h>
 #include <cstdint>
@@ -23,6 +24,8 @@ namespace rectv {
 // kernels are specialised for it and the host checks the formula.
 constexpr int kR = 4;
 constexpr int kTaps = 2 * kR + 1;
+// halo of the stored forward spectra (see UsGeo::qp)
+constexpr int kHalo = 24;
 // The USFFT kernels of the reference use this truncated value of pi
 // (kernels_radonusfft.cuh:1).
 constexpr double kPiUsfft = 3.1415926535;
@@ -43,7 +46,13 @@ struct UsGeo {
     int n, ntheta, m;   // detector width, projections, time samples
     int P;              // oversampled grid side 2n
     int hp;             // half-plane row length P/2+1 (complex)
-    long long img_fwd;  // complex elements per forward image (P*hp)
+    // Forward spectra are stored as the window rows [-kHalo, P+kHalo) x
+    // columns [-kHalo, n+kHalo) of the periodic full spectrum: the R2C output
+    // (rows [0,P), columns [0,n]) plus a halo of wrapped / Hermitian-mirrored
+    // cells, so that every tile footprint is one rectangular box.
+    int qp;             // row pitch of a forward image (complex), even
+    long long qoff;     // offset of cell (0, 0) in a forward image
+    long long img_fwd;  // complex elements per forward image ((P + 2 kHalo) qp)
     long long img_adj;  // complex elements per adjoint image (P*P)
     float tn;           // (float)(2n)
     float inv2n;        // 1/(2n)
@@ -61,8 +70,10 @@ struct GeoDev {
     float2 *shiftadj = nullptr;  // [n]
     float *deapod = nullptr;     // [n] exp(mu (x-n/2)^2)
     uint32_t *fwd_pts = nullptr; // point ids theta*n+k sorted by tile
-    int4 *fwd_items = nullptr;   // (tile, start, count, 0)
+    int4 *fwd_items = nullptr;   // (tile, start, count, 0): direct gather (k_gather_fwd)
     int n_fwd_items = 0;
+    int4 *fwd_tc_items = nullptr; // (tile, start, count, rays): tensor-core gather (k_gather_tc)
+    int n_fwd_tc_items = 0;
     uint32_t *adj_pts = nullptr; // point ids, one entry per tile a stencil touches
     int4 *adj_items = nullptr;   // (tile, start, count, split)
     int n_adj_items = 0;
@@ -76,18 +87,24 @@ struct HostPlan {
     std::vector<float2> sincos;
     std::vector<uint32_t> fwd_pts;
     std::vector<int4> fwd_items;
+    std::vector<int4> fwd_tc_items;
     std::vector<uint32_t> adj_pts;
     std::vector<int4> adj_items;
     std::vector<int> split_tiles;
 };
 
-HostPlan build_plan(const float *theta, int n, int ntheta, int T, int fwd_cap, int adj_cap);
+// Forward work items hold whole rays of one tile and at most fwd_cap samples;
+// an item with at least tc_min_spr samples per ray goes to the tensor-core
+// gather (tc_min_spr < 0: none does).
+HostPlan build_plan(const float *theta, int n, int ntheta, int T, int fwd_cap, int adj_cap, float tc_min_spr);
 
 // ---- USFFT kernel launchers (usfft_kernels.cu) ----
 void launch_deapod_pad(const float *u, float *spec, int nimg, const float *deapod, const UsGeo &g,
                        cudaStream_t s);
+// fill the halo of nimg forward spectra after the R2C transform
+void launch_spec_halo(float2 *spec, int nimg, const UsGeo &g, cudaStream_t s);
 void launch_gather_fwd(const float2 *spec, float2 *rows, int zb, const GeoDev &gd, const UsGeo &g,
-                       cudaStream_t s);
+                       const CUtensorMap *tmap, cudaStream_t s);
 void launch_finish_fwd(const float2 *rows, const float *gdata, float *out, int zb, float tau,
                        int residual, const UsGeo &g, cudaStream_t s);
 void launch_adj_prep(const float *h, float *rowsr, int zb, const UsGeo &g, cudaStream_t s);
@@ -96,6 +113,16 @@ void launch_scatter_adj(const float2 *rowsc, float2 *spec, int zb, const GeoDev 
                         const UsGeo &g, cudaStream_t s);
 void launch_crop_accum(const float2 *spec, float *u, int zb, float tau, const float *deapod,
                        const UsGeo &g, cudaStream_t s);
+// tensor-core gather (gather_tc.cu): items of fwd_tc_items, time samples
+// [jbase, jbase + 16)
+void launch_gather_tc(float2 *rows, int zb, const GeoDev &gd, const UsGeo &g, const CUtensorMap &tmap, int jbase,
+                      int accumulate, cudaStream_t s);
+// TMA descriptor of the forward spectra of a batch (zb*m images), boxes of
+// 16 images x 24 rows x 26 cells
+void make_spec_tensor_map(CUtensorMap *map, float2 *spec, int nimg, const UsGeo &g);
+void gather_tc_prepare();
+size_t gather_tc_smem();
+int gather_tc_table_capacity();
 size_t gather_fwd_smem(const UsGeo &g);
 size_t scatter_adj_smem(const UsGeo &g);
 void usfft_prepare();  // kernel attributes; call once, outside stream capture

@@ -19,37 +19,11 @@
 #include <cuda_runtime.h>
 
 #include "rectv_internal.cuh"
+#include "usfft_common.cuh"
 
 namespace rectv {
 
 namespace {
-
-__device__ __forceinline__ float2 cmul(float2 a, float2 b) {
-    return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
-}
-
-// Position of polar sample (theta, k): identical float operation sequence to
-// the host plan (plan.cpp) and to takexy (kernels_radonusfft.cuh:73-78).
-__device__ __forceinline__ void sample_pos(int k, float2 sc, const UsGeo &g, float &x0, float &y0,
-                                           int &fx, int &fy) {
-    const float q = __fdiv_rn((float)(k - g.n / 2), (float)g.n);
-    x0 = __fmul_rn(q, sc.x);
-    y0 = __fmul_rn(q, sc.y);
-    if (x0 >= 0.5f) x0 = 0.5f - 1e-5f;
-    if (y0 >= 0.5f) y0 = 0.5f - 1e-5f;
-    fx = (int)floorf(__fmul_rn(g.tn, x0));
-    fy = (int)floorf(__fmul_rn(g.tn, y0));
-}
-
-// Separable Gaussian weights exp(-pi^2/mu d^2) of the 9 taps per axis
-// (gather, kernels_radonusfft.cuh:116-118; pi/mu and 1/n are applied once).
-__device__ __forceinline__ void tap_weights(int f, float p0, const UsGeo &g, float (&e)[kTaps]) {
-#pragma unroll
-    for (int i = 0; i < kTaps; ++i) {
-        const float d = (float)(f - kR + i) * g.inv2n - p0;
-        e[i] = __expf(-g.wexp * d * d);
-    }
-}
 
 __device__ __forceinline__ void cp_async8(void *smem, const void *gmem) {
     const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
@@ -64,15 +38,17 @@ __device__ __forceinline__ void cp_async_wait_all() {
 
 // ---------------------------------------------------------------------------
 // Forward: deapodise, zero-pad to P x P and modulate by (-1)^(X+Y)
-// (divphi + fftshift, kernels_radonusfft.cuh:4-38), writing the in-place R2C
-// layout (rows of P+2 floats).
+// (divphi + fftshift, kernels_radonusfft.cuh:4-38), writing the real input of
+// the in-place R2C transform: row Y of image img starts at complex element
+// img_fwd*img + qoff + Y*qp (2*qp floats per row, P+2 written).
 // ---------------------------------------------------------------------------
-__global__ void k_deapod_pad(const float *__restrict__ u, float *__restrict__ spec,
-                             const float *__restrict__ dp, int n, int P, float inv4n2) {
+__global__ void k_deapod_pad(const float *__restrict__ u, float2 *__restrict__ spec,
+                             const float *__restrict__ dp, UsGeo g, float inv4n2) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;  // float pair in the row
     const int Y = blockIdx.y;
     const long long img = blockIdx.z;
-    const int npair = (P + 2) / 2;
+    const int n = g.n;
+    const int npair = (g.P + 2) / 2;
     if (i >= npair) return;
     const int X = 2 * i;
     float2 v = make_float2(0.f, 0.f);
@@ -84,7 +60,7 @@ __global__ void k_deapod_pad(const float *__restrict__ u, float *__restrict__ sp
         if (x0 >= 0 && x0 < n) v.x = row[x0] * dp[x0] * sy;   // X even: +1
         if (x1 >= 0 && x1 < n) v.y = -row[x1] * dp[x1] * sy;  // X+1 odd: -1
     }
-    reinterpret_cast<float2 *>(spec + img * (long long)P * (P + 2) + (long long)Y * (P + 2))[i] = v;
+    spec[img * g.img_fwd + g.qoff + (long long)Y * g.qp + i] = v;
 }
 
 void launch_deapod_pad(const float *u, float *spec, int nimg, const float *deapod, const UsGeo &g,
@@ -92,8 +68,52 @@ void launch_deapod_pad(const float *u, float *spec, int nimg, const float *deapo
     const int npair = (g.P + 2) / 2;
     dim3 bs(256), gs((npair + 255) / 256, g.P, nimg);
     const float inv4n2 = (float)(1.0 / (4.0 * g.n * (double)g.n));
-    k_deapod_pad<<<gs, bs, 0, s>>>(u, spec, deapod, g.n, g.P, inv4n2);
+    k_deapod_pad<<<gs, bs, 0, s>>>(u, reinterpret_cast<float2 *>(spec), deapod, g, inv4n2);
     LAUNCH_CHECK("k_deapod_pad");
+}
+
+// ---------------------------------------------------------------------------
+// Halo of the stored forward spectra: cell (y, x) of the window rows
+// [-kHalo, P+kHalo) x columns [-kHalo, n+kHalo) outside the R2C output gets
+// the periodic full-spectrum value F(y mod P, x mod P), read through the
+// Hermitian symmetry F(a, b) = conj F(-a, -b) of a real input when b > n.
+// One thread per halo cell: 2 kHalo full rows, then 2 kHalo - 1 columns of
+// every interior row.
+// ---------------------------------------------------------------------------
+__global__ void k_spec_halo(float2 *__restrict__ spec, UsGeo g) {
+    const int P = g.P, n = g.n;
+    const long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    const long long wide = (long long)(2 * kHalo) * g.qp;  // cells of the full halo rows
+    const int side = g.qp - (n + 1);                        // halo columns of an interior row
+    if (e >= wide + (long long)P * side) return;
+    int y, x;
+    if (e < wide) {
+        const int r = (int)(e / g.qp);
+        x = (int)(e - (long long)r * g.qp) - kHalo;
+        y = (r < kHalo) ? r - kHalo : P + (r - kHalo);
+    } else {
+        const long long e2 = e - wide;
+        y = (int)(e2 / side);
+        const int c = (int)(e2 - (long long)y * side);
+        x = (c < kHalo) ? c - kHalo : n + 1 + (c - kHalo);
+    }
+    float2 *img = spec + (long long)blockIdx.y * g.img_fwd + g.qoff;
+    const int a = ((y % P) + P) % P, b = ((x % P) + P) % P;
+    float2 v;
+    if (b <= n) {
+        v = img[(long long)a * g.qp + b];
+    } else {
+        v = img[(long long)((P - a) % P) * g.qp + (P - b)];
+        v.y = -v.y;
+    }
+    img[(long long)y * g.qp + x] = v;
+}
+
+void launch_spec_halo(float2 *spec, int nimg, const UsGeo &g, cudaStream_t s) {
+    const long long cells = (long long)(2 * kHalo) * g.qp + (long long)g.P * (g.qp - (g.n + 1));
+    dim3 gs((unsigned)((cells + 255) / 256), nimg);
+    k_spec_halo<<<gs, 256, 0, s>>>(spec, g);
+    LAUNCH_CHECK("k_spec_halo");
 }
 
 // ---------------------------------------------------------------------------
@@ -178,8 +198,8 @@ __global__ void __launch_bounds__(kThreads)
             int KX = txi * T - kR + col;
             KX += (KX < 0) ? P : 0;
             KX -= (KX >= P) ? P : 0;
-            const long long so = (KX <= half) ? (long long)KY * g.hp + KX
-                                              : (long long)(KY ? P - KY : 0) * g.hp + (P - KX);
+            const long long so = g.qoff + ((KX <= half) ? (long long)KY * g.qp + KX
+                                                        : (long long)(KY ? P - KY : 0) * g.qp + (P - KX));
             const float2 *src = img0 + (long long)jbase * g.img_fwd + so;
             float2 *dst = tile + cell * MP;
             const int sw = col & (MP - 1);
@@ -326,7 +346,7 @@ __global__ void k_zero_k0(float2 *rows, long long nrows, int n) {
 }
 
 void launch_gather_fwd(const float2 *spec, float2 *rows, int zb, const GeoDev &gd, const UsGeo &g,
-                       cudaStream_t s) {
+                       const CUtensorMap *tmap, cudaStream_t s) {
     const long long nrows = (long long)zb * g.ntheta;
     k_zero_k0<<<(unsigned)((nrows + 255) / 256), 256, 0, s>>>(rows, nrows, g.n);
     LAUNCH_CHECK("k_zero_k0");
@@ -334,6 +354,8 @@ void launch_gather_fwd(const float2 *spec, float2 *rows, int zb, const GeoDev &g
     const int mp = mp_for(g.m);
     for (int jb = 0; jb < g.m; jb += 16) {
         const int acc = jb > 0;
+        if (mp == 16) launch_gather_tc(rows, zb, gd, g, *tmap, jb, acc, s);
+        if (gd.n_fwd_items == 0) continue;
         switch (mp) {
             case 1: gather_fwd_t<1, 16>(spec, rows, zb, gd, g, jb, acc, gd.err, s); break;
             case 2: gather_fwd_t<2, 16>(spec, rows, zb, gd, g, jb, acc, gd.err, s); break;

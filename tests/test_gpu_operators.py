@@ -38,6 +38,8 @@ CASES = [
     (40, 60, 5, 2, 2, 2, 0.0),     # m not a power of two, 2n not a multiple of 16
     (64, 100, 1, 1, 1, 1, 0.0),
     (32, 64, 20, 1, 1, 4, 0.0),    # m > 16: two passes over time-sample groups
+    (128, 360, 16, 2, 2, 8, 1.5),  # tensor-core gather, several ray chunks per item
+    (96, 240, 12, 1, 1, 4, 0.0),   # tensor-core gather with zero-padded time samples
 ]
 
 
@@ -140,3 +142,32 @@ def test_gradient_divergent_match_oracle(env, flg):
     ref = orc.divergent(h.astype(np.float64), lam1, -0.5)
     obj.free()
     assert rel(got, ref) < 1e-5
+
+
+@pytest.mark.parametrize("case", [(128, 360, 16, 2, 8, 1.5), (64, 180, 24, 1, 4, 0.0), (80, 200, 9, 1, 2, -2.0)])
+def test_gather_paths_agree(env, case, monkeypatch):
+    """The tensor-core gather (ray-wise time-sample mixing on tcgen05 with a
+    three-term TF32/BF16 split) and the direct FP32 gather give the same
+    forward operator: both within OP_TOL of the oracle, and within 5e-6 of
+    each other."""
+    torch, rectv = env
+    n, ntheta, m, nz, nrot, dc = case
+    center = n / 2 + dc
+    theta, phi = _geometry(n, ntheta, m, nrot, 7)
+    f = np.random.default_rng(2).standard_normal((nz, m, n, n)).astype(np.float32)
+    ref = orc.Operators(n, ntheta, m, theta, phi, center).radonapr(f.astype(np.float64), 1.0)
+    dth, dph, df = dev(torch, theta), dev(torch, phi), dev(torch, f)
+    out = {}
+    for mode in ("direct", "tc", "auto"):
+        monkeypatch.setenv("RECTV_GATHER", mode)
+        obj = rectv(n, ntheta, m, nz, nz, 1)
+        dg = torch.zeros((nz, ntheta, n), dtype=torch.float32, device="cuda")
+        torch.cuda.synchronize()
+        obj.op_set_geometry(dth.data_ptr(), dph.data_ptr(), center)
+        obj.op_radonapr(dg.data_ptr(), df.data_ptr(), nz, 1.0)
+        out[mode] = dg.cpu().numpy()
+        obj.free()
+    for mode, got in out.items():
+        assert rel(got, ref) < OP_TOL, (mode, rel(got, ref))
+    assert rel(out["tc"], out["direct"].astype(np.float64)) < 5e-6
+    assert rel(out["auto"], out["direct"].astype(np.float64)) < 5e-6
