@@ -153,6 +153,7 @@ struct Handle {
         CUDA_CHECK(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
         usfft_prepare();
         gather_tc_prepare();
+        scatter_tc_prepare();
         const int P = 2 * n;
         ug.n = n;
         ug.ntheta = ntheta;
@@ -345,6 +346,11 @@ struct Handle {
             if (!std::strcmp(e, "tc") && mp16()) tc_min_spr = 0.0f;
         }
         HostPlan hp = build_plan(theta_h, n, ntheta, ug.T, table_capacity(), 1 << 30, tc_min_spr);
+        // adjoint: RECTV_SCATTER=tc selects the tensor-core time-sample mixing
+        // (k_scatter_tc); the direct FP32 scatter is the default
+        bool tc_scatter = false;
+        if (const char *e = std::getenv("RECTV_SCATTER"))
+            if (!std::strcmp(e, "tc") && mp16()) tc_scatter = true;
         auto up = [&](const void *src, size_t bytes) -> void * {
             void *p = nullptr;
             CUDA_CHECK(cudaMalloc(&p, std::max<size_t>(bytes, 16)));
@@ -363,6 +369,7 @@ struct Handle {
         gd.n_adj_items = (int)hp.adj_items.size();
         gd.split_tiles = (int *)up(hp.split_tiles.data(), hp.split_tiles.size() * 4);
         gd.n_split_tiles = (int)hp.split_tiles.size();
+        gd.tc_scatter = tc_scatter;
         if (gd.n_fwd_items > 2147483647 || gd.n_adj_items > 2147483647)
             throw Error(RECTV_ERR_ARG, "rectv: plan too large");
 

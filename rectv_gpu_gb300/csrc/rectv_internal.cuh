@@ -80,6 +80,7 @@ struct GeoDev {
     int *split_tiles = nullptr;  // tiles with more than one adjoint item
     int n_split_tiles = 0;
     int *err = nullptr;          // device counter of host/device bin disagreements
+    bool tc_scatter = false;     // adjoint time-sample mixing on the tensor cores (k_scatter_tc)
 };
 
 // Host-side angle plan (built in plan.cpp).
@@ -121,6 +122,10 @@ void launch_gather_tc(float2 *rows, int zb, const GeoDev &gd, const UsGeo &g, co
 // 16 images x 24 rows x 26 cells
 void make_spec_tensor_map(CUtensorMap *map, float2 *spec, int nimg, const UsGeo &g);
 void gather_tc_prepare();
+// tensor-core scatter (scatter_tc.cu): all adjoint items, time samples [jbase, jbase + 16)
+void launch_scatter_tc(const float2 *rowsc, float2 *spec, int zb, const GeoDev &gd, const UsGeo &g, int jbase,
+                       cudaStream_t s);
+void scatter_tc_prepare();
 size_t gather_tc_smem();
 int gather_tc_table_capacity();
 size_t gather_fwd_smem(const UsGeo &g);

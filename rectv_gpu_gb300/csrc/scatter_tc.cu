@@ -1,0 +1,320 @@
+// Adjoint USFFT scatter with the time-sample mixing on the tensor cores
+// (tcgen05).
+//
+// The adjoint (gather TOMO_ADJ + wrap TOMO_ADJ, kernels_radonusfft.cuh:40-144,
+// fused with shift/fftshift of radonusfft.cu:115-121 and the basis weights of
+// operators.cu:171-176) adds, for every polar sample p on ray theta, the
+// value conj(K'(theta, j)) w(p, c) E(p) to cell c of time sample j's grid.
+// Along one ray the factor conj(K'(theta, j)) is common to all samples, so
+//  1. each thread (one cell of the 16x16 tile) first sums its value of the
+//     single complex per-ray grid V(c, theta) = sum_p w(p, c) E(p) over the
+//     ray's samples (in plan order, so sums are reproducible; no atomics);
+//  2. the time samples are then a GEMM over rays:
+//     F(c, j) += sum_theta V(c, theta) conj(K'(theta, j)),
+//     [256 cells x 32] x [32 x 32] real per batch of 16 rays (K index
+//     2r + re/im of V; N index 2j + re/im of F), on the tensor cores with the
+//     three TF32 terms Vhi Khi + Vhi Klo + Vlo Khi for FP32 accuracy (the
+//     tensor core truncates FP32 input to TF32; lo = x - trunc(x)).
+// Each batch's product is formed in tensor memory (12 MMAs) and added to the
+// cell's FP32 sums in registers with IEEE adds -- the tensor core's FP32
+// accumulation rounds differently, and the thousands of batches of a tile
+// near the centre of the spectrum would otherwise drift.  The tile is stored
+// once (added, for a tile split over blocks).  One block of 256 threads per
+// (tile, slice); thread = cell.
+#include <cuda.h>
+#include <cuda_runtime.h>
+
+#include "rectv_internal.cuh"
+#include "tcgen05.cuh"
+#include "usfft_common.cuh"
+
+namespace rectv {
+
+namespace {
+
+constexpr int kT = 16;
+constexpr int kCells = kT * kT;     // 256 = 2 M tiles
+constexpr int kMT = kCells / 128;
+constexpr int kTab = 256;           // samples per table
+constexpr int kBatch = 16;          // rays per MMA batch (K = 32)
+constexpr int kK = 2 * kBatch;
+constexpr int kN = 32;              // 16 time samples x (re, im)
+constexpr int kThr = kCells;
+constexpr int kWarps = kThr / 32;
+constexpr uint32_t kTmemCols = 256;
+constexpr uint32_t kColAhi = 0;             // [mt*32, +32)
+constexpr uint32_t kColAlo = kMT * kK;      // 64
+constexpr uint32_t kColD = 2 * kMT * kK;    // 128: F accumulators [mt*32, +32)
+
+__device__ __forceinline__ int off32(int row, int kk) {
+    return (row >> 3) * 256 + (kk >> 2) * 32 + (row & 7) * 4 + (kk & 3);
+}
+
+struct ScTcSmem {
+    float w[kTab][20];            // 9 x weights, 9 y weights (16-byte rows)
+    int cb[kTab];                 // packed (dx + 32) | (dy + 32) << 8 of the stencil origin
+    int th[kTab];
+    float2 f[kTab];               // E(theta, k) of this slice
+    float bhi[kN * kK];           // B = conj K' of the batch's rays, FP32
+    float blo[kN * kK];           // B - trunc(B)
+    int seg_first[kTab + 1];
+    int wsum[kWarps];
+    unsigned long long bar;
+    uint32_t tslot;
+};
+
+__device__ __forceinline__ void st32(uint32_t taddr, const float (&v)[32]) {
+    asm volatile(
+        "tcgen05.st.sync.aligned.32x32b.x16.b32 [%0], {%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,%16};\n" ::"r"(
+            taddr),
+        "f"(v[0]), "f"(v[1]), "f"(v[2]), "f"(v[3]), "f"(v[4]), "f"(v[5]), "f"(v[6]), "f"(v[7]), "f"(v[8]), "f"(v[9]),
+        "f"(v[10]), "f"(v[11]), "f"(v[12]), "f"(v[13]), "f"(v[14]), "f"(v[15])
+        : "memory");
+    asm volatile(
+        "tcgen05.st.sync.aligned.32x32b.x16.b32 [%0], {%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,%16};\n" ::"r"(
+            taddr + 16),
+        "f"(v[16]), "f"(v[17]), "f"(v[18]), "f"(v[19]), "f"(v[20]), "f"(v[21]), "f"(v[22]), "f"(v[23]), "f"(v[24]),
+        "f"(v[25]), "f"(v[26]), "f"(v[27]), "f"(v[28]), "f"(v[29]), "f"(v[30]), "f"(v[31])
+        : "memory");
+}
+
+__device__ __forceinline__ void mma_tf32_ts(uint32_t d, uint32_t a, uint64_t b, uint32_t id, uint32_t acc) {
+    asm volatile(
+        "{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\n"
+        "tcgen05.mma.cta_group::1.kind::tf32 [%0], [%1], %2, %3, p;\n}\n" ::"r"(d),
+        "r"(a), "l"(b), "r"(id), "r"(acc)
+        : "memory");
+}
+
+}  // namespace
+
+__global__ void __launch_bounds__(kThr, 2)
+    k_scatter_tc(const float2 *__restrict__ rowsc, float2 *__restrict__ spec, const uint32_t *__restrict__ pts,
+                 const int4 *__restrict__ items, const float2 *__restrict__ sincos,
+                 const float2 *__restrict__ kmat, const float2 *__restrict__ shifta, UsGeo g, int jbase,
+                 int *__restrict__ err) {
+    extern __shared__ __align__(1024) unsigned char sc_smem_raw[];
+    ScTcSmem &sm = *reinterpret_cast<ScTcSmem *>(sc_smem_raw);
+    const int4 it = items[blockIdx.x];
+    const int z = blockIdx.y;
+    const int tyi = it.x / g.NT, txi = it.x - tyi * g.NT;
+    const int P = g.P, half = P / 2, hn = g.n / 2 + 1;
+    const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+    const float2 *rz = rowsc + (long long)z * g.ntheta * hn;
+    if (wid == 0) tc::alloc(&sm.tslot, kTmemCols);
+    if (tid == 0) {
+        tc::mbar_init(&sm.bar, 1);
+        tc::fence_mbar_init();
+    }
+    tc::fence_before();
+    __syncthreads();
+    tc::fence_after();
+    const uint32_t tbase = sm.tslot;
+    const int mt = wid >> 2, q = wid & 3;  // this thread's cell tid = mt*128 + 32q + lane
+    const int cx = tid % kT, cy = tid / kT;  // its column and row in the tile (warp w: rows 2w, 2w+1)
+    bool ok = true;
+    int nmma = 0;  // MMA batches issued
+    float acc[32];  // F of this cell: 16 time samples x (re, im)
+#pragma unroll
+    for (int i = 0; i < 32; ++i) acc[i] = 0.f;
+
+    for (int c0 = 0; c0 < it.z; c0 += kTab) {
+        const int cnt = min(kTab, it.z - c0);
+        __syncthreads();  // previous table consumed
+        for (int e = tid; e < cnt; e += kThr) {
+            const uint32_t id = __ldg(pts + it.y + c0 + e);
+            const int th = id / (uint32_t)g.n;
+            const int k = id - th * g.n;
+            float x0, y0;
+            int fx, fy;
+            sample_pos(k, __ldg(sincos + th), g, x0, y0, fx, fy);
+            int dx = g.n + fx - kR - txi * kT;
+            int dy = g.n + fy - kR - tyi * kT;
+            dx += (dx < -half) ? P : 0;
+            dx -= (dx > half) ? P : 0;
+            dy += (dy < -half) ? P : 0;
+            dy -= (dy > half) ? P : 0;
+#pragma unroll
+            for (int i = 0; i < kTaps; ++i) {
+                sm.w[e][i] = tap_weight(fx, i, x0, g);
+                sm.w[e][kTaps + i] = tap_weight(fy, i, y0, g);
+            }
+            // stencils of listed samples start within [-2r, T) of the tile
+            sm.cb[e] = ((dx + 32) & 0xff) | (((dy + 32) & 0xff) << 8);
+            sm.th[e] = th;
+            // E = (-1)^(k+1) shiftadj(k) FFT(row)(k) (pi/mu)/n  (Hermitian row spectrum)
+            float2 R = (k <= g.n / 2) ? __ldg(rz + (long long)th * hn + k) : __ldg(rz + (long long)th * hn + (g.n - k));
+            if (k > g.n / 2) R.y = -R.y;
+            const float2 E = cmul(R, __ldg(shifta + k));
+            const float c = (k & 1) ? g.cw : -g.cw;
+            sm.f[e] = make_float2(E.x * c, E.y * c);
+        }
+        __syncthreads();
+        // ---- first table row of each ray: block-wide scan of ray starts ----
+        int flag = 0;
+        if (tid < cnt) flag = (tid == 0 || sm.th[tid] != sm.th[tid - 1]) ? 1 : 0;
+        int incl = flag;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int y = __shfl_up_sync(0xffffffffu, incl, o);
+            if (lane >= o) incl += y;
+        }
+        if (lane == 31) sm.wsum[wid] = incl;
+        __syncthreads();
+        int base = 0, nseg = 0;
+#pragma unroll
+        for (int w = 0; w < kWarps; ++w) {
+            const int v = sm.wsum[w];
+            base += (w < wid) ? v : 0;
+            nseg += v;
+        }
+        incl += base;
+        if (tid < cnt && flag) sm.seg_first[incl - 1] = tid;
+        if (tid == 0) sm.seg_first[nseg] = cnt;
+
+        for (int sb = 0; sb < nseg; sb += kBatch) {
+            const int nb = min(kBatch, nseg - sb);
+            if (sb == 0) __syncthreads();  // the table's ray starts are written
+            // ---- 1. V(c, ray) of this cell for the batch's rays: sum over the
+            // ray's samples of w(p, c) E(p), samples in plan order; a warp
+            // skips samples whose 9 stencil rows miss its two tile rows ----
+            float vv[2 * kBatch];
+#pragma unroll
+            for (int r = 0; r < kBatch; ++r) {
+                float vr = 0.f, vi = 0.f;
+                if (r < nb) {
+                    const int e1 = sm.seg_first[sb + r + 1];
+                    for (int e = sm.seg_first[sb + r]; e < e1; ++e) {
+                        const int pk = sm.cb[e];
+                        const int dy = ((pk >> 8) & 0xff) - 32;
+                        if (dy > 2 * wid + 1 || dy + kTaps - 1 < 2 * wid) continue;  // warp-uniform
+                        const int dx = (pk & 0xff) - 32;
+                        const int ux = cx - dx, uy = cy - dy;
+                        const bool in = (unsigned)ux < (unsigned)kTaps && (unsigned)uy < (unsigned)kTaps;
+                        const float w = in ? sm.w[e][ux] * sm.w[e][kTaps + uy] : 0.f;
+                        const float2 E = sm.f[e];
+                        vr = fmaf(w, E.x, vr);
+                        vi = fmaf(w, E.y, vi);
+                    }
+                }
+                vv[2 * r] = vr;
+                vv[2 * r + 1] = vi;
+            }
+            // ---- previous batch's MMAs done: add its result to the cell's
+            // FP32 sums (IEEE adds: the tensor core's own accumulation is kept
+            // to one batch); A, B and the accumulator are then free ----
+            if (nmma > 0) {
+                ok = tc::mbar_wait(&sm.bar, (uint32_t)((nmma - 1) & 1)) && ok;
+                tc::fence_after();
+                float v[32];
+                tc::ld32(tbase + ((uint32_t)(32 * q) << 16) + kColD + mt * kN, v);
+#pragma unroll
+                for (int i = 0; i < 32; ++i) acc[i] += v[i];
+            }
+            // ---- B = conj K' rows of this batch: row 2j+o, K index 2r+s (threads = (row, 4 K values)) ----
+            {
+                const int nrow = tid >> 3, q4 = tid & 7;
+                const int j = nrow >> 1, o = nrow & 1;
+                float bv[4];
+#pragma unroll
+                for (int i = 0; i < 2; ++i) {
+                    const int r = 2 * q4 + i;
+                    float2 kv = make_float2(0.f, 0.f);
+                    if (r < nb && jbase + j < g.m)
+                        kv = __ldg(kmat + (long long)sm.th[sm.seg_first[sb + r]] * g.m + jbase + j);
+                    bv[2 * i] = o == 0 ? kv.x : -kv.y;
+                    bv[2 * i + 1] = o == 0 ? kv.y : kv.x;
+                }
+                const int o32 = off32(nrow, 4 * q4);
+                *reinterpret_cast<float4 *>(sm.bhi + o32) = make_float4(bv[0], bv[1], bv[2], bv[3]);
+                *reinterpret_cast<float4 *>(sm.blo + o32) =
+                    make_float4(bv[0] - tc::trunc_tf32(bv[0]), bv[1] - tc::trunc_tf32(bv[1]),
+                                bv[2] - tc::trunc_tf32(bv[2]), bv[3] - tc::trunc_tf32(bv[3]));
+            }
+            // ---- 2. A = V of this cell, hi and lo parts, into tensor memory ----
+            {
+                float lo[32];
+#pragma unroll
+                for (int i = 0; i < 32; ++i) lo[i] = vv[i] - tc::trunc_tf32(vv[i]);
+                const uint32_t ta0 = tbase + ((uint32_t)(32 * q) << 16);
+                st32(ta0 + kColAhi + mt * kK, vv);
+                st32(ta0 + kColAlo + mt * kK, lo);
+                asm volatile("tcgen05.wait::st.sync.aligned;\n" ::: "memory");
+            }
+            tc::fence_proxy_async();
+            tc::fence_before();
+            __syncthreads();
+            if (tid == 0) {
+                tc::fence_after();
+                constexpr uint32_t IT = tc::idesc(tc::kFmtTF32, 128, kN);
+                const uint64_t dh = tc::sdesc(tc::smem_addr(sm.bhi), 128, 1024);
+                const uint64_t dl = tc::sdesc(tc::smem_addr(sm.blo), 128, 1024);
+#pragma unroll
+                for (int m2 = 0; m2 < kMT; ++m2) {
+                    const uint32_t d = tbase + kColD + m2 * kN;
+#pragma unroll
+                    for (int s2 = 0; s2 < kK / 8; ++s2) {
+                        const uint32_t ah = tbase + kColAhi + m2 * kK + s2 * 8;
+                        const uint32_t al = tbase + kColAlo + m2 * kK + s2 * 8;
+                        mma_tf32_ts(d, ah, dh + (uint64_t)(16 * s2), IT, s2 > 0 ? 1u : 0u);
+                        mma_tf32_ts(d, ah, dl + (uint64_t)(16 * s2), IT, 1u);
+                        mma_tf32_ts(d, al, dh + (uint64_t)(16 * s2), IT, 1u);
+                    }
+                }
+                tc::commit(&sm.bar);
+            }
+            ++nmma;
+        }
+    }
+    // ---- store the cell's time samples (pre-IFFT fftshift sign); split tiles add ----
+    if (nmma > 0) {
+        ok = tc::mbar_wait(&sm.bar, (uint32_t)((nmma - 1) & 1)) && ok;
+        tc::fence_after();
+        float v[32];
+        tc::ld32(tbase + ((uint32_t)(32 * q) << 16) + kColD + mt * kN, v);
+#pragma unroll
+        for (int i = 0; i < 32; ++i) acc[i] += v[i];
+    }
+    const int ly = tid / kT, lx = tid - (tid / kT) * kT;
+    const int KY = tyi * kT + ly, KX = txi * kT + lx;
+    if (KY < P && KX < P) {
+        const float sg = ((KX + KY) & 1) ? -1.f : 1.f;
+        float2 *dst = spec + ((long long)z * g.m + jbase) * g.img_adj + (long long)KY * P + KX;
+#pragma unroll
+        for (int j = 0; j < 16; ++j) {
+            if (jbase + j >= g.m) break;
+            const float2 v = make_float2(sg * acc[2 * j], sg * acc[2 * j + 1]);
+            float2 *d = dst + (long long)j * g.img_adj;
+            if (it.w) {
+                atomicAdd(&d->x, v.x);
+                atomicAdd(&d->y, v.y);
+            } else {
+                *d = v;
+            }
+        }
+    }
+    tc::fence_before();
+    __syncthreads();
+    if (wid == 0) tc::dealloc(tbase, kTmemCols);
+    if (!ok && lane == 0) atomicAdd(err, 1);
+}
+
+// At most two blocks per SM: each holds 256 of the 512 tensor-memory columns
+// (a third resident block would wait in tcgen05.alloc), so the shared memory
+// request is raised to more than a third of the SM's 228 KB.
+constexpr size_t kScSmemBytes = sizeof(ScTcSmem) > 80 * 1024 ? sizeof(ScTcSmem) : 80 * 1024;
+
+void scatter_tc_prepare() {
+    CUDA_CHECK(cudaFuncSetAttribute(k_scatter_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kScSmemBytes));
+}
+
+void launch_scatter_tc(const float2 *rowsc, float2 *spec, int zb, const GeoDev &gd, const UsGeo &g, int jbase,
+                       cudaStream_t s) {
+    if (g.T != kT) throw Error(1, "tile size must be 16");
+    dim3 gs(gd.n_adj_items, zb);
+    k_scatter_tc<<<gs, kThr, kScSmemBytes, s>>>(rowsc, spec, gd.adj_pts, gd.adj_items, gd.sincos, gd.kmat,
+                                                   gd.shiftadj, g, jbase, gd.err);
+    LAUNCH_CHECK("k_scatter_tc");
+}
+
+}  // namespace rectv

@@ -633,6 +633,10 @@ void launch_scatter_adj(const float2 *rowsc, float2 *spec, int zb, const GeoDev 
     if (g.T != 16) throw Error(1, "tile size must be 16");
     const int mp = mp_for(g.m);
     for (int jb = 0; jb < g.m; jb += 16) {
+        if (mp == 16 && gd.tc_scatter) {
+            launch_scatter_tc(rowsc, spec, zb, gd, g, jb, s);
+            continue;
+        }
         switch (mp) {
             case 1: scatter_adj_t<1, 16>(rowsc, spec, zb, gd, g, jb, s); break;
             case 2: scatter_adj_t<2, 16>(rowsc, spec, zb, gd, g, jb, s); break;
