@@ -346,11 +346,11 @@ struct Handle {
             if (!std::strcmp(e, "tc") && mp16()) tc_min_spr = 0.0f;
         }
         HostPlan hp = build_plan(theta_h, n, ntheta, ug.T, table_capacity(), 1 << 30, tc_min_spr);
-        // adjoint: RECTV_SCATTER=tc selects the tensor-core time-sample mixing
-        // (k_scatter_tc); the direct FP32 scatter is the default
-        bool tc_scatter = false;
+        // adjoint: tensor-core time-sample mixing (k_scatter_tc) from 9 time
+        // samples up; RECTV_SCATTER=direct forces the FP32 scatter
+        bool tc_scatter = mp16();
         if (const char *e = std::getenv("RECTV_SCATTER"))
-            if (!std::strcmp(e, "tc") && mp16()) tc_scatter = true;
+            if (!std::strcmp(e, "direct")) tc_scatter = false;
         auto up = [&](const void *src, size_t bytes) -> void * {
             void *p = nullptr;
             CUDA_CHECK(cudaMalloc(&p, std::max<size_t>(bytes, 16)));
@@ -370,6 +370,12 @@ struct Handle {
         gd.split_tiles = (int *)up(hp.split_tiles.data(), hp.split_tiles.size() * 4);
         gd.n_split_tiles = (int)hp.split_tiles.size();
         gd.tc_scatter = tc_scatter;
+        if (tc_scatter) {
+            void *p = nullptr;
+            CUDA_CHECK(cudaMalloc(&p, std::max<size_t>(hp.adj_pts.size() * sizeof(AdjRec), 16)));
+            geo_owned.push_back(p);
+            gd.adj_recs = (AdjRec *)p;
+        }
         if (gd.n_fwd_items > 2147483647 || gd.n_adj_items > 2147483647)
             throw Error(RECTV_ERR_ARG, "rectv: plan too large");
 
@@ -414,6 +420,7 @@ struct Handle {
             dp[x] = (float)std::exp((double)mu_us * d * d);
         }
         gd.deapod = (float *)up(dp.data(), n * sizeof(float));
+        if (gd.tc_scatter) launch_adj_records(gd.adj_recs, gd, ug, stream);
         CUDA_CHECK(cudaStreamSynchronize(stream));  // host vectors go out of scope
     }
 

@@ -62,6 +62,15 @@ struct UsGeo {
     int NT;             // tiles per side P/T
 };
 
+// Weights of one polar sample restricted to one 16x16 tile of the adjoint
+// plan (zero outside the sample's 9x9 stencil), with its ray, detector index
+// and the mask of tile rows its stencil covers.
+struct AdjRec {
+    float wx[16];
+    float wy[16];
+    int th, k, mask, pad;
+};
+
 // Per-angle constants uploaded at geometry set-up.
 struct GeoDev {
     float2 *sincos = nullptr;    // [ntheta] (sin, cos) of theta
@@ -81,6 +90,7 @@ struct GeoDev {
     int n_split_tiles = 0;
     int *err = nullptr;          // device counter of host/device bin disagreements
     bool tc_scatter = false;     // adjoint time-sample mixing on the tensor cores (k_scatter_tc)
+    AdjRec *adj_recs = nullptr;  // geometry records of adj_pts (tensor-core scatter only)
 };
 
 // Host-side angle plan (built in plan.cpp).
@@ -126,6 +136,7 @@ void gather_tc_prepare();
 void launch_scatter_tc(const float2 *rowsc, float2 *spec, int zb, const GeoDev &gd, const UsGeo &g, int jbase,
                        cudaStream_t s);
 void scatter_tc_prepare();
+void launch_adj_records(AdjRec *recs, const GeoDev &gd, const UsGeo &g, cudaStream_t s);
 size_t gather_tc_smem();
 int gather_tc_table_capacity();
 size_t gather_fwd_smem(const UsGeo &g);

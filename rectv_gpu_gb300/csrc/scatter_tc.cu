@@ -3,24 +3,32 @@
 //
 // The adjoint (gather TOMO_ADJ + wrap TOMO_ADJ, kernels_radonusfft.cuh:40-144,
 // fused with shift/fftshift of radonusfft.cu:115-121 and the basis weights of
-// operators.cu:171-176) adds, for every polar sample p on ray theta, the
-// value conj(K'(theta, j)) w(p, c) E(p) to cell c of time sample j's grid.
-// Along one ray the factor conj(K'(theta, j)) is common to all samples, so
-//  1. each thread (one cell of the 16x16 tile) first sums its value of the
-//     single complex per-ray grid V(c, theta) = sum_p w(p, c) E(p) over the
-//     ray's samples (in plan order, so sums are reproducible; no atomics);
-//  2. the time samples are then a GEMM over rays:
-//     F(c, j) += sum_theta V(c, theta) conj(K'(theta, j)),
-//     [256 cells x 32] x [32 x 32] real per batch of 16 rays (K index
-//     2r + re/im of V; N index 2j + re/im of F), on the tensor cores with the
-//     three TF32 terms Vhi Khi + Vhi Klo + Vlo Khi for FP32 accuracy (the
-//     tensor core truncates FP32 input to TF32; lo = x - trunc(x)).
-// Each batch's product is formed in tensor memory (12 MMAs) and added to the
-// cell's FP32 sums in registers with IEEE adds -- the tensor core's FP32
-// accumulation rounds differently, and the thousands of batches of a tile
-// near the centre of the spectrum would otherwise drift.  The tile is stored
-// once (added, for a tile split over blocks).  One block of 256 threads per
-// (tile, slice); thread = cell.
+// operators.cu:171-176) adds, for every polar sample p on ray theta, the value
+// conj(K'(theta, j)) w(p, c) E(p) to cell c of time sample j's grid, with the
+// separable Gaussian weight w(p, c) = wx_p(cx) wy_p(cy).
+//
+// Geometry records.  The weights of a sample restricted to one 16x16 tile
+// do not depend on the slice, so they are computed once per geometry
+// (k_adj_records) for every (tile, sample) entry of the adjoint plan: the
+// x and y weight rows over the tile's 16 columns / rows (zero outside the
+// stencil), the ray, the detector index and a mask of the tile rows the
+// stencil covers.
+//
+// Per (slice, tile) block of 256 threads (thread = cell):
+//  * per sample: E(p) (the row spectrum value times (-1)^(k+1) shiftadj(k)
+//    (pi/mu)/n) and T_p(cy) = E(p) wy_p(cy) for the tile's 16 rows;
+//  * per batch of 16 rays: every cell sums its value of each ray's grid
+//    V(c, theta) = sum_p T_p(cy) wx_p(cx) over the ray's samples (plan order,
+//    so sums are reproducible; a warp skips samples that miss its two rows);
+//    the time samples are then a GEMM over the batch's rays,
+//    F(c, j) += sum_theta V(c, theta) conj(K'(theta, j)), [256 x 32] x
+//    [32 x 32] real on the tensor cores with the three TF32 terms
+//    Vhi Khi + Vhi Klo + Vlo Khi (the tensor core truncates FP32 input to
+//    TF32; lo = x - trunc(x)).  Each batch's product is added to the cell's
+//    FP32 sums in registers (the tensor core's own FP32 accumulation rounds
+//    differently and would drift over the many batches of central tiles),
+//    and the next batch's grids are formed while the MMAs run.
+// The tile is stored once per block (added, for a tile split over blocks).
 #include <cuda.h>
 #include <cuda_runtime.h>
 
@@ -44,17 +52,16 @@ constexpr int kWarps = kThr / 32;
 constexpr uint32_t kTmemCols = 256;
 constexpr uint32_t kColAhi = 0;             // [mt*32, +32)
 constexpr uint32_t kColAlo = kMT * kK;      // 64
-constexpr uint32_t kColD = 2 * kMT * kK;    // 128: F accumulators [mt*32, +32)
+constexpr uint32_t kColD = 2 * kMT * kK;    // 128: product of the batch [mt*32, +32)
 
 __device__ __forceinline__ int off32(int row, int kk) {
     return (row >> 3) * 256 + (kk >> 2) * 32 + (row & 7) * 4 + (kk & 3);
 }
 
 struct ScTcSmem {
-    float w[kTab][20];            // 9 x weights, 9 y weights (16-byte rows)
-    int cb[kTab];                 // packed (dx + 32) | (dy + 32) << 8 of the stencil origin
-    int th[kTab];
-    float2 f[kTab];               // E(theta, k) of this slice
+    AdjRec rec[kTab];             // geometry records of the table's samples
+    float2 t[kTab][kT];           // T_p(cy) = E(p) wy_p(cy)
+    float2 e[kTab];               // E(p) of this slice
     float bhi[kN * kK];           // B = conj K' of the batch's rays, FP32
     float blo[kN * kK];           // B - trunc(B)
     int seg_first[kTab + 1];
@@ -88,17 +95,64 @@ __device__ __forceinline__ void mma_tf32_ts(uint32_t d, uint32_t a, uint64_t b, 
 
 }  // namespace
 
+// ---------------------------------------------------------------------------
+// Geometry records of the adjoint plan: one block per work item, one thread
+// per entry.  The stencil origin is taken modulo the periodic grid nearest to
+// the tile (wrap TOMO_ADJ, kernels_radonusfft.cuh:40-64).
+// ---------------------------------------------------------------------------
+__global__ void k_adj_records(AdjRec *__restrict__ recs, const uint32_t *__restrict__ pts,
+                              const int4 *__restrict__ items, const float2 *__restrict__ sincos, UsGeo g) {
+    const int4 it = items[blockIdx.x];
+    const int tyi = it.x / g.NT, txi = it.x - tyi * g.NT;
+    const int P = g.P, half = P / 2;
+    for (int e = threadIdx.x; e < it.z; e += blockDim.x) {
+        const uint32_t id = pts[it.y + e];
+        const int th = id / (uint32_t)g.n;
+        const int k = id - th * g.n;
+        float x0, y0;
+        int fx, fy;
+        sample_pos(k, sincos[th], g, x0, y0, fx, fy);
+        int dx = g.n + fx - kR - txi * kT;
+        int dy = g.n + fy - kR - tyi * kT;
+        dx += (dx < -half) ? P : 0;
+        dx -= (dx > half) ? P : 0;
+        dy += (dy < -half) ? P : 0;
+        dy -= (dy > half) ? P : 0;
+        AdjRec r;
+        int mask = 0;
+#pragma unroll
+        for (int c = 0; c < kT; ++c) {
+            const int bx = c - dx, by = c - dy;
+            r.wx[c] = ((unsigned)bx < (unsigned)kTaps) ? tap_weight(fx, bx, x0, g) : 0.f;
+            const bool iny = (unsigned)by < (unsigned)kTaps;
+            r.wy[c] = iny ? tap_weight(fy, by, y0, g) : 0.f;
+            mask |= iny ? (1 << c) : 0;
+        }
+        r.th = th;
+        r.k = k;
+        r.mask = mask;
+        r.pad = 0;
+        recs[(long long)it.y + e] = r;
+    }
+}
+
+void launch_adj_records(AdjRec *recs, const GeoDev &gd, const UsGeo &g, cudaStream_t s) {
+    if (gd.n_adj_items == 0) return;
+    k_adj_records<<<gd.n_adj_items, 256, 0, s>>>(recs, gd.adj_pts, gd.adj_items, gd.sincos, g);
+    LAUNCH_CHECK("k_adj_records");
+}
+
 __global__ void __launch_bounds__(kThr, 2)
-    k_scatter_tc(const float2 *__restrict__ rowsc, float2 *__restrict__ spec, const uint32_t *__restrict__ pts,
-                 const int4 *__restrict__ items, const float2 *__restrict__ sincos,
-                 const float2 *__restrict__ kmat, const float2 *__restrict__ shifta, UsGeo g, int jbase,
-                 int *__restrict__ err) {
+    k_scatter_tc(const float2 *__restrict__ rowsc, float2 *__restrict__ spec, const AdjRec *__restrict__ recs,
+                 const int4 *__restrict__ items, const float2 *__restrict__ kmat, const float2 *__restrict__ shifta,
+                 UsGeo g, int zb, int jbase, int *__restrict__ err) {
     extern __shared__ __align__(1024) unsigned char sc_smem_raw[];
     ScTcSmem &sm = *reinterpret_cast<ScTcSmem *>(sc_smem_raw);
-    const int4 it = items[blockIdx.x];
-    const int z = blockIdx.y;
+    // slices fastest: consecutive blocks share the item's records in L2
+    const int z = (int)(blockIdx.x % (unsigned)zb);
+    const int4 it = items[blockIdx.x / (unsigned)zb];
     const int tyi = it.x / g.NT, txi = it.x - tyi * g.NT;
-    const int P = g.P, half = P / 2, hn = g.n / 2 + 1;
+    const int P = g.P, hn = g.n / 2 + 1;
     const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
     const float2 *rz = rowsc + (long long)z * g.ntheta * hn;
     if (wid == 0) tc::alloc(&sm.tslot, kTmemCols);
@@ -110,10 +164,11 @@ __global__ void __launch_bounds__(kThr, 2)
     __syncthreads();
     tc::fence_after();
     const uint32_t tbase = sm.tslot;
-    const int mt = wid >> 2, q = wid & 3;  // this thread's cell tid = mt*128 + 32q + lane
-    const int cx = tid % kT, cy = tid / kT;  // its column and row in the tile (warp w: rows 2w, 2w+1)
+    const int mt = wid >> 2, q = wid & 3;    // this thread's cell tid = mt*128 + 32q + lane
+    const int cx = tid % kT, cy = tid / kT;  // its column and row (warp w: rows 2w, 2w+1)
+    const int wmask = 3 << (2 * wid);
     bool ok = true;
-    int nmma = 0;  // MMA batches issued
+    int nmma = 0;   // MMA batches issued
     float acc[32];  // F of this cell: 16 time samples x (re, im)
 #pragma unroll
     for (int i = 0; i < 32; ++i) acc[i] = 0.f;
@@ -121,38 +176,32 @@ __global__ void __launch_bounds__(kThr, 2)
     for (int c0 = 0; c0 < it.z; c0 += kTab) {
         const int cnt = min(kTab, it.z - c0);
         __syncthreads();  // previous table consumed
+        {  // records of the table, 16-byte copies
+            const uint4 *src = reinterpret_cast<const uint4 *>(recs + (long long)it.y + c0);
+            uint4 *dst = reinterpret_cast<uint4 *>(sm.rec);
+            constexpr int kVec = sizeof(AdjRec) / 16;
+            for (int i = tid; i < cnt * kVec; i += kThr) dst[i] = __ldg(src + i);
+        }
+        __syncthreads();
+        // ---- E = (-1)^(k+1) shiftadj(k) FFT(row)(k) (pi/mu)/n, then T_p(cy) = E(p) wy_p(cy) ----
         for (int e = tid; e < cnt; e += kThr) {
-            const uint32_t id = __ldg(pts + it.y + c0 + e);
-            const int th = id / (uint32_t)g.n;
-            const int k = id - th * g.n;
-            float x0, y0;
-            int fx, fy;
-            sample_pos(k, __ldg(sincos + th), g, x0, y0, fx, fy);
-            int dx = g.n + fx - kR - txi * kT;
-            int dy = g.n + fy - kR - tyi * kT;
-            dx += (dx < -half) ? P : 0;
-            dx -= (dx > half) ? P : 0;
-            dy += (dy < -half) ? P : 0;
-            dy -= (dy > half) ? P : 0;
-#pragma unroll
-            for (int i = 0; i < kTaps; ++i) {
-                sm.w[e][i] = tap_weight(fx, i, x0, g);
-                sm.w[e][kTaps + i] = tap_weight(fy, i, y0, g);
-            }
-            // stencils of listed samples start within [-2r, T) of the tile
-            sm.cb[e] = ((dx + 32) & 0xff) | (((dy + 32) & 0xff) << 8);
-            sm.th[e] = th;
-            // E = (-1)^(k+1) shiftadj(k) FFT(row)(k) (pi/mu)/n  (Hermitian row spectrum)
+            const int th = sm.rec[e].th, k = sm.rec[e].k;
             float2 R = (k <= g.n / 2) ? __ldg(rz + (long long)th * hn + k) : __ldg(rz + (long long)th * hn + (g.n - k));
             if (k > g.n / 2) R.y = -R.y;
             const float2 E = cmul(R, __ldg(shifta + k));
             const float c = (k & 1) ? g.cw : -g.cw;
-            sm.f[e] = make_float2(E.x * c, E.y * c);
+            sm.e[e] = make_float2(E.x * c, E.y * c);
         }
         __syncthreads();
+        for (int i = tid; i < cnt * kT; i += kThr) {
+            const int e = i >> 4, row = i & 15;
+            const float2 E = sm.e[e];
+            const float w = sm.rec[e].wy[row];
+            sm.t[e][row] = make_float2(E.x * w, E.y * w);
+        }
         // ---- first table row of each ray: block-wide scan of ray starts ----
         int flag = 0;
-        if (tid < cnt) flag = (tid == 0 || sm.th[tid] != sm.th[tid - 1]) ? 1 : 0;
+        if (tid < cnt) flag = (tid == 0 || sm.rec[tid].th != sm.rec[tid - 1].th) ? 1 : 0;
         int incl = flag;
 #pragma unroll
         for (int o = 1; o < 32; o <<= 1) {
@@ -171,13 +220,11 @@ __global__ void __launch_bounds__(kThr, 2)
         incl += base;
         if (tid < cnt && flag) sm.seg_first[incl - 1] = tid;
         if (tid == 0) sm.seg_first[nseg] = cnt;
+        __syncthreads();  // ray starts and T written
 
         for (int sb = 0; sb < nseg; sb += kBatch) {
             const int nb = min(kBatch, nseg - sb);
-            if (sb == 0) __syncthreads();  // the table's ray starts are written
-            // ---- 1. V(c, ray) of this cell for the batch's rays: sum over the
-            // ray's samples of w(p, c) E(p), samples in plan order; a warp
-            // skips samples whose 9 stencil rows miss its two tile rows ----
+            // ---- 1. V(c, ray) of this cell for the batch's rays ----
             float vv[2 * kBatch];
 #pragma unroll
             for (int r = 0; r < kBatch; ++r) {
@@ -185,24 +232,18 @@ __global__ void __launch_bounds__(kThr, 2)
                 if (r < nb) {
                     const int e1 = sm.seg_first[sb + r + 1];
                     for (int e = sm.seg_first[sb + r]; e < e1; ++e) {
-                        const int pk = sm.cb[e];
-                        const int dy = ((pk >> 8) & 0xff) - 32;
-                        if (dy > 2 * wid + 1 || dy + kTaps - 1 < 2 * wid) continue;  // warp-uniform
-                        const int dx = (pk & 0xff) - 32;
-                        const int ux = cx - dx, uy = cy - dy;
-                        const bool in = (unsigned)ux < (unsigned)kTaps && (unsigned)uy < (unsigned)kTaps;
-                        const float w = in ? sm.w[e][ux] * sm.w[e][kTaps + uy] : 0.f;
-                        const float2 E = sm.f[e];
-                        vr = fmaf(w, E.x, vr);
-                        vi = fmaf(w, E.y, vi);
+                        if (!(sm.rec[e].mask & wmask)) continue;  // warp-uniform
+                        const float2 tv = sm.t[e][cy];
+                        const float w = sm.rec[e].wx[cx];
+                        vr = fmaf(w, tv.x, vr);
+                        vi = fmaf(w, tv.y, vi);
                     }
                 }
                 vv[2 * r] = vr;
                 vv[2 * r + 1] = vi;
             }
-            // ---- previous batch's MMAs done: add its result to the cell's
-            // FP32 sums (IEEE adds: the tensor core's own accumulation is kept
-            // to one batch); A, B and the accumulator are then free ----
+            // ---- previous batch's MMAs done: add its product to the cell's
+            // FP32 sums; A, B and the accumulator are then free ----
             if (nmma > 0) {
                 ok = tc::mbar_wait(&sm.bar, (uint32_t)((nmma - 1) & 1)) && ok;
                 tc::fence_after();
@@ -221,7 +262,7 @@ __global__ void __launch_bounds__(kThr, 2)
                     const int r = 2 * q4 + i;
                     float2 kv = make_float2(0.f, 0.f);
                     if (r < nb && jbase + j < g.m)
-                        kv = __ldg(kmat + (long long)sm.th[sm.seg_first[sb + r]] * g.m + jbase + j);
+                        kv = __ldg(kmat + (long long)sm.rec[sm.seg_first[sb + r]].th * g.m + jbase + j);
                     bv[2 * i] = o == 0 ? kv.x : -kv.y;
                     bv[2 * i + 1] = o == 0 ? kv.y : kv.x;
                 }
@@ -275,8 +316,7 @@ __global__ void __launch_bounds__(kThr, 2)
 #pragma unroll
         for (int i = 0; i < 32; ++i) acc[i] += v[i];
     }
-    const int ly = tid / kT, lx = tid - (tid / kT) * kT;
-    const int KY = tyi * kT + ly, KX = txi * kT + lx;
+    const int KY = tyi * kT + cy, KX = txi * kT + cx;
     if (KY < P && KX < P) {
         const float sg = ((KX + KY) & 1) ? -1.f : 1.f;
         float2 *dst = spec + ((long long)z * g.m + jbase) * g.img_adj + (long long)KY * P + KX;
@@ -311,9 +351,11 @@ void scatter_tc_prepare() {
 void launch_scatter_tc(const float2 *rowsc, float2 *spec, int zb, const GeoDev &gd, const UsGeo &g, int jbase,
                        cudaStream_t s) {
     if (g.T != kT) throw Error(1, "tile size must be 16");
-    dim3 gs(gd.n_adj_items, zb);
-    k_scatter_tc<<<gs, kThr, kScSmemBytes, s>>>(rowsc, spec, gd.adj_pts, gd.adj_items, gd.sincos, gd.kmat,
-                                                   gd.shiftadj, g, jbase, gd.err);
+    if (!gd.adj_recs) throw Error(1, "adjoint geometry records missing");
+    const long long nblk = (long long)zb * gd.n_adj_items;
+    if (nblk > 2147483647LL) throw Error(1, "adjoint grid too large");
+    k_scatter_tc<<<(unsigned)nblk, kThr, kScSmemBytes, s>>>(rowsc, spec, gd.adj_recs, gd.adj_items, gd.kmat,
+                                                           gd.shiftadj, g, zb, jbase, gd.err);
     LAUNCH_CHECK("k_scatter_tc");
 }
 
