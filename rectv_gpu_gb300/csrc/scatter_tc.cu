@@ -22,9 +22,10 @@
 //    so sums are reproducible; a warp skips samples that miss its two rows);
 //    the time samples are then a GEMM over the batch's rays,
 //    F(c, j) += sum_theta V(c, theta) conj(K'(theta, j)), [256 x 32] x
-//    [32 x 32] real on the tensor cores with the three TF32 terms
-//    Vhi Khi + Vhi Klo + Vlo Khi (the tensor core truncates FP32 input to
-//    TF32; lo = x - trunc(x)).  Each batch's product is added to the cell's
+//    [32 x 32] real on the tensor cores with TF32 parts for FP32 accuracy
+//    (the tensor core truncates FP32 input to TF32; lo = x - trunc(x)):
+//    the MMA's B holds [Khi | Klo] as 64 columns, so Vhi B + Vlo B gives
+//    Vhi Khi + Vhi Klo + Vlo Khi (+ the negligible Vlo Klo) in 16 MMAs.  Each batch's product is added to the cell's
 //    FP32 sums in registers (the tensor core's own FP32 accumulation rounds
 //    differently and would drift over the many batches of central tiles),
 //    and the next batch's grids are formed while the MMAs run.
@@ -47,12 +48,13 @@ constexpr int kTab = 256;           // samples per table
 constexpr int kBatch = 16;          // rays per MMA batch (K = 32)
 constexpr int kK = 2 * kBatch;
 constexpr int kN = 32;              // 16 time samples x (re, im)
+constexpr int kNP = 2 * kN;         // MMA N: B rows [Khi | Klo]
 constexpr int kThr = kCells;
 constexpr int kWarps = kThr / 32;
 constexpr uint32_t kTmemCols = 256;
 constexpr uint32_t kColAhi = 0;             // [mt*32, +32)
 constexpr uint32_t kColAlo = kMT * kK;      // 64
-constexpr uint32_t kColD = 2 * kMT * kK;    // 128: product of the batch [mt*32, +32)
+constexpr uint32_t kColD = 2 * kMT * kK;    // 128: product of the batch [mt*64, +64)
 
 __device__ __forceinline__ int off32(int row, int kk) {
     return (row >> 3) * 256 + (kk >> 2) * 32 + (row & 7) * 4 + (kk & 3);
@@ -62,8 +64,8 @@ struct ScTcSmem {
     AdjRec rec[kTab];             // geometry records of the table's samples
     float2 t[kTab][kT];           // T_p(cy) = E(p) wy_p(cy)
     float2 e[kTab];               // E(p) of this slice
-    float bhi[kN * kK];           // B = conj K' of the batch's rays, FP32
-    float blo[kN * kK];           // B - trunc(B)
+    float bhi[kN * kK];           // B = conj K' of the batch's rays, FP32: rows 0..31 of the MMA's B
+    float blo[kN * kK];           // B - trunc(B): rows 32..63 (contiguous with bhi)
     int seg_first[kTab + 1];
     int wsum[kWarps];
     unsigned long long bar;
@@ -166,7 +168,6 @@ __global__ void __launch_bounds__(kThr, 2)
     const uint32_t tbase = sm.tslot;
     const int mt = wid >> 2, q = wid & 3;    // this thread's cell tid = mt*128 + 32q + lane
     const int cx = tid % kT, cy = tid / kT;  // its column and row (warp w: rows 2w, 2w+1)
-    const int wmask = 3 << (2 * wid);
     bool ok = true;
     int nmma = 0;   // MMA batches issued
     float acc[32];  // F of this cell: 16 time samples x (re, im)
@@ -229,10 +230,10 @@ __global__ void __launch_bounds__(kThr, 2)
 #pragma unroll
             for (int r = 0; r < kBatch; ++r) {
                 float vr = 0.f, vi = 0.f;
-                if (r < nb) {
+                if (r < nb) {  // T and wx vanish outside the stencil: no tests in the loop
                     const int e1 = sm.seg_first[sb + r + 1];
+#pragma unroll 4
                     for (int e = sm.seg_first[sb + r]; e < e1; ++e) {
-                        if (!(sm.rec[e].mask & wmask)) continue;  // warp-uniform
                         const float2 tv = sm.t[e][cy];
                         const float w = sm.rec[e].wx[cx];
                         vr = fmaf(w, tv.x, vr);
@@ -247,10 +248,11 @@ __global__ void __launch_bounds__(kThr, 2)
             if (nmma > 0) {
                 ok = tc::mbar_wait(&sm.bar, (uint32_t)((nmma - 1) & 1)) && ok;
                 tc::fence_after();
-                float v[32];
-                tc::ld32(tbase + ((uint32_t)(32 * q) << 16) + kColD + mt * kN, v);
+                float v[32], w2[32];
+                tc::ld32(tbase + ((uint32_t)(32 * q) << 16) + kColD + mt * kNP, v);
+                tc::ld32(tbase + ((uint32_t)(32 * q) << 16) + kColD + mt * kNP + kN, w2);
 #pragma unroll
-                for (int i = 0; i < 32; ++i) acc[i] += v[i];
+                for (int i = 0; i < 32; ++i) acc[i] += v[i] + w2[i];
             }
             // ---- B = conj K' rows of this batch: row 2j+o, K index 2r+s (threads = (row, 4 K values)) ----
             {
@@ -285,21 +287,20 @@ __global__ void __launch_bounds__(kThr, 2)
             tc::fence_proxy_async();
             tc::fence_before();
             __syncthreads();
-            if (tid == 0) {
+            if (tid == 32 * (nmma % kWarps)) {  // the issuing warp rotates
                 tc::fence_after();
-                constexpr uint32_t IT = tc::idesc(tc::kFmtTF32, 128, kN);
-                const uint64_t dh = tc::sdesc(tc::smem_addr(sm.bhi), 128, 1024);
-                const uint64_t dl = tc::sdesc(tc::smem_addr(sm.blo), 128, 1024);
+                // D = [Ahi Bhi, Ahi Blo] + [Alo Bhi, Alo Blo]: both halves summed when read
+                constexpr uint32_t IT = tc::idesc(tc::kFmtTF32, 128, kNP);
+                const uint64_t db = tc::sdesc(tc::smem_addr(sm.bhi), 128, 1024);
 #pragma unroll
                 for (int m2 = 0; m2 < kMT; ++m2) {
-                    const uint32_t d = tbase + kColD + m2 * kN;
+                    const uint32_t d = tbase + kColD + m2 * kNP;
 #pragma unroll
                     for (int s2 = 0; s2 < kK / 8; ++s2) {
                         const uint32_t ah = tbase + kColAhi + m2 * kK + s2 * 8;
                         const uint32_t al = tbase + kColAlo + m2 * kK + s2 * 8;
-                        mma_tf32_ts(d, ah, dh + (uint64_t)(16 * s2), IT, s2 > 0 ? 1u : 0u);
-                        mma_tf32_ts(d, ah, dl + (uint64_t)(16 * s2), IT, 1u);
-                        mma_tf32_ts(d, al, dh + (uint64_t)(16 * s2), IT, 1u);
+                        mma_tf32_ts(d, ah, db + (uint64_t)(16 * s2), IT, s2 > 0 ? 1u : 0u);
+                        mma_tf32_ts(d, al, db + (uint64_t)(16 * s2), IT, 1u);
                     }
                 }
                 tc::commit(&sm.bar);
@@ -311,10 +312,11 @@ __global__ void __launch_bounds__(kThr, 2)
     if (nmma > 0) {
         ok = tc::mbar_wait(&sm.bar, (uint32_t)((nmma - 1) & 1)) && ok;
         tc::fence_after();
-        float v[32];
-        tc::ld32(tbase + ((uint32_t)(32 * q) << 16) + kColD + mt * kN, v);
+        float v[32], w2[32];
+        tc::ld32(tbase + ((uint32_t)(32 * q) << 16) + kColD + mt * kNP, v);
+        tc::ld32(tbase + ((uint32_t)(32 * q) << 16) + kColD + mt * kNP + kN, w2);
 #pragma unroll
-        for (int i = 0; i < 32; ++i) acc[i] += v[i];
+        for (int i = 0; i < 32; ++i) acc[i] += v[i] + w2[i];
     }
     const int KY = tyi * kT + cy, KX = txi * kT + cx;
     if (KY < P && KX < P) {
