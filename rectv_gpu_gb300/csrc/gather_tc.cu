@@ -351,24 +351,20 @@ __global__ void __launch_bounds__(kThr, 1)
                     float ex[kTaps];
 #pragma unroll
                     for (int b = 0; b < kTaps; ++b) ex[b] = sm.wx[e][b];
-                    float ax = 0.f, ay = 0.f;
+                    float2 acc2 = make_float2(0.f, 0.f);
 #pragma unroll
                     for (int i = 0; i < 3; ++i) {
                         const int a = part + 4 * i;
                         if (a < kTaps) {
                             const float2 *gr = gp + a * kFW;
-                            float rx = 0.f, ry = 0.f;
+                            float2 rr = make_float2(0.f, 0.f);
 #pragma unroll
-                            for (int b = 0; b < kTaps; ++b) {
-                                const float2 v = gr[b];
-                                rx = fmaf(ex[b], v.x, rx);
-                                ry = fmaf(ex[b], v.y, ry);
-                            }
+                            for (int b = 0; b < kTaps; ++b) rr = ffma2(make_float2(ex[b], ex[b]), gr[b], rr);
                             const float wy = sm.wy[e][a];
-                            ax = fmaf(wy, rx, ax);
-                            ay = fmaf(wy, ry, ay);
+                            acc2 = ffma2(make_float2(wy, wy), rr, acc2);
                         }
                     }
+                    float ax = acc2.x, ay = acc2.y;
                     ax += __shfl_xor_sync(gm, ax, 1);
                     ay += __shfl_xor_sync(gm, ay, 1);
                     ax += __shfl_xor_sync(gm, ax, 2);

@@ -229,19 +229,17 @@ __global__ void __launch_bounds__(kThr, 2)
             float vv[2 * kBatch];
 #pragma unroll
             for (int r = 0; r < kBatch; ++r) {
-                float vr = 0.f, vi = 0.f;
+                float2 v = make_float2(0.f, 0.f);
                 if (r < nb) {  // T and wx vanish outside the stencil: no tests in the loop
                     const int e1 = sm.seg_first[sb + r + 1];
 #pragma unroll 4
                     for (int e = sm.seg_first[sb + r]; e < e1; ++e) {
-                        const float2 tv = sm.t[e][cy];
                         const float w = sm.rec[e].wx[cx];
-                        vr = fmaf(w, tv.x, vr);
-                        vi = fmaf(w, tv.y, vi);
+                        v = ffma2(make_float2(w, w), sm.t[e][cy], v);
                     }
                 }
-                vv[2 * r] = vr;
-                vv[2 * r + 1] = vi;
+                vv[2 * r] = v.x;
+                vv[2 * r + 1] = v.y;
             }
             // ---- previous batch's MMAs done: add its product to the cell's
             // FP32 sums; A, B and the accumulator are then free ----

@@ -11,6 +11,17 @@ __device__ __forceinline__ float2 cmul(float2 a, float2 b) {
     return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
 }
 
+// (a.x b.x + c.x, a.y b.y + c.y) as one packed FP32x2 FMA (each lane an IEEE
+// fma.rn, so results equal two fmaf calls).
+__device__ __forceinline__ float2 ffma2(float2 a, float2 b, float2 c) {
+    unsigned long long d;
+    asm("fma.rn.f32x2 %0, %1, %2, %3;"
+        : "=l"(d)
+        : "l"(*reinterpret_cast<const unsigned long long *>(&a)), "l"(*reinterpret_cast<const unsigned long long *>(&b)),
+          "l"(*reinterpret_cast<const unsigned long long *>(&c)));
+    return *reinterpret_cast<const float2 *>(&d);
+}
+
 // Position of polar sample (theta, k): identical float operation sequence to
 // the host plan (plan.cpp) and to takexy (kernels_radonusfft.cuh:73-78).
 __device__ __forceinline__ void sample_pos(int k, float2 sc, const UsGeo &g, float &x0, float &y0, int &fx,
