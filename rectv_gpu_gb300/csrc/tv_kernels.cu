@@ -129,8 +129,9 @@ void launch_graddiv(const float *u_in, const float *u_old, float *u_out, const f
 //   h = G u_cur, ho = G u_old (the reference's h2stored),
 //   psi = shrink(h + mu/rho, lambda0/rho), mu += rho h - rho psi,
 //   sums of |h-psi|^2, |ho-h|^2 and, for q >= 1, (u_cur-u_old)^2.
-// One thread per (qx, qy, qz) marching along qt; the squares of one grid point
-// are summed in FP32 and accumulated across points in FP64; one FP64 partial
+// One thread per (qx, qy, qz) marching along qt; the squares along its qt
+// column are summed in FP32 (at most m+1 = 17 terms for m = 16) and the
+// thread sums are accumulated in FP64 in a fixed order; one FP64 partial
 // triple per block.  Blocks of 32x8 over (qx, qy), grid.z over (chunk, qz).
 // ---------------------------------------------------------------------------
 __global__ void __launch_bounds__(256)
@@ -142,7 +143,7 @@ __global__ void __launch_bounds__(256)
     const int n = t.n, m = t.m, nzp = t.nzp;
     const int qz = blockIdx.z % (nzp + 1);
     const int c = c0 + blockIdx.z / (nzp + 1);
-    double a0 = 0.0, a1 = 0.0, a2 = 0.0;
+    float a0 = 0.f, a1 = 0.f, a2 = 0.f;
     if (qx <= n && qy <= n) {
         const long long slab = t.vol_slab, nn = (long long)n * n;
         const long long zc = (long long)c * nzp;
@@ -191,11 +192,11 @@ __global__ void __launch_bounds__(256)
                 r2 += dr * dr;
                 s2 += ds * ds;
             }
-            a0 += (double)r2;
-            a1 += (double)s2;
+            a0 += r2;
+            a1 += s2;
             if (inner_xyz && qt >= 1) {  // voxel q-1 = (x0, y0, t0, z0) inside the chunk
-                const double dd = (double)fc - (double)fo;
-                a2 += dd * dd;
+                const float dd = fc - fo;
+                a2 = fmaf(dd, dd, a2);
             }
             fc = fct;
             fo = fot;
@@ -203,7 +204,7 @@ __global__ void __launch_bounds__(256)
         }
     }
     const long long bid = ((long long)blockIdx.z * gridDim.y + blockIdx.y) * gridDim.x + blockIdx.x;
-    block_reduce3<8>(a0, a1, a2, partials + 3 * bid);
+    block_reduce3<8>((double)a0, (double)a1, (double)a2, partials + 3 * bid);
 }
 
 int shrink_blocks(const TvGeo &t, int nchunks) {

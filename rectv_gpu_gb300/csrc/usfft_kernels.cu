@@ -40,35 +40,44 @@ __device__ __forceinline__ void cp_async_wait_all() {
 // Forward: deapodise, zero-pad to P x P and modulate by (-1)^(X+Y)
 // (divphi + fftshift, kernels_radonusfft.cuh:4-38), writing the real input of
 // the in-place R2C transform: row Y of image img starts at complex element
-// img_fwd*img + qoff + Y*qp (2*qp floats per row, P+2 written).
+// img_fwd*img + qoff + Y*qp (2*qp floats per row; the P reals are written).
+// One block per row, 16-byte stores; rows outside the image are zeros.
 // ---------------------------------------------------------------------------
-__global__ void k_deapod_pad(const float *__restrict__ u, float2 *__restrict__ spec,
-                             const float *__restrict__ dp, UsGeo g, float inv4n2) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;  // float pair in the row
-    const int Y = blockIdx.y;
-    const long long img = blockIdx.z;
+__global__ void __launch_bounds__(256)
+    k_deapod_pad(const float *__restrict__ u, float2 *__restrict__ spec, const float *__restrict__ dp, UsGeo g,
+                 float inv4n2) {
+    const int Y = blockIdx.x;
+    const long long img = blockIdx.y;
     const int n = g.n;
-    const int npair = (g.P + 2) / 2;
-    if (i >= npair) return;
-    const int X = 2 * i;
-    float2 v = make_float2(0.f, 0.f);
+    float2 *row = spec + img * g.img_fwd + g.qoff + (long long)Y * g.qp;  // 16-byte aligned (qp, qoff even)
+    float4 *row4 = reinterpret_cast<float4 *>(row);
+    const int n4 = n / 2;  // float4 stores: reals 4i .. 4i+3
     const int y = Y - n / 2;
-    if (y >= 0 && y < n) {
-        const float *row = u + (img * n + y) * (long long)n;
-        const float sy = (Y & 1) ? -dp[y] * inv4n2 : dp[y] * inv4n2;
-        const int x0 = X - n / 2, x1 = x0 + 1;
-        if (x0 >= 0 && x0 < n) v.x = row[x0] * dp[x0] * sy;   // X even: +1
-        if (x1 >= 0 && x1 < n) v.y = -row[x1] * dp[x1] * sy;  // X+1 odd: -1
+    if (y < 0 || y >= n) {
+        for (int i = threadIdx.x; i < n4; i += blockDim.x) row4[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+        if ((n & 1) && threadIdx.x == 0) row[n - 1] = make_float2(0.f, 0.f);
+        return;
     }
-    spec[img * g.img_fwd + g.qoff + (long long)Y * g.qp + i] = v;
+    const float *ur = u + (img * n + y) * (long long)n;
+    const float sy = ((Y & 1) ? -dp[y] : dp[y]) * inv4n2;
+    auto val = [&](int X) {  // real X of the padded row; (-1)^X of the fftshift
+        const int x = X - n / 2;
+        if (x < 0 || x >= n) return 0.f;
+        const float v = __ldg(ur + x) * __ldg(dp + x) * sy;
+        return (X & 1) ? -v : v;
+    };
+    for (int i = threadIdx.x; i < n4; i += blockDim.x) {
+        const int X = 4 * i;
+        row4[i] = make_float4(val(X), val(X + 1), val(X + 2), val(X + 3));
+    }
+    if ((n & 1) && threadIdx.x == 0) row[n - 1] = make_float2(val(2 * n - 2), val(2 * n - 1));
 }
 
 void launch_deapod_pad(const float *u, float *spec, int nimg, const float *deapod, const UsGeo &g,
                        cudaStream_t s) {
-    const int npair = (g.P + 2) / 2;
-    dim3 bs(256), gs((npair + 255) / 256, g.P, nimg);
+    dim3 gs(g.P, nimg);
     const float inv4n2 = (float)(1.0 / (4.0 * g.n * (double)g.n));
-    k_deapod_pad<<<gs, bs, 0, s>>>(u, reinterpret_cast<float2 *>(spec), deapod, g, inv4n2);
+    k_deapod_pad<<<gs, 256, 0, s>>>(u, reinterpret_cast<float2 *>(spec), deapod, g, inv4n2);
     LAUNCH_CHECK("k_deapod_pad");
 }
 
