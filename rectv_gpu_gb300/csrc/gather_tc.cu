@@ -275,8 +275,12 @@ __global__ void __launch_bounds__(kThr, 1)
     uint32_t mma_par = 0;
     const unsigned gm = 0xfu << (lane & 28);  // the four lanes of a sample
     const int q = wid & 3;                    // TMEM lane quarter of this warp
-    for (int z = z0; z < z1; ++z) {
-        // ---- footprint box -> A operand in tensor memory (thread = cell) ----
+    // MMAs are issued by lane 0 of the last warp: a chunk rarely has enough
+    // samples to give that warp gather work
+    const int issuer = kThr - 32;
+
+    // footprint box of slice z -> A operand in tensor memory (thread = cell)
+    auto convert = [&](int z) {
         ok = tc::mbar_wait(&sm.bar_tma, (uint32_t)((z - z0) & 1)) && ok;
         for (int mt = wid >> 2; mt < kMT; mt += kWarps / 4) {
             const int cell = mt * 128 + 32 * q + lane;
@@ -308,11 +312,19 @@ __global__ void __launch_bounds__(kThr, 1)
         tc::fence_proxy_async();
         tc::fence_before();
         __syncthreads();
-        if (tid == 0) {
+        if (tid == issuer) {
             if (z + 1 < z1) tma_issue(z + 1);  // the box buffer has been read
             tc::fence_after();
-            if (nch > 0) issue(tbase, 0, 0);
+            issue(tbase, 0, 0);
         }
+    };
+
+    if (nch == 0) {  // no samples: only the first box is in flight
+        ok = tc::mbar_wait(&sm.bar_tma, 0u) && ok;
+    } else {
+        convert(z0);
+    }
+    for (int z = z0; z < z1 && nch > 0; ++z) {
         for (int ch = 0; ch < nch; ++ch) {
             const int nr = min(kRays, nseg - ch * kRays);
             ok = tc::mbar_wait(&sm.bar_mma, mma_par) && ok;
@@ -331,13 +343,19 @@ __global__ void __launch_bounds__(kThr, 1)
             }
             tc::fence_before();
             __syncthreads();
-            if (tid == 0 && ch + 1 < nch) {  // next chunk's MMAs run during this chunk's samples
-                tc::fence_after();
-                issue(tbase, ch + 1, (ch + 1) & 1);
-            }
-            if (nch > 2 && ch + 2 < nch) {
-                stage_b(ch + 2, ch & 1);
-                tc::fence_proxy_async();
+            if (ch + 1 < nch) {  // next chunk's MMAs run during this chunk's samples
+                if (tid == issuer) {
+                    tc::fence_after();
+                    issue(tbase, ch + 1, (ch + 1) & 1);
+                }
+                if (nch > 2 && ch + 2 < nch) {
+                    stage_b(ch + 2, ch & 1);
+                    tc::fence_proxy_async();
+                }
+            } else if (z + 1 < z1) {
+                // all MMAs of slice z are done: the next slice's A operand and
+                // first MMAs go ahead, and run during this chunk's samples
+                convert(z + 1);
             }
             // ---- samples of this chunk: four threads per sample (rows p, p+4, p+8) ----
             {
