@@ -348,7 +348,7 @@ struct Handle {
         HostPlan hp = build_plan(theta_h, n, ntheta, ug.T, table_capacity(), 1 << 30, tc_min_spr);
         // adjoint: tensor-core time-sample mixing (k_scatter_tc) from 9 time
         // samples up; RECTV_SCATTER=direct forces the FP32 scatter
-        bool tc_scatter = mp16();
+        bool tc_scatter = mp16() && ntheta < 65536;  // ray index packed in 16 bits
         if (const char *e = std::getenv("RECTV_SCATTER"))
             if (!std::strcmp(e, "direct")) tc_scatter = false;
         auto up = [&](const void *src, size_t bytes) -> void * {

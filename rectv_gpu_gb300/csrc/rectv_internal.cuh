@@ -63,12 +63,15 @@ struct UsGeo {
 };
 
 // Weights of one polar sample restricted to one 16x16 tile of the adjoint
-// plan (zero outside the sample's 9x9 stencil), with its ray, detector index
-// and the mask of tile rows its stencil covers.
+// plan (zero outside the sample's 9x9 stencil), with its ray and the mask of
+// tile rows its stencil covers (thm = theta << 16 | mask, theta < 65536),
+// its detector index and row factor (-1)^(k+1) shiftadj(k) (pi/mu)/n.
 struct AdjRec {
     float wx[16];
     float wy[16];
-    int th, k, mask, pad;
+    int thm;
+    int k;
+    float2 sf;
 };
 
 // Per-angle constants uploaded at geometry set-up.

@@ -103,7 +103,8 @@ __device__ __forceinline__ void mma_tf32_ts(uint32_t d, uint32_t a, uint64_t b, 
 // the tile (wrap TOMO_ADJ, kernels_radonusfft.cuh:40-64).
 // ---------------------------------------------------------------------------
 __global__ void k_adj_records(AdjRec *__restrict__ recs, const uint32_t *__restrict__ pts,
-                              const int4 *__restrict__ items, const float2 *__restrict__ sincos, UsGeo g) {
+                              const int4 *__restrict__ items, const float2 *__restrict__ sincos,
+                              const float2 *__restrict__ shifta, UsGeo g) {
     const int4 it = items[blockIdx.x];
     const int tyi = it.x / g.NT, txi = it.x - tyi * g.NT;
     const int P = g.P, half = P / 2;
@@ -130,17 +131,18 @@ __global__ void k_adj_records(AdjRec *__restrict__ recs, const uint32_t *__restr
             r.wy[c] = iny ? tap_weight(fy, by, y0, g) : 0.f;
             mask |= iny ? (1 << c) : 0;
         }
-        r.th = th;
+        r.thm = (th << 16) | mask;
         r.k = k;
-        r.mask = mask;
-        r.pad = 0;
+        const float2 sh = shifta[k];
+        const float cf = (k & 1) ? g.cw : -g.cw;
+        r.sf = make_float2(sh.x * cf, sh.y * cf);
         recs[(long long)it.y + e] = r;
     }
 }
 
 void launch_adj_records(AdjRec *recs, const GeoDev &gd, const UsGeo &g, cudaStream_t s) {
     if (gd.n_adj_items == 0) return;
-    k_adj_records<<<gd.n_adj_items, 256, 0, s>>>(recs, gd.adj_pts, gd.adj_items, gd.sincos, g);
+    k_adj_records<<<gd.n_adj_items, 256, 0, s>>>(recs, gd.adj_pts, gd.adj_items, gd.sincos, gd.shiftadj, g);
     LAUNCH_CHECK("k_adj_records");
 }
 
@@ -186,12 +188,10 @@ __global__ void __launch_bounds__(kThr, 2)
         __syncthreads();
         // ---- E = (-1)^(k+1) shiftadj(k) FFT(row)(k) (pi/mu)/n, then T_p(cy) = E(p) wy_p(cy) ----
         for (int e = tid; e < cnt; e += kThr) {
-            const int th = sm.rec[e].th, k = sm.rec[e].k;
+            const int th = (unsigned)sm.rec[e].thm >> 16, k = sm.rec[e].k;
             float2 R = (k <= g.n / 2) ? __ldg(rz + (long long)th * hn + k) : __ldg(rz + (long long)th * hn + (g.n - k));
             if (k > g.n / 2) R.y = -R.y;
-            const float2 E = cmul(R, __ldg(shifta + k));
-            const float c = (k & 1) ? g.cw : -g.cw;
-            sm.e[e] = make_float2(E.x * c, E.y * c);
+            sm.e[e] = cmul(R, sm.rec[e].sf);
         }
         __syncthreads();
         for (int i = tid; i < cnt * kT; i += kThr) {
@@ -202,7 +202,7 @@ __global__ void __launch_bounds__(kThr, 2)
         }
         // ---- first table row of each ray: block-wide scan of ray starts ----
         int flag = 0;
-        if (tid < cnt) flag = (tid == 0 || sm.rec[tid].th != sm.rec[tid - 1].th) ? 1 : 0;
+        if (tid < cnt) flag = (tid == 0 || (sm.rec[tid].thm >> 16) != (sm.rec[tid - 1].thm >> 16)) ? 1 : 0;
         int incl = flag;
 #pragma unroll
         for (int o = 1; o < 32; o <<= 1) {
@@ -262,7 +262,7 @@ __global__ void __launch_bounds__(kThr, 2)
                     const int r = 2 * q4 + i;
                     float2 kv = make_float2(0.f, 0.f);
                     if (r < nb && jbase + j < g.m)
-                        kv = __ldg(kmat + (long long)sm.rec[sm.seg_first[sb + r]].th * g.m + jbase + j);
+                        kv = __ldg(kmat + (long long)((unsigned)sm.rec[sm.seg_first[sb + r]].thm >> 16) * g.m + jbase + j);
                     bv[2 * i] = o == 0 ? kv.x : -kv.y;
                     bv[2 * i + 1] = o == 0 ? kv.y : kv.x;
                 }
