@@ -67,6 +67,10 @@ struct ScTcSmem {
     float bhi[kN * kK];           // B = conj K' of the batch's rays, FP32: rows 0..31 of the MMA's B
     float blo[kN * kK];           // B - trunc(B): rows 32..63 (contiguous with bhi)
     int seg_first[kTab + 1];
+    // per warp and ray: the table rows [lo, hi) from the first to the last
+    // sample whose stencil covers one of the warp's two tile rows (samples
+    // move monotonically along a ray, so the others contribute zero weight)
+    unsigned short rlo[kWarps][kTab], rhi[kWarps][kTab];
     int wsum[kWarps];
     unsigned long long bar;
     uint32_t tslot;
@@ -222,6 +226,30 @@ __global__ void __launch_bounds__(kThr, 2)
         if (tid < cnt && flag) sm.seg_first[incl - 1] = tid;
         if (tid == 0) sm.seg_first[nseg] = cnt;
         __syncthreads();  // ray starts and T written
+        for (int r = tid; r < nseg; r += kThr) {
+            const int e0 = sm.seg_first[r], e1 = sm.seg_first[r + 1];
+            int lo[kWarps], hi[kWarps];
+#pragma unroll
+            for (int w = 0; w < kWarps; ++w) {
+                lo[w] = e1;
+                hi[w] = e0;
+            }
+            for (int e = e0; e < e1; ++e) {
+                const int msk = sm.rec[e].thm & 0xffff;
+#pragma unroll
+                for (int w = 0; w < kWarps; ++w)
+                    if (msk & (3 << (2 * w))) {
+                        lo[w] = min(lo[w], e);
+                        hi[w] = e + 1;
+                    }
+            }
+#pragma unroll
+            for (int w = 0; w < kWarps; ++w) {
+                sm.rlo[w][r] = (unsigned short)lo[w];
+                sm.rhi[w][r] = (unsigned short)max(lo[w], hi[w]);
+            }
+        }
+        __syncthreads();
 
         for (int sb = 0; sb < nseg; sb += kBatch) {
             const int nb = min(kBatch, nseg - sb);
@@ -231,9 +259,9 @@ __global__ void __launch_bounds__(kThr, 2)
             for (int r = 0; r < kBatch; ++r) {
                 float2 v = make_float2(0.f, 0.f);
                 if (r < nb) {  // T and wx vanish outside the stencil: no tests in the loop
-                    const int e1 = sm.seg_first[sb + r + 1];
+                    const int e1 = sm.rhi[wid][sb + r];
 #pragma unroll 4
-                    for (int e = sm.seg_first[sb + r]; e < e1; ++e) {
+                    for (int e = sm.rlo[wid][sb + r]; e < e1; ++e) {
                         const float w = sm.rec[e].wx[cx];
                         v = ffma2(make_float2(w, w), sm.t[e][cy], v);
                     }
