@@ -44,7 +44,7 @@ def _compile(src, verbose):
     obj = os.path.join(BUILD_DIR, os.path.splitext(src)[0] + ".o")
     path = os.path.join(CSRC, src)
     cmd = [_nvcc(), "-c", path, "-o", obj, "-O3", "-std=c++17", "-I", INCLUDE, "-I", CSRC,
-           "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off"]
+           "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off", "-Xcompiler", "-pthread"]
     if src.endswith(".cu"):
         cmd += ARCH + ["-lineinfo", "--expt-relaxed-constexpr"]
         if os.environ.get("RECTV_PTXAS_VERBOSE"):
@@ -81,7 +81,7 @@ def build(force=False, verbose=False):
         libdir = os.path.join(_cuda_home(), "lib")
     tmp = LIB_PATH + ".tmp"
     cmd = [_nvcc(), "-shared", "-o", tmp] + objs + ARCH + [
-        "-L", libdir, "-lcufft", "-lcudart", "-Xlinker", "-rpath," + libdir]
+        "-L", libdir, "-lcufft", "-lcudart", "-Xcompiler", "-pthread", "-Xlinker", "-rpath," + libdir]
     res = subprocess.run(cmd, capture_output=True, text=True)
     if res.returncode != 0:
         raise RuntimeError("link failed: %s\n%s\n%s" % (" ".join(cmd), res.stdout, res.stderr))

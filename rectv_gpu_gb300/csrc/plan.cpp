@@ -16,6 +16,10 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdint>
+#include <exception>
+#include <mutex>
+#include <thread>
+#include <utility>
 #include <vector>
 
 #include "rectv_internal.cuh"
@@ -26,6 +30,31 @@ namespace {
 inline int wrapi(int a, int m) {
     a %= m;
     return a < 0 ? a + m : a;
+}
+
+// fn(0) .. fn(nthr-1) on nthr host threads (the calling thread runs fn(0))
+template <class F>
+void parallel_for(int nthr, F &&fn) {
+    std::vector<std::thread> pool;
+    std::exception_ptr err;
+    std::mutex mu;
+    for (int w = 1; w < nthr; ++w)
+        pool.emplace_back([&, w] {
+            try {
+                fn(w);
+            } catch (...) {
+                std::lock_guard<std::mutex> lk(mu);
+                if (!err) err = std::current_exception();
+            }
+        });
+    try {
+        fn(0);
+    } catch (...) {
+        std::lock_guard<std::mutex> lk(mu);
+        if (!err) err = std::current_exception();
+    }
+    for (auto &t : pool) t.join();
+    if (err) std::rethrow_exception(err);
 }
 }  // namespace
 
@@ -42,61 +71,91 @@ HostPlan build_plan(const float *theta, int n, int ntheta, int T, int fwd_cap, i
     const long long npts = (long long)ntheta * (n - 1);
     std::vector<int> ftile(npts);
     std::vector<int4> atiles(npts);  // up to 4 tiles, -1 = none
-    std::vector<int> fcnt(ntiles, 0), acnt(ntiles, 0);
     const float tn = (float)(2 * n);
-    long long ip = 0;
-    for (int th = 0; th < ntheta; ++th) {
-        const float s = p.sincos[th].x, c = p.sincos[th].y;
-        for (int k = 1; k < n; ++k, ++ip) {
-            const float q = (float)(k - n / 2) / (float)n;
-            float x0 = q * s, y0 = q * c;
-            if (x0 >= 0.5f) x0 = 0.5f - 1e-5f;
-            if (y0 >= 0.5f) y0 = 0.5f - 1e-5f;
-            const int fx = (int)std::floor(tn * x0);
-            const int fy = (int)std::floor(tn * y0);
-            const int KX = n + fx, KY = n + fy;  // in [0, P)
-            const int t = (KY / T) * NT + (KX / T);
-            ftile[ip] = t;
-            fcnt[t]++;
-            // tiles holding any cell of the 9x9 stencil (cells wrap modulo P)
-            int xs[kTaps], ys[kTaps], nx = 0, ny = 0;
-            for (int i = 0; i < kTaps; ++i) {
-                const int tx = wrapi(KX - kR + i, P) / T, ty = wrapi(KY - kR + i, P) / T;
-                bool seen = false;
-                for (int a = 0; a < nx; ++a) seen |= (xs[a] == tx);
-                if (!seen) xs[nx++] = tx;
-                seen = false;
-                for (int a = 0; a < ny; ++a) seen |= (ys[a] == ty);
-                if (!seen) ys[ny++] = ty;
+    std::vector<float> qk(n);
+    for (int k = 1; k < n; ++k) qk[k] = (float)(k - n / 2) / (float)n;
+    if (T < kTaps) throw Error(1, "tile smaller than the interpolation stencil");
+    // Angles are split into contiguous ranges, one per host thread; each
+    // thread counts its samples per tile and later places them at its own
+    // offsets, so every tile keeps the theta-major sample order.
+    const int nthr = std::max(1, std::min<int>((int)std::thread::hardware_concurrency(), std::min(16, ntheta)));
+    auto th_range = [&](int w) { return std::make_pair((int)((long long)ntheta * w / nthr),
+                                                      (int)((long long)ntheta * (w + 1) / nthr)); };
+    std::vector<std::vector<int>> fcw(nthr, std::vector<int>(ntiles, 0)), acw(nthr, std::vector<int>(ntiles, 0));
+    auto bin = [&](int w) {
+        const auto rg = th_range(w);
+        std::vector<int> &fcnt = fcw[w], &acnt = acw[w];
+        long long ip = (long long)rg.first * (n - 1);
+        for (int th = rg.first; th < rg.second; ++th) {
+            const float s = p.sincos[th].x, c = p.sincos[th].y;
+            for (int k = 1; k < n; ++k, ++ip) {
+                const float q = qk[k];
+                float x0 = q * s, y0 = q * c;
+                if (x0 >= 0.5f) x0 = 0.5f - 1e-5f;
+                if (y0 >= 0.5f) y0 = 0.5f - 1e-5f;
+                const int fx = (int)std::floor(tn * x0);
+                const int fy = (int)std::floor(tn * y0);
+                const int KX = n + fx, KY = n + fy;  // in [0, P)
+                const int t = (KY / T) * NT + (KX / T);
+                ftile[ip] = t;
+                fcnt[t]++;
+                // tiles holding any cell of the 9x9 stencil (cells wrap modulo P):
+                // a stencil row spans 9 < T cells, so it touches the tiles of its
+                // first and last cell and none between
+                const int xa = wrapi(KX - kR, P) / T, xb = wrapi(KX + kR, P) / T;
+                const int ya = wrapi(KY - kR, P) / T, yb = wrapi(KY + kR, P) / T;
+                const int nx = (xa == xb) ? 1 : 2, ny = (ya == yb) ? 1 : 2;
+                const int xs[2] = {xa, xb}, ys[2] = {ya, yb};
+                int tl[4] = {-1, -1, -1, -1}, nt = 0;
+                for (int a = 0; a < ny; ++a)
+                    for (int b = 0; b < nx; ++b) tl[nt++] = ys[a] * NT + xs[b];
+                atiles[ip] = make_int4(tl[0], tl[1], tl[2], tl[3]);
+                for (int i = 0; i < nt; ++i) acnt[tl[i]]++;
             }
-            if (nx > 2 || ny > 2) throw Error(1, "tile smaller than the interpolation stencil");
-            int tl[4] = {-1, -1, -1, -1}, nt = 0;
-            for (int a = 0; a < ny; ++a)
-                for (int b = 0; b < nx; ++b) tl[nt++] = ys[a] * NT + xs[b];
-            atiles[ip] = make_int4(tl[0], tl[1], tl[2], tl[3]);
-            for (int i = 0; i < nt; ++i) acnt[tl[i]]++;
         }
-    }
-    // forward: counting sort by tile (stable: theta-major order inside a tile)
+    };
+    parallel_for(nthr, bin);
+    // forward and adjoint: counting sort by tile (stable: theta-major order inside a tile)
     std::vector<long long> foff(ntiles + 1, 0), aoff(ntiles + 1, 0);
+    std::vector<int> fcnt(ntiles, 0), acnt(ntiles, 0);
     for (int t = 0; t < ntiles; ++t) {
+        for (int w = 0; w < nthr; ++w) {
+            fcnt[t] += fcw[w][t];
+            acnt[t] += acw[w][t];
+        }
         foff[t + 1] = foff[t] + fcnt[t];
         aoff[t + 1] = aoff[t] + acnt[t];
     }
     p.fwd_pts.resize(foff[ntiles]);
     p.adj_pts.resize(aoff[ntiles]);
     {
-        std::vector<long long> fpos(foff.begin(), foff.end() - 1), apos(aoff.begin(), aoff.end() - 1);
-        ip = 0;
-        for (int th = 0; th < ntheta; ++th)
-            for (int k = 1; k < n; ++k, ++ip) {
-                const uint32_t id = (uint32_t)th * (uint32_t)n + (uint32_t)k;
-                p.fwd_pts[fpos[ftile[ip]]++] = id;
-                const int4 a = atiles[ip];
-                const int tl[4] = {a.x, a.y, a.z, a.w};
-                for (int i = 0; i < 4; ++i)
-                    if (tl[i] >= 0) p.adj_pts[apos[tl[i]]++] = id;
+        // thread w's first slot in tile t: the tile's offset plus the counts of threads before it
+        std::vector<std::vector<long long>> fpos(nthr, std::vector<long long>(ntiles)),
+            apos(nthr, std::vector<long long>(ntiles));
+        for (int t = 0; t < ntiles; ++t) {
+            long long f = foff[t], a = aoff[t];
+            for (int w = 0; w < nthr; ++w) {
+                fpos[w][t] = f;
+                apos[w][t] = a;
+                f += fcw[w][t];
+                a += acw[w][t];
             }
+        }
+        auto place = [&](int w) {
+            const auto rg = th_range(w);
+            std::vector<long long> &fp = fpos[w], &ap = apos[w];
+            long long ip = (long long)rg.first * (n - 1);
+            for (int th = rg.first; th < rg.second; ++th)
+                for (int k = 1; k < n; ++k, ++ip) {
+                    const uint32_t id = (uint32_t)th * (uint32_t)n + (uint32_t)k;
+                    p.fwd_pts[fp[ftile[ip]]++] = id;
+                    const int4 a = atiles[ip];
+                    const int tl[4] = {a.x, a.y, a.z, a.w};
+                    for (int i = 0; i < 4; ++i)
+                        if (tl[i] >= 0) p.adj_pts[ap[tl[i]]++] = id;
+                }
+        };
+        parallel_for(nthr, place);
     }
     // forward items: whole rays (runs of equal theta) of one tile, at most
     // fwd_cap samples; rays with several samples each go to the tensor cores

@@ -109,6 +109,13 @@ struct Handle {
     // cuFFT
     cufftHandle p_r2c2d = 0, p_c2c2d = 0, p_rows_c2c = 0, p_rows_r2c = 0;
     CUtensorMap spec_tmap;  // TMA boxes of the forward spectra (tensor-core gather)
+    // key of the geometry on the device (set_geometry)
+    bool geo_valid = false, geo_has_phi = false, geo_tc_scatter = false;
+    float geo_center = 0.f, geo_tc_spr = 0.f;
+    std::vector<float> geo_theta, geo_phi;
+    // key of the captured graphs besides the geometry (setup)
+    int graph_titer = -1;
+    float graph_lambda0 = 0.f, graph_lambda1 = 0.f;
     bool plans_made = false;
     int img_per_fft = 0;
     void *fft_work = nullptr;
@@ -295,6 +302,7 @@ struct Handle {
     }
 
     void free_geo() {
+        geo_valid = false;
         for (void *p : geo_owned) cudaFree(p);
         geo_owned.clear();
         int *err = gd.err;
@@ -331,9 +339,10 @@ struct Handle {
     }
 
     // ---- geometry: angle plan, basis mixing matrix, centre shifts ----
-    void set_geometry(const float *theta_h, const float *phi_h, float center) {
-        drop_graphs();
-        free_geo();
+    // Returns true when the geometry was (re)built: plan, K', shifts and
+    // records are a function of (theta, phi, center) and of the kernel choice,
+    // so a call with the same values keeps them (and the captured graphs).
+    bool set_geometry(const float *theta_h, const float *phi_h, float center) {
         // gather items hold at most one sample table; scatter items are whole
         // tiles (one block owns each tile, so tiles are stored, never added)
         // forward items with >= 2 samples per ray use the tensor-core gather
@@ -345,12 +354,19 @@ struct Handle {
             if (!std::strcmp(e, "direct")) tc_min_spr = -1.0f;
             if (!std::strcmp(e, "tc") && mp16()) tc_min_spr = 0.0f;
         }
-        HostPlan hp = build_plan(theta_h, n, ntheta, ug.T, table_capacity(), 1 << 30, tc_min_spr);
         // adjoint: tensor-core time-sample mixing (k_scatter_tc) from 9 time
         // samples up; RECTV_SCATTER=direct forces the FP32 scatter
         bool tc_scatter = mp16() && ntheta < 65536;  // ray index packed in 16 bits
         if (const char *e = std::getenv("RECTV_SCATTER"))
             if (!std::strcmp(e, "direct")) tc_scatter = false;
+        const size_t nphi = phi_h ? (size_t)2 * m * ntheta : 0;
+        if (geo_valid && center == geo_center && tc_min_spr == geo_tc_spr && tc_scatter == geo_tc_scatter &&
+            (phi_h != nullptr) == geo_has_phi && !std::memcmp(theta_h, geo_theta.data(), sizeof(float) * ntheta) &&
+            (!phi_h || !std::memcmp(phi_h, geo_phi.data(), sizeof(float) * nphi)))
+            return false;
+        drop_graphs();
+        free_geo();
+        HostPlan hp = build_plan(theta_h, n, ntheta, ug.T, table_capacity(), 1 << 30, tc_min_spr);
         auto up = [&](const void *src, size_t bytes) -> void * {
             void *p = nullptr;
             CUDA_CHECK(cudaMalloc(&p, std::max<size_t>(bytes, 16)));
@@ -422,6 +438,14 @@ struct Handle {
         gd.deapod = (float *)up(dp.data(), n * sizeof(float));
         if (gd.tc_scatter) launch_adj_records(gd.adj_recs, gd, ug, stream);
         CUDA_CHECK(cudaStreamSynchronize(stream));  // host vectors go out of scope
+        geo_theta.assign(theta_h, theta_h + ntheta);
+        geo_phi.assign(phi_h, phi_h + nphi);
+        geo_has_phi = phi_h != nullptr;
+        geo_center = center;
+        geo_tc_spr = tc_min_spr;
+        geo_tc_scatter = tc_scatter;
+        geo_valid = true;
+        return true;
     }
 
     // ---- operators on one batch of zb slices ----
@@ -516,11 +540,17 @@ struct Handle {
         check_live();
         if (titer_ < 0) throw Error(RECTV_ERR_ARG, "rectv: titer must be >= 0");
         if (!phi_h) throw Error(RECTV_ERR_ARG, "rectv: phi is required");
-        set_geometry(theta_h, phi_h, center);
+        const bool rebuilt = set_geometry(theta_h, phi_h, center);
         lambda0 = lambda0_;
         set_lambda1(lambda1_);
         titer = titer_;
-        drop_graphs();
+        // graphs bake in the geometry, titer and the two lambdas
+        if (rebuilt || titer != graph_titer || lambda0 != graph_lambda0 || lambda1 != graph_lambda1) {
+            drop_graphs();
+            graph_titer = titer;
+            graph_lambda0 = lambda0;
+            graph_lambda1 = lambda1;
+        }
         // initial guess (zero, as rectv.cu:119-120, unless given) and ADMM state (rectv.cu:121-125)
         cur = 0;
         if (init)
