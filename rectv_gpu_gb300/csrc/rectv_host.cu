@@ -107,7 +107,7 @@ struct Handle {
     std::vector<void *> geo_owned;
 
     // cuFFT
-    cufftHandle p_r2c2d = 0, p_c2c2d = 0, p_rows_c2c = 0, p_rows_r2c = 0;
+    cufftHandle p_r2c2d = 0, p_c2c2d = 0, p_rows_c2c = 0, p_rows_r2c = 0, p_c2r2d = 0;
     CUtensorMap spec_tmap;  // TMA boxes of the forward spectra (tensor-core gather)
     // key of the geometry on the device (set_geometry)
     bool geo_valid = false, geo_has_phi = false, geo_tc_scatter = false;
@@ -253,10 +253,12 @@ struct Handle {
         size_t ws = 0, w1 = 0;
         CUFFT_CHECK(cufftCreate(&p_r2c2d));
         CUFFT_CHECK(cufftCreate(&p_c2c2d));
+        CUFFT_CHECK(cufftCreate(&p_c2r2d));
         CUFFT_CHECK(cufftCreate(&p_rows_c2c));
         CUFFT_CHECK(cufftCreate(&p_rows_r2c));
         plans_made = true;
-        for (cufftHandle h : {p_r2c2d, p_c2c2d, p_rows_c2c, p_rows_r2c}) CUFFT_CHECK(cufftSetAutoAllocation(h, 0));
+        for (cufftHandle h : {p_r2c2d, p_c2c2d, p_rows_c2c, p_rows_r2c, p_c2r2d})
+            CUFFT_CHECK(cufftSetAutoAllocation(h, 0));
         {  // 2D R2C in place inside the padded forward images: real rows of
            // 2 qp floats -> P/2+1 complex of a qp-complex row
             int nn[2] = {P, P};
@@ -264,6 +266,14 @@ struct Handle {
             int onem[2] = {P, ug.qp};
             CUFFT_CHECK(cufftMakePlanMany(p_r2c2d, 2, nn, inem, 1, (int)(2 * ug.img_fwd), onem, 1, (int)ug.img_fwd,
                                           CUFFT_R2C, per, &w1));
+            ws = std::max(ws, w1);
+        }
+        {  // 2D C2R in place: Hermitian half planes of P/2+1 complex -> real rows of P+2 floats
+            int nn[2] = {P, P};
+            int inem[2] = {P, P / 2 + 1};
+            int onem[2] = {P, P + 2};
+            CUFFT_CHECK(cufftMakePlanMany(p_c2r2d, 2, nn, inem, 1, P * (P / 2 + 1), onem, 1, P * (P + 2), CUFFT_C2R,
+                                          per, &w1));
             ws = std::max(ws, w1);
         }
         {  // 2D C2C full plane
@@ -287,7 +297,7 @@ struct Handle {
             ws = std::max(ws, w1);
         }
         if (ws > 0) fft_work = dalloc<char>(ws, owned);
-        for (cufftHandle h : {p_r2c2d, p_c2c2d, p_rows_c2c, p_rows_r2c}) {
+        for (cufftHandle h : {p_r2c2d, p_c2c2d, p_rows_c2c, p_rows_r2c, p_c2r2d}) {
             CUFFT_CHECK(cufftSetWorkArea(h, fft_work));
             CUFFT_CHECK(cufftSetStream(h, stream));
         }
@@ -317,6 +327,7 @@ struct Handle {
         if (plans_made) {
             cufftDestroy(p_r2c2d);
             cufftDestroy(p_c2c2d);
+            cufftDestroy(p_c2r2d);
             cufftDestroy(p_rows_c2c);
             cufftDestroy(p_rows_r2c);
             plans_made = false;
@@ -470,9 +481,22 @@ struct Handle {
         CUFFT_CHECK(cufftExecR2C(p_rows_r2c, reinterpret_cast<cufftReal *>(rows),
                                  reinterpret_cast<cufftComplex *>(rows)));
         if (row_filter) launch_filter_rows(rows, row_filter, (long long)zb * ntheta, n, stream);
+        const int nimg = zb * m;
+        if (gd.tc_scatter) {
+            // Re IFFT2 of the scattered grids as a C2R of their Hermitian part,
+            // which the tensor-core scatter adds into zeroed half planes
+            const long long img_half = (long long)ug.P * (ug.P / 2 + 1);
+            CUDA_CHECK(cudaMemsetAsync(spec, 0, sizeof(float2) * (size_t)nimg * img_half, stream));
+            launch_scatter_adj(rows, spec, zb, gd, ug, stream);
+            for (int i = 0; i < nimg; i += img_per_fft) {
+                cufftComplex *p = reinterpret_cast<cufftComplex *>(spec + (size_t)i * img_half);
+                CUFFT_CHECK(cufftExecC2R(p_c2r2d, p, reinterpret_cast<cufftReal *>(p)));
+            }
+            launch_crop_accum_real(reinterpret_cast<const float *>(spec), u, zb, tau, gd.deapod, ug, stream);
+            return;
+        }
         launch_zero_split(spec, zb, gd, ug, stream);
         launch_scatter_adj(rows, spec, zb, gd, ug, stream);
-        const int nimg = zb * m;
         for (int i = 0; i < nimg; i += img_per_fft) {
             cufftComplex *p = reinterpret_cast<cufftComplex *>(spec + (size_t)i * ug.img_adj);
             CUFFT_CHECK(cufftExecC2C(p_c2c2d, p, p, CUFFT_INVERSE));
@@ -749,8 +773,9 @@ struct Handle {
                 *bytes = (double)zb * m * P * (P / 2 + 1) * 8.0 + (double)zb * ntheta * n * 8.0;
                 *flops = npts * (81.0 * 2.0 * m * 2.0 + 8.0 * m + 18.0 * 4.0);
                 break;
-            case 1:  // scatter: half row spectra in, full-plane grids out
-                *bytes = (double)zb * ntheta * (n / 2 + 1) * 8.0 + (double)zb * m * P * P * 8.0;
+            case 1:  // scatter: half row spectra in; Hermitian half planes out (tensor-core path), else full planes
+                *bytes = (double)zb * ntheta * (n / 2 + 1) * 8.0 +
+                         (gd.tc_scatter ? (double)zb * m * P * (P / 2 + 1) * 8.0 : (double)zb * m * P * P * 8.0);
                 *flops = npts * (81.0 * 2.0 * m * 2.0 + 8.0 * m + 18.0 * 4.0);
                 break;
             case 2:  // graddiv: u in, u out, psi and mu in

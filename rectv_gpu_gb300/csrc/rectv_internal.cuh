@@ -127,6 +127,9 @@ void launch_scatter_adj(const float2 *rowsc, float2 *spec, int zb, const GeoDev 
                         const UsGeo &g, cudaStream_t s);
 void launch_crop_accum(const float2 *spec, float *u, int zb, float tau, const float *deapod,
                        const UsGeo &g, cudaStream_t s);
+// the same from the real output of the C2R inverse (rows of 2 (P/2+1) floats)
+void launch_crop_accum_real(const float *out, float *u, int zb, float tau, const float *deapod, const UsGeo &g,
+                            cudaStream_t s);
 // tensor-core gather (gather_tc.cu): items of fwd_tc_items, time samples
 // [jbase, jbase + 16)
 void launch_gather_tc(float2 *rows, int zb, const GeoDev &gd, const UsGeo &g, const CUtensorMap &tmap, int jbase,
@@ -135,7 +138,8 @@ void launch_gather_tc(float2 *rows, int zb, const GeoDev &gd, const UsGeo &g, co
 // 16 images x 24 rows x 26 cells
 void make_spec_tensor_map(CUtensorMap *map, float2 *spec, int nimg, const UsGeo &g);
 void gather_tc_prepare();
-// tensor-core scatter (scatter_tc.cu): all adjoint items, time samples [jbase, jbase + 16)
+// tensor-core scatter (scatter_tc.cu): all adjoint items, time samples [jbase, jbase + 16),
+// added into the zeroed Hermitian half planes [z][t][P][P/2+1] of the C2R inverse
 void launch_scatter_tc(const float2 *rowsc, float2 *spec, int zb, const GeoDev &gd, const UsGeo &g, int jbase,
                        cudaStream_t s);
 void scatter_tc_prepare();

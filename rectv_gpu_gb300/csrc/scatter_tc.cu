@@ -29,7 +29,8 @@
 //    FP32 sums in registers (the tensor core's own FP32 accumulation rounds
 //    differently and would drift over the many batches of central tiles),
 //    and the next batch's grids are formed while the MMAs run.
-// The tile is stored once per block (added, for a tile split over blocks).
+// The tile is added once per block into the Hermitian half plane that the
+// C2R inverse transform takes (see the epilogue).
 #include <cuda.h>
 #include <cuda_runtime.h>
 
@@ -344,21 +345,27 @@ __global__ void __launch_bounds__(kThr, 2)
 #pragma unroll
         for (int i = 0; i < 32; ++i) acc[i] += v[i] + w2[i];
     }
+    // ---- the adjoint only needs Re IFFT2(X) = C2R of the Hermitian part
+    // H(k) = (X(k) + conj X(-k)) / 2 on the half plane kx <= n: each cell adds
+    // X(k)/2 to H(k) and conj(X(k))/2 to H(-k) where they lie in the half plane
+    // (at most two adds per H cell from two blocks, onto zeros: the sum does not
+    // depend on their order); the pre-IFFT fftshift sign is applied here ----
     const int KY = tyi * kT + cy, KX = txi * kT + cx;
     if (KY < P && KX < P) {
-        const float sg = ((KX + KY) & 1) ? -1.f : 1.f;
-        float2 *dst = spec + ((long long)z * g.m + jbase) * g.img_adj + (long long)KY * P + KX;
+        const int half = P / 2, hp = half + 1;
+        const long long img_half = (long long)P * hp;
+        const float sg = ((KX + KY) & 1) ? -0.5f : 0.5f;
+        const bool here = KX <= half, mirror = KX >= half || KX == 0;
+        const long long o1 = (long long)KY * hp + KX;
+        const long long o2 = (long long)((P - KY) % P) * hp + (P - KX) % P;
+        float2 *dst = spec + ((long long)z * g.m + jbase) * img_half;
 #pragma unroll
         for (int j = 0; j < 16; ++j) {
             if (jbase + j >= g.m) break;
             const float2 v = make_float2(sg * acc[2 * j], sg * acc[2 * j + 1]);
-            float2 *d = dst + (long long)j * g.img_adj;
-            if (it.w) {
-                atomicAdd(&d->x, v.x);
-                atomicAdd(&d->y, v.y);
-            } else {
-                *d = v;
-            }
+            float2 *d = dst + (long long)j * img_half;
+            if (here) atomicAdd(d + o1, v);
+            if (mirror) atomicAdd(d + o2, make_float2(v.x, -v.y));
         }
     }
     tc::fence_before();

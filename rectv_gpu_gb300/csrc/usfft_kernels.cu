@@ -682,6 +682,30 @@ void launch_crop_accum(const float2 *spec, float *u, int zb, float tau, const fl
     LAUNCH_CHECK("k_crop_accum");
 }
 
+// Same epilogue after the C2R inverse of the Hermitian half planes: real
+// images with rows of 2 (P/2+1) floats.
+__global__ void k_crop_accum_real(const float *__restrict__ out, float *__restrict__ u,
+                                  const float *__restrict__ dp, int n, int P, long long img_real, float c) {
+    const int x = blockIdx.x * blockDim.x + threadIdx.x;
+    const int y = blockIdx.y;
+    const long long img = blockIdx.z;
+    if (x >= n) return;
+    const int X = x + n / 2, Y = y + n / 2;
+    float v = out[img * img_real + (long long)Y * (P + 2) + X];
+    v = ((X + Y) & 1) ? -v : v;
+    u[(img * n + y) * n + x] += c * v * dp[x] * dp[y];
+}
+
+void launch_crop_accum_real(const float *out, float *u, int zb, float tau, const float *deapod, const UsGeo &g,
+                            cudaStream_t s) {
+    dim3 gs((g.n + 255) / 256, g.n, zb * g.m);
+    const double scale = 1.0 / std::sqrt((double)g.n * (double)g.ntheta);
+    const float c = (float)(tau * scale / (4.0 * g.n * (double)g.n));
+    const long long img_real = 2LL * g.P * (g.P / 2 + 1);
+    k_crop_accum_real<<<gs, 256, 0, s>>>(out, u, deapod, g.n, g.P, img_real, c);
+    LAUNCH_CHECK("k_crop_accum_real");
+}
+
 template <int MP, int T>
 static void set_attrs() {
     const int fs = (int)((T + 2 * kR) * (T + 2 * kR) * MP * sizeof(float2) + sizeof(EntryTab));
