@@ -394,6 +394,8 @@ struct Handle {
         gd.adj_pts = (uint32_t *)up(hp.adj_pts.data(), hp.adj_pts.size() * 4);
         gd.adj_items = (int4 *)up(hp.adj_items.data(), hp.adj_items.size() * sizeof(int4));
         gd.n_adj_items = (int)hp.adj_items.size();
+        gd.n_adj_busy = 0;
+        while (gd.n_adj_busy < gd.n_adj_items && hp.adj_items[gd.n_adj_busy].z > 0) ++gd.n_adj_busy;
         gd.split_tiles = (int *)up(hp.split_tiles.data(), hp.split_tiles.size() * 4);
         gd.n_split_tiles = (int)hp.split_tiles.size();
         gd.tc_scatter = tc_scatter;

@@ -94,6 +94,7 @@ struct GeoDev {
     int *err = nullptr;          // device counter of host/device bin disagreements
     bool tc_scatter = false;     // adjoint time-sample mixing on the tensor cores (k_scatter_tc)
     AdjRec *adj_recs = nullptr;  // geometry records of adj_pts (tensor-core scatter only)
+    int n_adj_busy = 0;          // leading adj_items with samples (items are sorted by count)
 };
 
 // Host-side angle plan (built in plan.cpp).

@@ -14,7 +14,10 @@
 // stencil), the ray, the detector index and a mask of the tile rows the
 // stencil covers.
 //
-// Per (slice, tile) block of 256 threads (thread = cell):
+// Persistent blocks of 256 threads (thread = cell), two per SM, take the
+// (tile, slice) units with samples round-robin; the records of the next table
+// of samples are bulk-copied into a second shared buffer (TMA engine,
+// mbarrier) while the current one is processed.  Per unit and table:
 //  * per sample: E(p) (the row spectrum value times (-1)^(k+1) shiftadj(k)
 //    (pi/mu)/n) and T_p(cy) = E(p) wy_p(cy) for the tile's 16 rows;
 //  * per batch of 16 rays: every cell sums its value of each ray's grid
@@ -29,10 +32,12 @@
 //    FP32 sums in registers (the tensor core's own FP32 accumulation rounds
 //    differently and would drift over the many batches of central tiles),
 //    and the next batch's grids are formed while the MMAs run.
-// The tile is added once per block into the Hermitian half plane that the
+// The tile is added once per unit into the Hermitian half plane that the
 // C2R inverse transform takes (see the epilogue).
 #include <cuda.h>
 #include <cuda_runtime.h>
+
+#include <algorithm>
 
 #include "rectv_internal.cuh"
 #include "tcgen05.cuh"
@@ -45,7 +50,7 @@ namespace {
 constexpr int kT = 16;
 constexpr int kCells = kT * kT;     // 256 = 2 M tiles
 constexpr int kMT = kCells / 128;
-constexpr int kTab = 256;           // samples per table
+constexpr int kTab = 192;           // samples per table (two record buffers and two blocks per SM)
 constexpr int kBatch = 16;          // rays per MMA batch (K = 32)
 constexpr int kK = 2 * kBatch;
 constexpr int kN = 32;              // 16 time samples x (re, im)
@@ -62,7 +67,7 @@ __device__ __forceinline__ int off32(int row, int kk) {
 }
 
 struct ScTcSmem {
-    AdjRec rec[kTab];             // geometry records of the table's samples
+    AdjRec rec[2][kTab];          // geometry records of this table and the next (bulk copies)
     float2 t[kTab][kT];           // T_p(cy) = E(p) wy_p(cy)
     float2 e[kTab];               // E(p) of this slice
     float bhi[kN * kK];           // B = conj K' of the batch's rays, FP32: rows 0..31 of the MMA's B
@@ -73,7 +78,8 @@ struct ScTcSmem {
     // move monotonically along a ray, so the others contribute zero weight)
     unsigned short rlo[kWarps][kTab], rhi[kWarps][kTab];
     int wsum[kWarps];
-    unsigned long long bar;
+    unsigned long long bar;      // MMA batch done
+    unsigned long long rbar[2];  // record buffer landed
     uint32_t tslot;
 };
 
@@ -154,19 +160,16 @@ void launch_adj_records(AdjRec *recs, const GeoDev &gd, const UsGeo &g, cudaStre
 __global__ void __launch_bounds__(kThr, 2)
     k_scatter_tc(const float2 *__restrict__ rowsc, float2 *__restrict__ spec, const AdjRec *__restrict__ recs,
                  const int4 *__restrict__ items, const float2 *__restrict__ kmat, const float2 *__restrict__ shifta,
-                 UsGeo g, int zb, int jbase, int *__restrict__ err) {
+                 UsGeo g, int zb, int nunits, int jbase, int *__restrict__ err) {
     extern __shared__ __align__(1024) unsigned char sc_smem_raw[];
     ScTcSmem &sm = *reinterpret_cast<ScTcSmem *>(sc_smem_raw);
-    // slices fastest: consecutive blocks share the item's records in L2
-    const int z = (int)(blockIdx.x % (unsigned)zb);
-    const int4 it = items[blockIdx.x / (unsigned)zb];
-    const int tyi = it.x / g.NT, txi = it.x - tyi * g.NT;
     const int P = g.P, hn = g.n / 2 + 1;
     const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
-    const float2 *rz = rowsc + (long long)z * g.ntheta * hn;
     if (wid == 0) tc::alloc(&sm.tslot, kTmemCols);
     if (tid == 0) {
         tc::mbar_init(&sm.bar, 1);
+        tc::mbar_init(&sm.rbar[0], 1);
+        tc::mbar_init(&sm.rbar[1], 1);
         tc::fence_mbar_init();
     }
     tc::fence_before();
@@ -176,198 +179,227 @@ __global__ void __launch_bounds__(kThr, 2)
     const int mt = wid >> 2, q = wid & 3;    // this thread's cell tid = mt*128 + 32q + lane
     const int cx = tid % kT, cy = tid / kT;  // its column and row (warp w: rows 2w, 2w+1)
     bool ok = true;
-    int nmma = 0;   // MMA batches issued
-    float acc[32];  // F of this cell: 16 time samples x (re, im)
-#pragma unroll
-    for (int i = 0; i < 32; ++i) acc[i] = 0.f;
+    int nmma = 0;  // MMA batches issued by this block (phase of sm.bar)
+    int seq = 0;   // tables consumed: buffer seq & 1, its fill (seq >> 1) & 1
+    // Thread 0's copy cursor: the next table (unit, first entry) to fetch, in
+    // the order the tables are consumed; a table is fetched while the one
+    // before it is processed.
+    int fu = blockIdx.x, fc0 = 0;
+    auto fetch = [&](int slot) {
+        if (fu >= nunits) return;
+        const int4 fit = __ldg(items + fu / zb);
+        const uint32_t bytes = (uint32_t)min(kTab, fit.z - fc0) * (uint32_t)sizeof(AdjRec);
+        tc::bulk_g2s(sm.rec[slot], recs + (long long)fit.y + fc0, bytes, &sm.rbar[slot]);
+        fc0 += kTab;
+        if (fc0 >= fit.z) {
+            fc0 = 0;
+            fu += gridDim.x;
+        }
+    };
+    if (tid == 0) fetch(0);
 
-    for (int c0 = 0; c0 < it.z; c0 += kTab) {
-        const int cnt = min(kTab, it.z - c0);
-        __syncthreads();  // previous table consumed
-        {  // records of the table, 16-byte copies
-            const uint4 *src = reinterpret_cast<const uint4 *>(recs + (long long)it.y + c0);
-            uint4 *dst = reinterpret_cast<uint4 *>(sm.rec);
-            constexpr int kVec = sizeof(AdjRec) / 16;
-            for (int i = tid; i < cnt * kVec; i += kThr) dst[i] = __ldg(src + i);
-        }
-        __syncthreads();
-        // ---- E = (-1)^(k+1) shiftadj(k) FFT(row)(k) (pi/mu)/n, then T_p(cy) = E(p) wy_p(cy) ----
-        for (int e = tid; e < cnt; e += kThr) {
-            const int th = (unsigned)sm.rec[e].thm >> 16, k = sm.rec[e].k;
-            float2 R = (k <= g.n / 2) ? __ldg(rz + (long long)th * hn + k) : __ldg(rz + (long long)th * hn + (g.n - k));
-            if (k > g.n / 2) R.y = -R.y;
-            sm.e[e] = cmul(R, sm.rec[e].sf);
-        }
-        __syncthreads();
-        for (int i = tid; i < cnt * kT; i += kThr) {
-            const int e = i >> 4, row = i & 15;
-            const float2 E = sm.e[e];
-            const float w = sm.rec[e].wy[row];
-            sm.t[e][row] = make_float2(E.x * w, E.y * w);
-        }
-        // ---- first table row of each ray: block-wide scan of ray starts ----
-        int flag = 0;
-        if (tid < cnt) flag = (tid == 0 || (sm.rec[tid].thm >> 16) != (sm.rec[tid - 1].thm >> 16)) ? 1 : 0;
-        int incl = flag;
+    // persistent: units (tile item, slice) round-robin, slices fastest, so the
+    // blocks in flight share their items' records in L2; all units hold samples
+    for (int u = blockIdx.x; u < nunits; u += gridDim.x) {
+        const int z = u % zb;
+        const int4 it = __ldg(items + u / zb);
+        const int tyi = it.x / g.NT, txi = it.x - tyi * g.NT;
+        const float2 *rz = rowsc + (long long)z * g.ntheta * hn;
+        int nbu = 0;    // MMA batches of this unit
+        float acc[32];  // F of this cell: 16 time samples x (re, im)
 #pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {
-            const int y = __shfl_up_sync(0xffffffffu, incl, o);
-            if (lane >= o) incl += y;
-        }
-        if (lane == 31) sm.wsum[wid] = incl;
-        __syncthreads();
-        int base = 0, nseg = 0;
-#pragma unroll
-        for (int w = 0; w < kWarps; ++w) {
-            const int v = sm.wsum[w];
-            base += (w < wid) ? v : 0;
-            nseg += v;
-        }
-        incl += base;
-        if (tid < cnt && flag) sm.seg_first[incl - 1] = tid;
-        if (tid == 0) sm.seg_first[nseg] = cnt;
-        __syncthreads();  // ray starts and T written
-        for (int r = tid; r < nseg; r += kThr) {
-            const int e0 = sm.seg_first[r], e1 = sm.seg_first[r + 1];
-            int lo[kWarps], hi[kWarps];
-#pragma unroll
-            for (int w = 0; w < kWarps; ++w) {
-                lo[w] = e1;
-                hi[w] = e0;
-            }
-            for (int e = e0; e < e1; ++e) {
-                const int msk = sm.rec[e].thm & 0xffff;
-#pragma unroll
-                for (int w = 0; w < kWarps; ++w)
-                    if (msk & (3 << (2 * w))) {
-                        lo[w] = min(lo[w], e);
-                        hi[w] = e + 1;
-                    }
-            }
-#pragma unroll
-            for (int w = 0; w < kWarps; ++w) {
-                sm.rlo[w][r] = (unsigned short)lo[w];
-                sm.rhi[w][r] = (unsigned short)max(lo[w], hi[w]);
-            }
-        }
-        __syncthreads();
+        for (int i = 0; i < 32; ++i) acc[i] = 0.f;
 
-        for (int sb = 0; sb < nseg; sb += kBatch) {
-            const int nb = min(kBatch, nseg - sb);
-            // ---- 1. V(c, ray) of this cell for the batch's rays ----
-            float vv[2 * kBatch];
-#pragma unroll
-            for (int r = 0; r < kBatch; ++r) {
-                float2 v = make_float2(0.f, 0.f);
-                if (r < nb) {  // T and wx vanish outside the stencil: no tests in the loop
-                    const int e1 = sm.rhi[wid][sb + r];
-#pragma unroll 4
-                    for (int e = sm.rlo[wid][sb + r]; e < e1; ++e) {
-                        const float w = sm.rec[e].wx[cx];
-                        v = ffma2(make_float2(w, w), sm.t[e][cy], v);
-                    }
-                }
-                vv[2 * r] = v.x;
-                vv[2 * r + 1] = v.y;
+        for (int c0 = 0; c0 < it.z; c0 += kTab) {
+            const int cnt = min(kTab, it.z - c0);
+            const int buf = seq & 1;
+            __syncthreads();  // previous table consumed: its buffer takes the next one
+            if (tid == 0) {
+                tc::fence_proxy_async();
+                fetch(buf ^ 1);
             }
-            // ---- previous batch's MMAs done: add its product to the cell's
-            // FP32 sums; A, B and the accumulator are then free ----
-            if (nmma > 0) {
-                ok = tc::mbar_wait(&sm.bar, (uint32_t)((nmma - 1) & 1)) && ok;
-                tc::fence_after();
-                float v[32], w2[32];
-                tc::ld32(tbase + ((uint32_t)(32 * q) << 16) + kColD + mt * kNP, v);
-                tc::ld32(tbase + ((uint32_t)(32 * q) << 16) + kColD + mt * kNP + kN, w2);
-#pragma unroll
-                for (int i = 0; i < 32; ++i) acc[i] += v[i] + w2[i];
+            ok = tc::mbar_wait(&sm.rbar[buf], (uint32_t)((seq >> 1) & 1)) && ok;
+            ++seq;
+            const AdjRec *rec = sm.rec[buf];
+            // ---- E = (-1)^(k+1) shiftadj(k) FFT(row)(k) (pi/mu)/n, then T_p(cy) = E(p) wy_p(cy) ----
+            for (int e = tid; e < cnt; e += kThr) {
+                const int th = (unsigned)rec[e].thm >> 16, k = rec[e].k;
+                float2 R = (k <= g.n / 2) ? __ldg(rz + (long long)th * hn + k) : __ldg(rz + (long long)th * hn + (g.n - k));
+                if (k > g.n / 2) R.y = -R.y;
+                sm.e[e] = cmul(R, rec[e].sf);
             }
-            // ---- B = conj K' rows of this batch: row 2j+o, K index 2r+s (threads = (row, 4 K values)) ----
-            {
-                const int nrow = tid >> 3, q4 = tid & 7;
-                const int j = nrow >> 1, o = nrow & 1;
-                float bv[4];
-#pragma unroll
-                for (int i = 0; i < 2; ++i) {
-                    const int r = 2 * q4 + i;
-                    float2 kv = make_float2(0.f, 0.f);
-                    if (r < nb && jbase + j < g.m)
-                        kv = __ldg(kmat + (long long)((unsigned)sm.rec[sm.seg_first[sb + r]].thm >> 16) * g.m + jbase + j);
-                    bv[2 * i] = o == 0 ? kv.x : -kv.y;
-                    bv[2 * i + 1] = o == 0 ? kv.y : kv.x;
-                }
-                const int o32 = off32(nrow, 4 * q4);
-                *reinterpret_cast<float4 *>(sm.bhi + o32) = make_float4(bv[0], bv[1], bv[2], bv[3]);
-                *reinterpret_cast<float4 *>(sm.blo + o32) =
-                    make_float4(bv[0] - tc::trunc_tf32(bv[0]), bv[1] - tc::trunc_tf32(bv[1]),
-                                bv[2] - tc::trunc_tf32(bv[2]), bv[3] - tc::trunc_tf32(bv[3]));
-            }
-            // ---- 2. A = V of this cell, hi and lo parts, into tensor memory ----
-            {
-                float lo[32];
-#pragma unroll
-                for (int i = 0; i < 32; ++i) lo[i] = vv[i] - tc::trunc_tf32(vv[i]);
-                const uint32_t ta0 = tbase + ((uint32_t)(32 * q) << 16);
-                st32(ta0 + kColAhi + mt * kK, vv);
-                st32(ta0 + kColAlo + mt * kK, lo);
-                asm volatile("tcgen05.wait::st.sync.aligned;\n" ::: "memory");
-            }
-            tc::fence_proxy_async();
-            tc::fence_before();
             __syncthreads();
-            if (tid == 32 * (nmma % kWarps)) {  // the issuing warp rotates
-                tc::fence_after();
-                // D = [Ahi Bhi, Ahi Blo] + [Alo Bhi, Alo Blo]: both halves summed when read
-                constexpr uint32_t IT = tc::idesc(tc::kFmtTF32, 128, kNP);
-                const uint64_t db = tc::sdesc(tc::smem_addr(sm.bhi), 128, 1024);
-#pragma unroll
-                for (int m2 = 0; m2 < kMT; ++m2) {
-                    const uint32_t d = tbase + kColD + m2 * kNP;
-#pragma unroll
-                    for (int s2 = 0; s2 < kK / 8; ++s2) {
-                        const uint32_t ah = tbase + kColAhi + m2 * kK + s2 * 8;
-                        const uint32_t al = tbase + kColAlo + m2 * kK + s2 * 8;
-                        mma_tf32_ts(d, ah, db + (uint64_t)(16 * s2), IT, s2 > 0 ? 1u : 0u);
-                        mma_tf32_ts(d, al, db + (uint64_t)(16 * s2), IT, 1u);
-                    }
-                }
-                tc::commit(&sm.bar);
+            for (int i = tid; i < cnt * kT; i += kThr) {
+                const int e = i >> 4, row = i & 15;
+                const float2 E = sm.e[e];
+                const float w = rec[e].wy[row];
+                sm.t[e][row] = make_float2(E.x * w, E.y * w);
             }
-            ++nmma;
-        }
-    }
-    // ---- store the cell's time samples (pre-IFFT fftshift sign); split tiles add ----
-    if (nmma > 0) {
-        ok = tc::mbar_wait(&sm.bar, (uint32_t)((nmma - 1) & 1)) && ok;
-        tc::fence_after();
-        float v[32], w2[32];
-        tc::ld32(tbase + ((uint32_t)(32 * q) << 16) + kColD + mt * kNP, v);
-        tc::ld32(tbase + ((uint32_t)(32 * q) << 16) + kColD + mt * kNP + kN, w2);
+            // ---- first table row of each ray: block-wide scan of ray starts ----
+            int flag = 0;
+            if (tid < cnt) flag = (tid == 0 || (rec[tid].thm >> 16) != (rec[tid - 1].thm >> 16)) ? 1 : 0;
+            int incl = flag;
 #pragma unroll
-        for (int i = 0; i < 32; ++i) acc[i] += v[i] + w2[i];
-    }
-    // ---- the adjoint only needs Re IFFT2(X) = C2R of the Hermitian part
-    // H(k) = (X(k) + conj X(-k)) / 2 on the half plane kx <= n: each cell adds
-    // X(k)/2 to H(k) and conj(X(k))/2 to H(-k) where they lie in the half plane
-    // (at most two adds per H cell from two blocks, onto zeros: the sum does not
-    // depend on their order); the pre-IFFT fftshift sign is applied here ----
-    const int KY = tyi * kT + cy, KX = txi * kT + cx;
-    if (KY < P && KX < P) {
-        const int half = P / 2, hp = half + 1;
-        const long long img_half = (long long)P * hp;
-        const float sg = ((KX + KY) & 1) ? -0.5f : 0.5f;
-        const bool here = KX <= half, mirror = KX >= half || KX == 0;
-        const long long o1 = (long long)KY * hp + KX;
-        const long long o2 = (long long)((P - KY) % P) * hp + (P - KX) % P;
-        float2 *dst = spec + ((long long)z * g.m + jbase) * img_half;
+            for (int o = 1; o < 32; o <<= 1) {
+                const int y = __shfl_up_sync(0xffffffffu, incl, o);
+                if (lane >= o) incl += y;
+            }
+            if (lane == 31) sm.wsum[wid] = incl;
+            __syncthreads();
+            int base = 0, nseg = 0;
 #pragma unroll
-        for (int j = 0; j < 16; ++j) {
-            if (jbase + j >= g.m) break;
-            const float2 v = make_float2(sg * acc[2 * j], sg * acc[2 * j + 1]);
-            float2 *d = dst + (long long)j * img_half;
-            if (here) atomicAdd(d + o1, v);
-            if (mirror) atomicAdd(d + o2, make_float2(v.x, -v.y));
+            for (int w = 0; w < kWarps; ++w) {
+                const int v = sm.wsum[w];
+                base += (w < wid) ? v : 0;
+                nseg += v;
+            }
+            incl += base;
+            if (tid < cnt && flag) sm.seg_first[incl - 1] = tid;
+            if (tid == 0) sm.seg_first[nseg] = cnt;
+            __syncthreads();  // ray starts and T written
+            for (int r = tid; r < nseg; r += kThr) {
+                const int e0 = sm.seg_first[r], e1 = sm.seg_first[r + 1];
+                int lo[kWarps], hi[kWarps];
+#pragma unroll
+                for (int w = 0; w < kWarps; ++w) {
+                    lo[w] = e1;
+                    hi[w] = e0;
+                }
+                for (int e = e0; e < e1; ++e) {
+                    const int msk = rec[e].thm & 0xffff;
+#pragma unroll
+                    for (int w = 0; w < kWarps; ++w)
+                        if (msk & (3 << (2 * w))) {
+                            lo[w] = min(lo[w], e);
+                            hi[w] = e + 1;
+                        }
+                }
+#pragma unroll
+                for (int w = 0; w < kWarps; ++w) {
+                    sm.rlo[w][r] = (unsigned short)lo[w];
+                    sm.rhi[w][r] = (unsigned short)max(lo[w], hi[w]);
+                }
+            }
+            __syncthreads();
+
+            for (int sb = 0; sb < nseg; sb += kBatch) {
+                const int nb = min(kBatch, nseg - sb);
+                // ---- 1. V(c, ray) of this cell for the batch's rays ----
+                float vv[2 * kBatch];
+#pragma unroll
+                for (int r = 0; r < kBatch; ++r) {
+                    float2 v = make_float2(0.f, 0.f);
+                    if (r < nb) {  // T and wx vanish outside the stencil: no tests in the loop
+                        const int e1 = sm.rhi[wid][sb + r];
+#pragma unroll 4
+                        for (int e = sm.rlo[wid][sb + r]; e < e1; ++e) {
+                            const float w = rec[e].wx[cx];
+                            v = ffma2(make_float2(w, w), sm.t[e][cy], v);
+                        }
+                    }
+                    vv[2 * r] = v.x;
+                    vv[2 * r + 1] = v.y;
+                }
+                // ---- previous batch's MMAs done: add its product to the cell's
+                // FP32 sums; A, B and the accumulator are then free ----
+                if (nbu > 0) {
+                    ok = tc::mbar_wait(&sm.bar, (uint32_t)((nmma - 1) & 1)) && ok;
+                    tc::fence_after();
+                    float v[32], w2[32];
+                    tc::ld32(tbase + ((uint32_t)(32 * q) << 16) + kColD + mt * kNP, v);
+                    tc::ld32(tbase + ((uint32_t)(32 * q) << 16) + kColD + mt * kNP + kN, w2);
+#pragma unroll
+                    for (int i = 0; i < 32; ++i) acc[i] += v[i] + w2[i];
+                }
+                // ---- B = conj K' rows of this batch: row 2j+o, K index 2r+s (threads = (row, 4 K values)) ----
+                {
+                    const int nrow = tid >> 3, q4 = tid & 7;
+                    const int j = nrow >> 1, o = nrow & 1;
+                    float bv[4];
+#pragma unroll
+                    for (int i = 0; i < 2; ++i) {
+                        const int r = 2 * q4 + i;
+                        float2 kv = make_float2(0.f, 0.f);
+                        if (r < nb && jbase + j < g.m)
+                            kv = __ldg(kmat + (long long)((unsigned)rec[sm.seg_first[sb + r]].thm >> 16) * g.m + jbase + j);
+                        bv[2 * i] = o == 0 ? kv.x : -kv.y;
+                        bv[2 * i + 1] = o == 0 ? kv.y : kv.x;
+                    }
+                    const int o32 = off32(nrow, 4 * q4);
+                    *reinterpret_cast<float4 *>(sm.bhi + o32) = make_float4(bv[0], bv[1], bv[2], bv[3]);
+                    *reinterpret_cast<float4 *>(sm.blo + o32) =
+                        make_float4(bv[0] - tc::trunc_tf32(bv[0]), bv[1] - tc::trunc_tf32(bv[1]),
+                                    bv[2] - tc::trunc_tf32(bv[2]), bv[3] - tc::trunc_tf32(bv[3]));
+                }
+                // ---- 2. A = V of this cell, hi and lo parts, into tensor memory ----
+                {
+                    float lo[32];
+#pragma unroll
+                    for (int i = 0; i < 32; ++i) lo[i] = vv[i] - tc::trunc_tf32(vv[i]);
+                    const uint32_t ta0 = tbase + ((uint32_t)(32 * q) << 16);
+                    st32(ta0 + kColAhi + mt * kK, vv);
+                    st32(ta0 + kColAlo + mt * kK, lo);
+                    asm volatile("tcgen05.wait::st.sync.aligned;\n" ::: "memory");
+                }
+                tc::fence_proxy_async();
+                tc::fence_before();
+                __syncthreads();
+                if (tid == 32 * (nmma % kWarps)) {  // the issuing warp rotates
+                    tc::fence_after();
+                    // D = [Ahi Bhi, Ahi Blo] + [Alo Bhi, Alo Blo]: both halves summed when read
+                    constexpr uint32_t IT = tc::idesc(tc::kFmtTF32, 128, kNP);
+                    const uint64_t db = tc::sdesc(tc::smem_addr(sm.bhi), 128, 1024);
+#pragma unroll
+                    for (int m2 = 0; m2 < kMT; ++m2) {
+                        const uint32_t d = tbase + kColD + m2 * kNP;
+#pragma unroll
+                        for (int s2 = 0; s2 < kK / 8; ++s2) {
+                            const uint32_t ah = tbase + kColAhi + m2 * kK + s2 * 8;
+                            const uint32_t al = tbase + kColAlo + m2 * kK + s2 * 8;
+                            mma_tf32_ts(d, ah, db + (uint64_t)(16 * s2), IT, s2 > 0 ? 1u : 0u);
+                            mma_tf32_ts(d, al, db + (uint64_t)(16 * s2), IT, 1u);
+                        }
+                    }
+                    tc::commit(&sm.bar);
+                }
+                ++nmma;
+                ++nbu;
+            }
         }
-    }
+        // ---- the unit's last product ----
+        if (nbu > 0) {
+            ok = tc::mbar_wait(&sm.bar, (uint32_t)((nmma - 1) & 1)) && ok;
+            tc::fence_after();
+            float v[32], w2[32];
+            tc::ld32(tbase + ((uint32_t)(32 * q) << 16) + kColD + mt * kNP, v);
+            tc::ld32(tbase + ((uint32_t)(32 * q) << 16) + kColD + mt * kNP + kN, w2);
+#pragma unroll
+            for (int i = 0; i < 32; ++i) acc[i] += v[i] + w2[i];
+        }
+        // ---- the adjoint only needs Re IFFT2(X) = C2R of the Hermitian part
+        // H(k) = (X(k) + conj X(-k)) / 2 on the half plane kx <= n: each cell adds
+        // X(k)/2 to H(k) and conj(X(k))/2 to H(-k) where they lie in the half plane
+        // (at most two adds per H cell from two blocks, onto zeros: the sum does not
+        // depend on their order); the pre-IFFT fftshift sign is applied here ----
+        const int KY = tyi * kT + cy, KX = txi * kT + cx;
+        if (KY < P && KX < P) {
+            const int half = P / 2, hp = half + 1;
+            const long long img_half = (long long)P * hp;
+            const float sg = ((KX + KY) & 1) ? -0.5f : 0.5f;
+            const bool here = KX <= half, mirror = KX >= half || KX == 0;
+            const long long o1 = (long long)KY * hp + KX;
+            const long long o2 = (long long)((P - KY) % P) * hp + (P - KX) % P;
+            float2 *dst = spec + ((long long)z * g.m + jbase) * img_half;
+#pragma unroll
+            for (int j = 0; j < 16; ++j) {
+                if (jbase + j >= g.m) break;
+                const float2 v = make_float2(sg * acc[2 * j], sg * acc[2 * j + 1]);
+                float2 *d = dst + (long long)j * img_half;
+                if (here) atomicAdd(d + o1, v);
+                if (mirror) atomicAdd(d + o2, make_float2(v.x, -v.y));
+            }
+        }
+    }  // units
     tc::fence_before();
     __syncthreads();
     if (wid == 0) tc::dealloc(tbase, kTmemCols);
@@ -387,10 +419,20 @@ void launch_scatter_tc(const float2 *rowsc, float2 *spec, int zb, const GeoDev &
                        cudaStream_t s) {
     if (g.T != kT) throw Error(1, "tile size must be 16");
     if (!gd.adj_recs) throw Error(1, "adjoint geometry records missing");
-    const long long nblk = (long long)zb * gd.n_adj_items;
-    if (nblk > 2147483647LL) throw Error(1, "adjoint grid too large");
-    k_scatter_tc<<<(unsigned)nblk, kThr, kScSmemBytes, s>>>(rowsc, spec, gd.adj_recs, gd.adj_items, gd.kmat,
-                                                           gd.shiftadj, g, zb, jbase, gd.err);
+    // items with samples (sorted by count, so the empty tiles, whose half
+    // planes stay zero, come last)
+    const long long nunits = (long long)zb * gd.n_adj_busy;
+    if (nunits == 0) return;
+    if (nunits > 2147483647LL) throw Error(1, "adjoint grid too large");
+    static int nsm = 0;
+    if (nsm == 0) {
+        int dev = 0;
+        CUDA_CHECK(cudaGetDevice(&dev));
+        CUDA_CHECK(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+    }
+    const int grid = (int)std::min<long long>(nunits, 2LL * nsm);
+    k_scatter_tc<<<grid, kThr, kScSmemBytes, s>>>(rowsc, spec, gd.adj_recs, gd.adj_items, gd.kmat, gd.shiftadj, g,
+                                                  zb, (int)nunits, jbase, gd.err);
     LAUNCH_CHECK("k_scatter_tc");
 }
 

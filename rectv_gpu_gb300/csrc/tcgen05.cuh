@@ -71,6 +71,19 @@ __device__ __forceinline__ void fence_mbar_init() {
     asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
 }
 
+// One-thread 1D bulk copy (TMA engine) of `bytes` (a multiple of 16, both
+// addresses 16-byte aligned) from global to shared memory; completion is
+// counted on the mbarrier as transaction bytes (one arrival per copy).
+__device__ __forceinline__ void bulk_g2s(void *dst, const void *src, uint32_t bytes, void *bar) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(smem_addr(bar)), "r"(bytes)
+                 : "memory");
+    asm volatile(
+        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];\n" ::"r"(
+            smem_addr(dst)),
+        "l"(src), "r"(bytes), "r"(smem_addr(bar))
+        : "memory");
+}
+
 // Wait for phase `parity` of the mbarrier; false after about one second.
 __device__ __forceinline__ bool mbar_wait(void *bar, uint32_t parity) {
     const uint32_t a = smem_addr(bar);
