@@ -74,9 +74,9 @@ struct ScTcSmem {
     float blo[kN * kK];           // B - trunc(B): rows 32..63 (contiguous with bhi)
     int seg_first[kTab + 1];
     // per warp and ray: the table rows [lo, hi) from the first to the last
-    // sample whose stencil covers one of the warp's two tile rows (samples
-    // move monotonically along a ray, so the others contribute zero weight)
-    unsigned short rlo[kWarps][kTab], rhi[kWarps][kTab];
+    // sample whose stencil covers one of the warp's two tile rows (the others
+    // in between contribute zero weight); empty: lo = kTab, hi = 0
+    int rlo[kWarps][kTab], rhi[kWarps][kTab];
     int wsum[kWarps];
     unsigned long long bar;      // MMA batch done
     unsigned long long rbar[2];  // record buffer landed
@@ -254,36 +254,49 @@ __global__ void __launch_bounds__(kThr, 2)
                 nseg += v;
             }
             incl += base;
-            if (tid < cnt && flag) sm.seg_first[incl - 1] = tid;
+            const int seg = incl - 1;  // ray (segment) of this thread's sample
+            if (tid < cnt && flag) {
+                sm.seg_first[seg] = tid;
+#pragma unroll
+                for (int w = 0; w < kWarps; ++w) {
+                    sm.rlo[w][seg] = kTab;
+                    sm.rhi[w][seg] = 0;
+                }
+            }
             if (tid == 0) sm.seg_first[nseg] = cnt;
-            __syncthreads();  // ray starts and T written
-            for (int r = tid; r < nseg; r += kThr) {
-                const int e0 = sm.seg_first[r], e1 = sm.seg_first[r + 1];
-                int lo[kWarps], hi[kWarps];
+            __syncthreads();  // ray starts, empty ranges and T written
+            // ---- per warp and ray: first and last sample covering the warp's
+            // rows, from the samples where a covered run starts or ends ----
+            if (tid < cnt) {
+                const int msk = rec[tid].thm & 0xffff;
+                const int mprev = flag ? 0 : (rec[tid - 1].thm & 0xffff);
+                const bool last = tid + 1 == cnt || (rec[tid + 1].thm >> 16) != (rec[tid].thm >> 16);
+                const int mnext = last ? 0 : (rec[tid + 1].thm & 0xffff);
 #pragma unroll
                 for (int w = 0; w < kWarps; ++w) {
-                    lo[w] = e1;
-                    hi[w] = e0;
-                }
-                for (int e = e0; e < e1; ++e) {
-                    const int msk = rec[e].thm & 0xffff;
-#pragma unroll
-                    for (int w = 0; w < kWarps; ++w)
-                        if (msk & (3 << (2 * w))) {
-                            lo[w] = min(lo[w], e);
-                            hi[w] = e + 1;
-                        }
-                }
-#pragma unroll
-                for (int w = 0; w < kWarps; ++w) {
-                    sm.rlo[w][r] = (unsigned short)lo[w];
-                    sm.rhi[w][r] = (unsigned short)max(lo[w], hi[w]);
+                    const int bits = 3 << (2 * w);
+                    if (msk & bits) {
+                        if (!(mprev & bits)) atomicMin(&sm.rlo[w][seg], tid);
+                        if (!(mnext & bits)) atomicMax(&sm.rhi[w][seg], tid + 1);
+                    }
                 }
             }
             __syncthreads();
 
             for (int sb = 0; sb < nseg; sb += kBatch) {
                 const int nb = min(kBatch, nseg - sb);
+                // K'(ray, j) of this thread's two B entries, loaded before the ray
+                // sums so that the L2 latency is not in front of the batch barrier
+                const int brow = tid >> 3, bq4 = tid & 7;  // B row 2j+o, K values 4 bq4 .. 4 bq4 + 3
+                const int bj = brow >> 1;
+                float2 kv[2];
+#pragma unroll
+                for (int i = 0; i < 2; ++i) {
+                    const int r = 2 * bq4 + i;
+                    kv[i] = make_float2(0.f, 0.f);
+                    if (r < nb && jbase + bj < g.m)
+                        kv[i] = __ldg(kmat + (long long)((unsigned)rec[sm.seg_first[sb + r]].thm >> 16) * g.m + jbase + bj);
+                }
                 // ---- 1. V(c, ray) of this cell for the batch's rays ----
                 float vv[2 * kBatch];
 #pragma unroll
@@ -313,19 +326,14 @@ __global__ void __launch_bounds__(kThr, 2)
                 }
                 // ---- B = conj K' rows of this batch: row 2j+o, K index 2r+s (threads = (row, 4 K values)) ----
                 {
-                    const int nrow = tid >> 3, q4 = tid & 7;
-                    const int j = nrow >> 1, o = nrow & 1;
+                    const int o = brow & 1;
                     float bv[4];
 #pragma unroll
                     for (int i = 0; i < 2; ++i) {
-                        const int r = 2 * q4 + i;
-                        float2 kv = make_float2(0.f, 0.f);
-                        if (r < nb && jbase + j < g.m)
-                            kv = __ldg(kmat + (long long)((unsigned)rec[sm.seg_first[sb + r]].thm >> 16) * g.m + jbase + j);
-                        bv[2 * i] = o == 0 ? kv.x : -kv.y;
-                        bv[2 * i + 1] = o == 0 ? kv.y : kv.x;
+                        bv[2 * i] = o == 0 ? kv[i].x : -kv[i].y;
+                        bv[2 * i + 1] = o == 0 ? kv[i].y : kv[i].x;
                     }
-                    const int o32 = off32(nrow, 4 * q4);
+                    const int o32 = off32(brow, 4 * bq4);
                     *reinterpret_cast<float4 *>(sm.bhi + o32) = make_float4(bv[0], bv[1], bv[2], bv[3]);
                     *reinterpret_cast<float4 *>(sm.blo + o32) =
                         make_float4(bv[0] - tc::trunc_tf32(bv[0]), bv[1] - tc::trunc_tf32(bv[1]),
