@@ -61,6 +61,7 @@ constexpr uint32_t kTmemCols = 256;
 constexpr uint32_t kColAhi = 0;             // [mt*32, +32)
 constexpr uint32_t kColAlo = kMT * kK;      // 64
 constexpr uint32_t kColD = 2 * kMT * kK;    // 128: product of the batch [mt*64, +64)
+static_assert(kTab <= kThr, "one table entry per thread");
 
 __device__ __forceinline__ int off32(int row, int kk) {
     return (row >> 3) * 256 + (kk >> 2) * 32 + (row & 7) * 4 + (kk & 3);
@@ -70,6 +71,7 @@ struct ScTcSmem {
     AdjRec rec[2][kTab];          // geometry records of this table and the next (bulk copies)
     float2 t[kTab][kT];           // T_p(cy) = E(p) wy_p(cy)
     float2 e[kTab];               // E(p) of this slice
+    float2 rnext[kTab];           // row spectrum values of the next table's samples (cp.async)
     float bhi[kN * kK];           // B = conj K' of the batch's rays, FP32: rows 0..31 of the MMA's B
     float blo[kN * kK];           // B - trunc(B): rows 32..63 (contiguous with bhi)
     int seg_first[kTab + 1];
@@ -197,6 +199,7 @@ __global__ void __launch_bounds__(kThr, 2)
         }
     };
     if (tid == 0) fetch(0);
+    bool have_next = false;  // rnext holds the current table's row spectrum values
 
     // persistent: units (tile item, slice) round-robin, slices fastest, so the
     // blocks in flight share their items' records in L2; all units hold samples
@@ -222,11 +225,12 @@ __global__ void __launch_bounds__(kThr, 2)
             ++seq;
             const AdjRec *rec = sm.rec[buf];
             // ---- E = (-1)^(k+1) shiftadj(k) FFT(row)(k) (pi/mu)/n, then T_p(cy) = E(p) wy_p(cy) ----
-            for (int e = tid; e < cnt; e += kThr) {
-                const int th = (unsigned)rec[e].thm >> 16, k = rec[e].k;
-                float2 R = (k <= g.n / 2) ? __ldg(rz + (long long)th * hn + k) : __ldg(rz + (long long)th * hn + (g.n - k));
+            if (have_next) asm volatile("cp.async.wait_all;\n" ::: "memory");  // this thread's own entry
+            if (tid < cnt) {
+                const int th = (unsigned)rec[tid].thm >> 16, k = rec[tid].k;
+                float2 R = have_next ? sm.rnext[tid] : __ldg(rz + (long long)th * hn + (k <= g.n / 2 ? k : g.n - k));
                 if (k > g.n / 2) R.y = -R.y;
-                sm.e[e] = cmul(R, rec[e].sf);
+                sm.e[tid] = cmul(R, rec[tid].sf);
             }
             __syncthreads();
             for (int i = tid; i < cnt * kT; i += kThr) {
@@ -278,6 +282,30 @@ __global__ void __launch_bounds__(kThr, 2)
                     if (msk & bits) {
                         if (!(mprev & bits)) atomicMin(&sm.rlo[w][seg], tid);
                         if (!(mnext & bits)) atomicMax(&sm.rhi[w][seg], tid + 1);
+                    }
+                }
+            }
+            // ---- the next table's row spectrum values, copied while this
+            // table's batches run (its records were fetched at this table's start) ----
+            {
+                int nc0 = c0 + kTab, nu = u;
+                if (nc0 >= it.z) {
+                    nc0 = 0;
+                    nu = u + gridDim.x;
+                }
+                have_next = nu < nunits;
+                if (have_next) {
+                    const int4 nit = nu == u ? it : __ldg(items + nu / zb);
+                    const float2 *nrz = rowsc + (long long)(nu % zb) * g.ntheta * hn;
+                    ok = tc::mbar_wait(&sm.rbar[buf ^ 1], (uint32_t)((seq >> 1) & 1)) && ok;
+                    if (tid < min(kTab, nit.z - nc0)) {
+                        const AdjRec &nr = sm.rec[buf ^ 1][tid];
+                        const int th = (unsigned)nr.thm >> 16, k = nr.k;
+                        const float2 *src = nrz + (long long)th * hn + (k <= g.n / 2 ? k : g.n - k);
+                        asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(tc::smem_addr(&sm.rnext[tid])),
+                                     "l"(src)
+                                     : "memory");
+                        asm volatile("cp.async.commit_group;\n" ::: "memory");
                     }
                 }
             }
