@@ -169,7 +169,7 @@ __global__ void __launch_bounds__(kThr, 2)
     const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
     if (wid == 0) tc::alloc(&sm.tslot, kTmemCols);
     if (tid == 0) {
-        tc::mbar_init(&sm.bar, 1);
+        tc::mbar_init(&sm.bar, kMT);  // one commit per M tile
         tc::mbar_init(&sm.rbar[0], 1);
         tc::mbar_init(&sm.rbar[1], 1);
         tc::fence_mbar_init();
@@ -380,21 +380,22 @@ __global__ void __launch_bounds__(kThr, 2)
                 tc::fence_proxy_async();
                 tc::fence_before();
                 __syncthreads();
-                if (tid == 32 * (nmma % kWarps)) {  // the issuing warp rotates
+                // one issuing thread per M tile (its own accumulator chain), in
+                // two warps that rotate, so that no warp carries all 16 issues
+                const int iw = (2 * nmma) % kWarps;
+                if (lane == 0 && (wid == iw || wid == iw + 1)) {
                     tc::fence_after();
                     // D = [Ahi Bhi, Ahi Blo] + [Alo Bhi, Alo Blo]: both halves summed when read
                     constexpr uint32_t IT = tc::idesc(tc::kFmtTF32, 128, kNP);
                     const uint64_t db = tc::sdesc(tc::smem_addr(sm.bhi), 128, 1024);
+                    const int m2 = wid - iw;
+                    const uint32_t d = tbase + kColD + m2 * kNP;
 #pragma unroll
-                    for (int m2 = 0; m2 < kMT; ++m2) {
-                        const uint32_t d = tbase + kColD + m2 * kNP;
-#pragma unroll
-                        for (int s2 = 0; s2 < kK / 8; ++s2) {
-                            const uint32_t ah = tbase + kColAhi + m2 * kK + s2 * 8;
-                            const uint32_t al = tbase + kColAlo + m2 * kK + s2 * 8;
-                            mma_tf32_ts(d, ah, db + (uint64_t)(16 * s2), IT, s2 > 0 ? 1u : 0u);
-                            mma_tf32_ts(d, al, db + (uint64_t)(16 * s2), IT, 1u);
-                        }
+                    for (int s2 = 0; s2 < kK / 8; ++s2) {
+                        const uint32_t ah = tbase + kColAhi + m2 * kK + s2 * 8;
+                        const uint32_t al = tbase + kColAlo + m2 * kK + s2 * 8;
+                        mma_tf32_ts(d, ah, db + (uint64_t)(16 * s2), IT, s2 > 0 ? 1u : 0u);
+                        mma_tf32_ts(d, al, db + (uint64_t)(16 * s2), IT, 1u);
                     }
                     tc::commit(&sm.bar);
                 }
