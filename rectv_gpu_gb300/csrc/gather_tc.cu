@@ -27,7 +27,8 @@
 //    shared memory (the next slice's box is loaded while this slice is
 //    computed); threads convert it (Hermitian-mirrored tiles read the mirrored
 //    box, conjugated) into the A operand in tensor memory, hi and lo parts;
-//  * per chunk of 16 rays: one thread issues 60 MMAs into the accumulator,
+//  * per chunk of 16 rays: 60 MMAs into the accumulator, issued by five
+//    threads (one per M tile of 128 cells: its own accumulation chain);
 //    the block moves G to shared memory, the next chunk's MMAs are issued,
 //    and four threads per sample sum its 81 taps of G and write the row value
 //    (times (-1)^(k+1) shift(k) (pi/mu)/n).
@@ -133,7 +134,7 @@ __global__ void __launch_bounds__(kThr, 1)
 
     if (wid == 0) tc::alloc(&sm.tslot, kTmemCols);
     if (tid == 0) {
-        tc::mbar_init(&sm.bar_mma, 1);
+        tc::mbar_init(&sm.bar_mma, kMT);  // one commit per M tile
         tc::mbar_init(&sm.bar_tma, 1);
         tc::fence_mbar_init();
     }
@@ -242,23 +243,20 @@ __global__ void __launch_bounds__(kThr, 1)
                         bv[2] - tc::trunc_tf32(bv[2]), bv[3] - tc::trunc_tf32(bv[3]));
     };
 
-    // G = A B^T for chunk ch (B in buffer buf) into the accumulator; N = 16
-    // when the chunk has at most 8 rays.
-    auto issue = [&](uint32_t tbase, int ch, int buf) {
+    // G = A B^T for chunk ch (B in buffer buf), M tile mt, into the
+    // accumulator; N = 16 when the chunk has at most 8 rays.
+    auto issue = [&](uint32_t tbase, int ch, int buf, int mt) {
         const int nr = min(kRays, nseg - ch * kRays);
         const uint32_t IT = nr > 8 ? tc::idesc(tc::kFmtTF32, 128, 32) : tc::idesc(tc::kFmtTF32, 128, 16);
         const uint64_t dh = tc::sdesc(tc::smem_addr(sm.bhi[buf]), 128, 1024);
         const uint64_t dl = tc::sdesc(tc::smem_addr(sm.blo[buf]), 128, 1024);
+        const uint32_t d = tbase + kColD + mt * kN;
 #pragma unroll
-        for (int mt = 0; mt < kMT; ++mt) {
-            const uint32_t d = tbase + kColD + mt * kN;
-#pragma unroll
-            for (int s = 0; s < kK / 8; ++s) {  // 8 K values per MMA; +256 B per K step
-                const uint32_t ah = tbase + kColAhi + mt * kK + s * 8, al = tbase + kColAlo + mt * kK + s * 8;
-                mma_tf32_ts(d, ah, dh + (uint64_t)(16 * s), IT, s > 0 ? 1u : 0u);
-                mma_tf32_ts(d, ah, dl + (uint64_t)(16 * s), IT, 1u);
-                mma_tf32_ts(d, al, dh + (uint64_t)(16 * s), IT, 1u);
-            }
+        for (int s = 0; s < kK / 8; ++s) {  // 8 K values per MMA; +256 B per K step
+            const uint32_t ah = tbase + kColAhi + mt * kK + s * 8, al = tbase + kColAlo + mt * kK + s * 8;
+            mma_tf32_ts(d, ah, dh + (uint64_t)(16 * s), IT, s > 0 ? 1u : 0u);
+            mma_tf32_ts(d, ah, dl + (uint64_t)(16 * s), IT, 1u);
+            mma_tf32_ts(d, al, dh + (uint64_t)(16 * s), IT, 1u);
         }
         tc::commit(&sm.bar_mma);
     };
@@ -275,9 +273,11 @@ __global__ void __launch_bounds__(kThr, 1)
     uint32_t mma_par = 0;
     const unsigned gm = 0xfu << (lane & 28);  // the four lanes of a sample
     const int q = wid & 3;                    // TMEM lane quarter of this warp
-    // MMAs are issued by lane 0 of the last warp: a chunk rarely has enough
-    // samples to give that warp gather work
+    // the TMA box is requested by lane 0 of the last warp, the MMAs of M tile
+    // mt by lane 0 of warp kWarps - kMT + mt (the last warps: a chunk rarely
+    // has enough samples to give them gather work)
     const int issuer = kThr - 32;
+    const int imt = (lane == 0 && wid >= kWarps - kMT) ? wid - (kWarps - kMT) : -1;
 
     // footprint box of slice z -> A operand in tensor memory (thread = cell)
     auto convert = [&](int z) {
@@ -312,10 +312,10 @@ __global__ void __launch_bounds__(kThr, 1)
         tc::fence_proxy_async();
         tc::fence_before();
         __syncthreads();
-        if (tid == issuer) {
-            if (z + 1 < z1) tma_issue(z + 1);  // the box buffer has been read
+        if (tid == issuer && z + 1 < z1) tma_issue(z + 1);  // the box buffer has been read
+        if (imt >= 0) {
             tc::fence_after();
-            issue(tbase, 0, 0);
+            issue(tbase, 0, 0, imt);
         }
     };
 
@@ -344,9 +344,9 @@ __global__ void __launch_bounds__(kThr, 1)
             tc::fence_before();
             __syncthreads();
             if (ch + 1 < nch) {  // next chunk's MMAs run during this chunk's samples
-                if (tid == issuer) {
+                if (imt >= 0) {
                     tc::fence_after();
-                    issue(tbase, ch + 1, (ch + 1) & 1);
+                    issue(tbase, ch + 1, (ch + 1) & 1, imt);
                 }
                 if (nch > 2 && ch + 2 < nch) {
                     stage_b(ch + 2, ch & 1);
