@@ -330,16 +330,27 @@ __global__ void __launch_bounds__(kThr, 1)
             ok = tc::mbar_wait(&sm.bar_mma, mma_par) && ok;
             mma_par ^= 1u;
             tc::fence_after();
-            // ---- accumulator -> G (warp w reads TMEM lanes 32 (w % 4) ..) ----
-            for (int mt = wid >> 2; mt < kMT; mt += kWarps / 4) {
+            // ---- accumulator -> G (warp w reads TMEM lanes 32 (w % 4) ..):
+            // M tiles 0-3 one per group of four warps; tile 4 holds cells in
+            // lanes 0-63 only, split four ways by rays (8 columns per warp) ----
+            {
+                const int mt = wid >> 2;
                 float v[32];
                 tc::ld32(tbase + ((uint32_t)(32 * q) << 16) + kColD + mt * kN, v);
                 const int cell = mt * 128 + 32 * q + lane;
-                if (cell < kCells) {
 #pragma unroll
-                    for (int r = 0; r < kRays; ++r)
-                        if (r < nr) sm.g[r][cell] = make_float2(v[2 * r], v[2 * r + 1]);
-                }
+                for (int r = 0; r < kRays; ++r)
+                    if (r < nr) sm.g[r][cell] = make_float2(v[2 * r], v[2 * r + 1]);
+            }
+            static_assert(kMT == 5 && kCells - 4 * 128 <= 64 && kWarps == 16, "G read-out split");
+            if (q < 2) {
+                const int r0 = 4 * (wid >> 2);  // rays r0 .. r0 + 3
+                float v[8];
+                tc::ld8(tbase + ((uint32_t)(32 * q) << 16) + kColD + 4 * kN + 2 * r0, v);
+                const int cell = 4 * 128 + 32 * q + lane;
+#pragma unroll
+                for (int r = 0; r < 4; ++r)
+                    if (r0 + r < nr) sm.g[r0 + r][cell] = make_float2(v[2 * r], v[2 * r + 1]);
             }
             tc::fence_before();
             __syncthreads();
