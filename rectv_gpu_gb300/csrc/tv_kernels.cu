@@ -134,7 +134,7 @@ void launch_graddiv(const float *u_in, const float *u_old, float *u_out, const f
 // thread sums are accumulated in FP64 in a fixed order; one FP64 partial
 // triple per block.  Blocks of 32x8 over (qx, qy), grid.z over (chunk, qz).
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(256)
+__global__ void __launch_bounds__(256, 4)
     k_shrink(const float *__restrict__ ucur, const float *__restrict__ uold, float *__restrict__ psi,
              float *__restrict__ mu, const float *__restrict__ rhop, float lambda0, TvGeo t, int c0,
              int nch_total, double *__restrict__ partials) {
@@ -166,18 +166,36 @@ __global__ void __launch_bounds__(256)
         long long q = (long long)c * t.gp + ((long long)qz * (m + 1)) * (n + 1) * (n + 1) + (long long)qy * (n + 1) + qx;
         const long long st = (long long)(n + 1) * (n + 1);
         float fc = c0p[p00], fo = o0p[p00];  // values at (x0, y0, t0 = clamp(qt-1) = 0, z0)
-        for (int qt = 0; qt <= m; ++qt) {
+        // loads of time point qt + 1 are issued before qt is computed and
+        // stored (two time points of loads in flight per thread)
+        float lu[8], lm[4];
+        auto load = [&](int qt, long long qq) {
             const long long o0 = (long long)(qt > 0 ? qt - 1 : 0) * nn;  // t0 = clamp(qt-1)
             const long long o1 = (long long)(qt < m ? qt : m - 1) * nn;  // t1 = clamp(qt)
-            const float fcx = c0p[o0 + px], fcy = c0p[o0 + py], fct = c0p[o1 + p00], fcz = c1p[o0 + p00];
-            const float fox = o0p[o0 + px], foy = o0p[o0 + py], fot = o0p[o1 + p00], foz = o1p[o0 + p00];
+            lu[0] = c0p[o0 + px];
+            lu[1] = c0p[o0 + py];
+            lu[2] = c0p[o1 + p00];
+            lu[3] = c1p[o0 + p00];
+            lu[4] = o0p[o0 + px];
+            lu[5] = o0p[o0 + py];
+            lu[6] = o0p[o1 + p00];
+            lu[7] = o1p[o0 + p00];
+#pragma unroll
+            for (int i = 0; i < 4; ++i) lm[i] = mu[i * cs + qq];
+        };
+        load(0, q);
+        for (int qt = 0; qt <= m; ++qt) {
+            const float fcx = lu[0], fcy = lu[1], fct = lu[2], fcz = lu[3];
+            const float fox = lu[4], foy = lu[5], fot = lu[6], foz = lu[7];
+            float mv[4], ps[4];
+#pragma unroll
+            for (int i = 0; i < 4; ++i) mv[i] = lm[i];
+            if (qt < m) load(qt + 1, q + st);
             const float h[4] = {sg * (fcx - fc), sg * (fcy - fc), sgt * (fct - fc), sg * (fcz - fc)};
             const float ho[4] = {sg * (fox - fo), sg * (foy - fo), sgt * (fot - fo), sg * (foz - fo)};
-            float mv[4], ps[4];
             float za2 = 0.f;
 #pragma unroll
             for (int i = 0; i < 4; ++i) {
-                mv[i] = mu[i * cs + q];
                 ps[i] = h[i] + mv[i] / rho;  // solve_reg_ker, admm.cu:49-52
                 za2 += ps[i] * ps[i];
             }
