@@ -14,10 +14,13 @@
 // stencil), the ray, the detector index and a mask of the tile rows the
 // stencil covers.
 //
-// Persistent blocks of 256 threads (thread = cell), two per SM, take the
-// (tile, slice) units with samples round-robin; the records of the next table
-// of samples are bulk-copied into a second shared buffer (TMA engine,
-// mbarrier) while the current one is processed.  Per unit and table:
+// Persistent blocks of 512 threads, one per SM, take the (tile, slice pair)
+// units with samples round-robin; each block half (256 threads, thread =
+// cell) works on one slice of the pair, and the halves share what does not
+// depend on the slice: the records, the ray starts and sample ranges, K' (the
+// MMA's B) and the barriers.  The records of the next table of samples are
+// bulk-copied into a second shared buffer (TMA engine, mbarrier) while the
+// current one is processed.  Per unit and table:
 //  * per sample: E(p) (the row spectrum value times (-1)^(k+1) shiftadj(k)
 //    (pi/mu)/n) and T_p(cy) = E(p) wy_p(cy) for the tile's 16 rows;
 //  * per batch of 16 rays: every cell sums its value of each ray's grid
@@ -50,18 +53,21 @@ namespace {
 constexpr int kT = 16;
 constexpr int kCells = kT * kT;     // 256 = 2 M tiles
 constexpr int kMT = kCells / 128;
-constexpr int kTab = 192;           // samples per table (two record buffers and two blocks per SM)
+constexpr int kZ = 2;               // slices per unit: one per block half
+constexpr int kTab = 256;           // samples per table
 constexpr int kBatch = 16;          // rays per MMA batch (K = 32)
 constexpr int kK = 2 * kBatch;
 constexpr int kN = 32;              // 16 time samples x (re, im)
 constexpr int kNP = 2 * kN;         // MMA N: B rows [Khi | Klo]
-constexpr int kThr = kCells;
-constexpr int kWarps = kThr / 32;
-constexpr uint32_t kTmemCols = 256;
-constexpr uint32_t kColAhi = 0;             // [mt*32, +32)
-constexpr uint32_t kColAlo = kMT * kK;      // 64
-constexpr uint32_t kColD = 2 * kMT * kK;    // 128: product of the batch [mt*64, +64)
-static_assert(kTab <= kThr, "one table entry per thread");
+constexpr int kHalf = kCells;       // threads per slice: one per cell
+constexpr int kThr = kZ * kHalf;    // 512
+constexpr int kHW = kHalf / 32;     // warps per half: warp w covers tile rows 2w, 2w+1
+constexpr uint32_t kSliceCols = 256;           // TMEM columns of one slice:
+constexpr uint32_t kColAhi = 0;                //   A hi [mt*32, +32)
+constexpr uint32_t kColAlo = kMT * kK;         //   A lo (64)
+constexpr uint32_t kColD = 2 * kMT * kK;       //   product of the batch [128 + mt*64, +64)
+constexpr uint32_t kTmemCols = kZ * kSliceCols;  // 512: the whole SM (one block per SM)
+static_assert(kTab <= kHalf, "one table entry per thread of a half");
 
 __device__ __forceinline__ int off32(int row, int kk) {
     return (row >> 3) * 256 + (kk >> 2) * 32 + (row & 7) * 4 + (kk & 3);
@@ -69,18 +75,18 @@ __device__ __forceinline__ int off32(int row, int kk) {
 
 struct ScTcSmem {
     AdjRec rec[2][kTab];          // geometry records of this table and the next (bulk copies)
-    float2 t[kTab][kT];           // T_p(cy) = E(p) wy_p(cy)
-    float2 e[kTab];               // E(p) of this slice
-    float2 rnext[kTab];           // row spectrum values of the next table's samples (cp.async)
+    float2 t[kZ][kTab][kT];       // T_p(cy) = E(p) wy_p(cy), per slice of the pair
+    float2 e[kZ][kTab];           // E(p)
+    float2 rnext[kZ][kTab];       // row spectrum values of the next table's samples (cp.async)
     float bhi[kN * kK];           // B = conj K' of the batch's rays, FP32: rows 0..31 of the MMA's B
     float blo[kN * kK];           // B - trunc(B): rows 32..63 (contiguous with bhi)
     int seg_first[kTab + 1];
-    // per warp and ray: the table rows [lo, hi) from the first to the last
-    // sample whose stencil covers one of the warp's two tile rows (the others
-    // in between contribute zero weight); empty: lo = kTab, hi = 0
-    int rlo[kWarps][kTab], rhi[kWarps][kTab];
-    int wsum[kWarps];
-    unsigned long long bar;      // MMA batch done
+    // per warp (of a half) and ray: the table rows [lo, hi) from the first to
+    // the last sample whose stencil covers one of the warp's two tile rows
+    // (the others in between contribute zero weight); empty: lo = kTab, hi = 0
+    int rlo[kHW][kTab], rhi[kHW][kTab];
+    int wsum[kHW];
+    unsigned long long bar;      // MMA batch done (both slices)
     unsigned long long rbar[2];  // record buffer landed
     uint32_t tslot;
 };
@@ -159,17 +165,20 @@ void launch_adj_records(AdjRec *recs, const GeoDev &gd, const UsGeo &g, cudaStre
     LAUNCH_CHECK("k_adj_records");
 }
 
-__global__ void __launch_bounds__(kThr, 2)
+__global__ void __launch_bounds__(kThr, 1)
     k_scatter_tc(const float2 *__restrict__ rowsc, float2 *__restrict__ spec, const AdjRec *__restrict__ recs,
                  const int4 *__restrict__ items, const float2 *__restrict__ kmat, const float2 *__restrict__ shifta,
-                 UsGeo g, int zb, int nunits, int jbase, int *__restrict__ err) {
+                 UsGeo g, int zb, int npairs, int nunits, int jbase, int *__restrict__ err) {
     extern __shared__ __align__(1024) unsigned char sc_smem_raw[];
     ScTcSmem &sm = *reinterpret_cast<ScTcSmem *>(sc_smem_raw);
     const int P = g.P, hn = g.n / 2 + 1;
     const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+    const int h = tid / kHalf;     // block half: slice 2 pair + h
+    const int ct = tid % kHalf;    // this thread's cell ct = mt*128 + 32q + lane
+    const int hw = wid % kHW;      // warp within the half (tile rows 2hw, 2hw+1)
     if (wid == 0) tc::alloc(&sm.tslot, kTmemCols);
     if (tid == 0) {
-        tc::mbar_init(&sm.bar, kMT);  // one commit per M tile
+        tc::mbar_init(&sm.bar, kZ * kMT);  // one commit per (slice, M tile) chain
         tc::mbar_init(&sm.rbar[0], 1);
         tc::mbar_init(&sm.rbar[1], 1);
         tc::fence_mbar_init();
@@ -178,8 +187,9 @@ __global__ void __launch_bounds__(kThr, 2)
     __syncthreads();
     tc::fence_after();
     const uint32_t tbase = sm.tslot;
-    const int mt = wid >> 2, q = wid & 3;    // this thread's cell tid = mt*128 + 32q + lane
-    const int cx = tid % kT, cy = tid / kT;  // its column and row (warp w: rows 2w, 2w+1)
+    const uint32_t tsl = tbase + h * kSliceCols;  // this slice's TMEM columns
+    const int mt = ct >> 7, q = wid & 3;          // TMEM lane quarter of this warp
+    const int cx = ct % kT, cy = ct / kT;
     bool ok = true;
     int nmma = 0;  // MMA batches issued by this block (phase of sm.bar)
     int seq = 0;   // tables consumed: buffer seq & 1, its fill (seq >> 1) & 1
@@ -189,7 +199,7 @@ __global__ void __launch_bounds__(kThr, 2)
     int fu = blockIdx.x, fc0 = 0;
     auto fetch = [&](int slot) {
         if (fu >= nunits) return;
-        const int4 fit = __ldg(items + fu / zb);
+        const int4 fit = __ldg(items + fu / npairs);
         const uint32_t bytes = (uint32_t)min(kTab, fit.z - fc0) * (uint32_t)sizeof(AdjRec);
         tc::bulk_g2s(sm.rec[slot], recs + (long long)fit.y + fc0, bytes, &sm.rbar[slot]);
         fc0 += kTab;
@@ -201,13 +211,16 @@ __global__ void __launch_bounds__(kThr, 2)
     if (tid == 0) fetch(0);
     bool have_next = false;  // rnext holds the current table's row spectrum values
 
-    // persistent: units (tile item, slice) round-robin, slices fastest, so the
-    // blocks in flight share their items' records in L2; all units hold samples
+    // persistent: units (tile item, slice pair) round-robin, pairs fastest, so
+    // the blocks in flight share their items' records in L2; all units hold
+    // samples.  The two halves share the records, ray starts, sample ranges and
+    // K' (B); each has its slice's E, T, A, accumulator and sums.
     for (int u = blockIdx.x; u < nunits; u += gridDim.x) {
-        const int z = u % zb;
-        const int4 it = __ldg(items + u / zb);
+        const int z = 2 * (u % npairs) + h;
+        const bool zok = z < zb;  // the last pair of an odd batch has one slice
+        const int4 it = __ldg(items + u / npairs);
         const int tyi = it.x / g.NT, txi = it.x - tyi * g.NT;
-        const float2 *rz = rowsc + (long long)z * g.ntheta * hn;
+        const float2 *rz = rowsc + (long long)min(z, zb - 1) * g.ntheta * hn;
         int nbu = 0;    // MMA batches of this unit
         float acc[32];  // F of this cell: 16 time samples x (re, im)
 #pragma unroll
@@ -226,43 +239,44 @@ __global__ void __launch_bounds__(kThr, 2)
             const AdjRec *rec = sm.rec[buf];
             // ---- E = (-1)^(k+1) shiftadj(k) FFT(row)(k) (pi/mu)/n, then T_p(cy) = E(p) wy_p(cy) ----
             if (have_next) asm volatile("cp.async.wait_all;\n" ::: "memory");  // this thread's own entry
-            if (tid < cnt) {
-                const int th = (unsigned)rec[tid].thm >> 16, k = rec[tid].k;
-                float2 R = have_next ? sm.rnext[tid] : __ldg(rz + (long long)th * hn + (k <= g.n / 2 ? k : g.n - k));
+            if (ct < cnt) {
+                const int th = (unsigned)rec[ct].thm >> 16, k = rec[ct].k;
+                float2 R = make_float2(0.f, 0.f);
+                if (zok) R = have_next ? sm.rnext[h][ct] : __ldg(rz + (long long)th * hn + (k <= g.n / 2 ? k : g.n - k));
                 if (k > g.n / 2) R.y = -R.y;
-                sm.e[tid] = cmul(R, rec[tid].sf);
+                sm.e[h][ct] = cmul(R, rec[ct].sf);
             }
             __syncthreads();
-            for (int i = tid; i < cnt * kT; i += kThr) {
+            for (int i = ct; i < cnt * kT; i += kHalf) {
                 const int e = i >> 4, row = i & 15;
-                const float2 E = sm.e[e];
+                const float2 E = sm.e[h][e];
                 const float w = rec[e].wy[row];
-                sm.t[e][row] = make_float2(E.x * w, E.y * w);
+                sm.t[h][e][row] = make_float2(E.x * w, E.y * w);
             }
-            // ---- first table row of each ray: block-wide scan of ray starts ----
+            // ---- first table row of each ray: scan of ray starts (half 0) ----
             int flag = 0;
-            if (tid < cnt) flag = (tid == 0 || (rec[tid].thm >> 16) != (rec[tid - 1].thm >> 16)) ? 1 : 0;
+            if (h == 0 && ct < cnt) flag = (ct == 0 || (rec[ct].thm >> 16) != (rec[ct - 1].thm >> 16)) ? 1 : 0;
             int incl = flag;
 #pragma unroll
             for (int o = 1; o < 32; o <<= 1) {
                 const int y = __shfl_up_sync(0xffffffffu, incl, o);
                 if (lane >= o) incl += y;
             }
-            if (lane == 31) sm.wsum[wid] = incl;
+            if (h == 0 && lane == 31) sm.wsum[hw] = incl;
             __syncthreads();
             int base = 0, nseg = 0;
 #pragma unroll
-            for (int w = 0; w < kWarps; ++w) {
+            for (int w = 0; w < kHW; ++w) {
                 const int v = sm.wsum[w];
-                base += (w < wid) ? v : 0;
+                base += (w < hw) ? v : 0;
                 nseg += v;
             }
             incl += base;
-            const int seg = incl - 1;  // ray (segment) of this thread's sample
-            if (tid < cnt && flag) {
-                sm.seg_first[seg] = tid;
+            const int seg = incl - 1;  // ray (segment) of this thread's sample (half 0)
+            if (h == 0 && ct < cnt && flag) {
+                sm.seg_first[seg] = ct;
 #pragma unroll
-                for (int w = 0; w < kWarps; ++w) {
+                for (int w = 0; w < kHW; ++w) {
                     sm.rlo[w][seg] = kTab;
                     sm.rhi[w][seg] = 0;
                 }
@@ -271,17 +285,17 @@ __global__ void __launch_bounds__(kThr, 2)
             __syncthreads();  // ray starts, empty ranges and T written
             // ---- per warp and ray: first and last sample covering the warp's
             // rows, from the samples where a covered run starts or ends ----
-            if (tid < cnt) {
-                const int msk = rec[tid].thm & 0xffff;
-                const int mprev = flag ? 0 : (rec[tid - 1].thm & 0xffff);
-                const bool last = tid + 1 == cnt || (rec[tid + 1].thm >> 16) != (rec[tid].thm >> 16);
-                const int mnext = last ? 0 : (rec[tid + 1].thm & 0xffff);
+            if (h == 0 && ct < cnt) {
+                const int msk = rec[ct].thm & 0xffff;
+                const int mprev = flag ? 0 : (rec[ct - 1].thm & 0xffff);
+                const bool last = ct + 1 == cnt || (rec[ct + 1].thm >> 16) != (rec[ct].thm >> 16);
+                const int mnext = last ? 0 : (rec[ct + 1].thm & 0xffff);
 #pragma unroll
-                for (int w = 0; w < kWarps; ++w) {
+                for (int w = 0; w < kHW; ++w) {
                     const int bits = 3 << (2 * w);
                     if (msk & bits) {
-                        if (!(mprev & bits)) atomicMin(&sm.rlo[w][seg], tid);
-                        if (!(mnext & bits)) atomicMax(&sm.rhi[w][seg], tid + 1);
+                        if (!(mprev & bits)) atomicMin(&sm.rlo[w][seg], ct);
+                        if (!(mnext & bits)) atomicMax(&sm.rhi[w][seg], ct + 1);
                     }
                 }
             }
@@ -295,14 +309,15 @@ __global__ void __launch_bounds__(kThr, 2)
                 }
                 have_next = nu < nunits;
                 if (have_next) {
-                    const int4 nit = nu == u ? it : __ldg(items + nu / zb);
-                    const float2 *nrz = rowsc + (long long)(nu % zb) * g.ntheta * hn;
+                    const int4 nit = nu == u ? it : __ldg(items + nu / npairs);
+                    const int nz = 2 * (nu % npairs) + h;
                     ok = tc::mbar_wait(&sm.rbar[buf ^ 1], (uint32_t)((seq >> 1) & 1)) && ok;
-                    if (tid < min(kTab, nit.z - nc0)) {
-                        const AdjRec &nr = sm.rec[buf ^ 1][tid];
+                    if (nz < zb && ct < min(kTab, nit.z - nc0)) {
+                        const float2 *nrz = rowsc + (long long)nz * g.ntheta * hn;
+                        const AdjRec &nr = sm.rec[buf ^ 1][ct];
                         const int th = (unsigned)nr.thm >> 16, k = nr.k;
                         const float2 *src = nrz + (long long)th * hn + (k <= g.n / 2 ? k : g.n - k);
-                        asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(tc::smem_addr(&sm.rnext[tid])),
+                        asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(tc::smem_addr(&sm.rnext[h][ct])),
                                      "l"(src)
                                      : "memory");
                         asm volatile("cp.async.commit_group;\n" ::: "memory");
@@ -313,16 +328,16 @@ __global__ void __launch_bounds__(kThr, 2)
 
             for (int sb = 0; sb < nseg; sb += kBatch) {
                 const int nb = min(kBatch, nseg - sb);
-                // K'(ray, j) of this thread's two B entries, loaded before the ray
-                // sums so that the L2 latency is not in front of the batch barrier
-                const int brow = tid >> 3, bq4 = tid & 7;  // B row 2j+o, K values 4 bq4 .. 4 bq4 + 3
+                // K'(ray, j) of this thread's two B entries (half 0), loaded before
+                // the ray sums so that the L2 latency is not in front of the barrier
+                const int brow = ct >> 3, bq4 = ct & 7;  // B row 2j+o, K values 4 bq4 .. 4 bq4 + 3
                 const int bj = brow >> 1;
                 float2 kv[2];
 #pragma unroll
                 for (int i = 0; i < 2; ++i) {
                     const int r = 2 * bq4 + i;
                     kv[i] = make_float2(0.f, 0.f);
-                    if (r < nb && jbase + bj < g.m)
+                    if (h == 0 && r < nb && jbase + bj < g.m)
                         kv[i] = __ldg(kmat + (long long)((unsigned)rec[sm.seg_first[sb + r]].thm >> 16) * g.m + jbase + bj);
                 }
                 // ---- 1. V(c, ray) of this cell for the batch's rays ----
@@ -331,11 +346,11 @@ __global__ void __launch_bounds__(kThr, 2)
                 for (int r = 0; r < kBatch; ++r) {
                     float2 v = make_float2(0.f, 0.f);
                     if (r < nb) {  // T and wx vanish outside the stencil: no tests in the loop
-                        const int e1 = sm.rhi[wid][sb + r];
+                        const int e1 = sm.rhi[hw][sb + r];
 #pragma unroll 4
-                        for (int e = sm.rlo[wid][sb + r]; e < e1; ++e) {
+                        for (int e = sm.rlo[hw][sb + r]; e < e1; ++e) {
                             const float w = rec[e].wx[cx];
-                            v = ffma2(make_float2(w, w), sm.t[e][cy], v);
+                            v = ffma2(make_float2(w, w), sm.t[h][e][cy], v);
                         }
                     }
                     vv[2 * r] = v.x;
@@ -347,13 +362,13 @@ __global__ void __launch_bounds__(kThr, 2)
                     ok = tc::mbar_wait(&sm.bar, (uint32_t)((nmma - 1) & 1)) && ok;
                     tc::fence_after();
                     float v[32], w2[32];
-                    tc::ld32(tbase + ((uint32_t)(32 * q) << 16) + kColD + mt * kNP, v);
-                    tc::ld32(tbase + ((uint32_t)(32 * q) << 16) + kColD + mt * kNP + kN, w2);
+                    tc::ld32(tsl + ((uint32_t)(32 * q) << 16) + kColD + mt * kNP, v);
+                    tc::ld32(tsl + ((uint32_t)(32 * q) << 16) + kColD + mt * kNP + kN, w2);
 #pragma unroll
                     for (int i = 0; i < 32; ++i) acc[i] += v[i] + w2[i];
                 }
-                // ---- B = conj K' rows of this batch: row 2j+o, K index 2r+s (threads = (row, 4 K values)) ----
-                {
+                // ---- B = conj K' rows of this batch: row 2j+o, K index 2r+s (half 0: threads = (row, 4 K values)) ----
+                if (h == 0) {
                     const int o = brow & 1;
                     float bv[4];
 #pragma unroll
@@ -372,7 +387,7 @@ __global__ void __launch_bounds__(kThr, 2)
                     float lo[32];
 #pragma unroll
                     for (int i = 0; i < 32; ++i) lo[i] = vv[i] - tc::trunc_tf32(vv[i]);
-                    const uint32_t ta0 = tbase + ((uint32_t)(32 * q) << 16);
+                    const uint32_t ta0 = tsl + ((uint32_t)(32 * q) << 16);
                     st32(ta0 + kColAhi + mt * kK, vv);
                     st32(ta0 + kColAlo + mt * kK, lo);
                     asm volatile("tcgen05.wait::st.sync.aligned;\n" ::: "memory");
@@ -380,20 +395,20 @@ __global__ void __launch_bounds__(kThr, 2)
                 tc::fence_proxy_async();
                 tc::fence_before();
                 __syncthreads();
-                // one issuing thread per M tile (its own accumulator chain), in
-                // two warps that rotate, so that no warp carries all 16 issues
-                const int iw = (2 * nmma) % kWarps;
-                if (lane == 0 && (wid == iw || wid == iw + 1)) {
+                // one issuing thread per (slice, M tile) accumulator chain, two
+                // rotating warps per half, so that no warp carries all issues
+                const int iw = (2 * nmma) % kHW;
+                if (lane == 0 && (hw == iw || hw == iw + 1)) {
                     tc::fence_after();
                     // D = [Ahi Bhi, Ahi Blo] + [Alo Bhi, Alo Blo]: both halves summed when read
                     constexpr uint32_t IT = tc::idesc(tc::kFmtTF32, 128, kNP);
                     const uint64_t db = tc::sdesc(tc::smem_addr(sm.bhi), 128, 1024);
-                    const int m2 = wid - iw;
-                    const uint32_t d = tbase + kColD + m2 * kNP;
+                    const int m2 = hw - iw;
+                    const uint32_t d = tsl + kColD + m2 * kNP;
 #pragma unroll
                     for (int s2 = 0; s2 < kK / 8; ++s2) {
-                        const uint32_t ah = tbase + kColAhi + m2 * kK + s2 * 8;
-                        const uint32_t al = tbase + kColAlo + m2 * kK + s2 * 8;
+                        const uint32_t ah = tsl + kColAhi + m2 * kK + s2 * 8;
+                        const uint32_t al = tsl + kColAlo + m2 * kK + s2 * 8;
                         mma_tf32_ts(d, ah, db + (uint64_t)(16 * s2), IT, s2 > 0 ? 1u : 0u);
                         mma_tf32_ts(d, al, db + (uint64_t)(16 * s2), IT, 1u);
                     }
@@ -408,8 +423,8 @@ __global__ void __launch_bounds__(kThr, 2)
             ok = tc::mbar_wait(&sm.bar, (uint32_t)((nmma - 1) & 1)) && ok;
             tc::fence_after();
             float v[32], w2[32];
-            tc::ld32(tbase + ((uint32_t)(32 * q) << 16) + kColD + mt * kNP, v);
-            tc::ld32(tbase + ((uint32_t)(32 * q) << 16) + kColD + mt * kNP + kN, w2);
+            tc::ld32(tsl + ((uint32_t)(32 * q) << 16) + kColD + mt * kNP, v);
+            tc::ld32(tsl + ((uint32_t)(32 * q) << 16) + kColD + mt * kNP + kN, w2);
 #pragma unroll
             for (int i = 0; i < 32; ++i) acc[i] += v[i] + w2[i];
         }
@@ -419,7 +434,7 @@ __global__ void __launch_bounds__(kThr, 2)
         // (at most two adds per H cell from two blocks, onto zeros: the sum does not
         // depend on their order); the pre-IFFT fftshift sign is applied here ----
         const int KY = tyi * kT + cy, KX = txi * kT + cx;
-        if (KY < P && KX < P) {
+        if (zok && KY < P && KX < P) {
             const int half = P / 2, hp = half + 1;
             const long long img_half = (long long)P * hp;
             const float sg = ((KX + KY) & 1) ? -0.5f : 0.5f;
@@ -443,10 +458,8 @@ __global__ void __launch_bounds__(kThr, 2)
     if (!ok && lane == 0) atomicAdd(err, 1);
 }
 
-// At most two blocks per SM: each holds 256 of the 512 tensor-memory columns
-// (a third resident block would wait in tcgen05.alloc), so the shared memory
-// request is raised to more than a third of the SM's 228 KB.
-constexpr size_t kScSmemBytes = sizeof(ScTcSmem) > 80 * 1024 ? sizeof(ScTcSmem) : 80 * 1024;
+// One block per SM: it holds all 512 tensor-memory columns (two slices x 256).
+constexpr size_t kScSmemBytes = sizeof(ScTcSmem);
 
 void scatter_tc_prepare() {
     CUDA_CHECK(cudaFuncSetAttribute(k_scatter_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kScSmemBytes));
@@ -457,8 +470,9 @@ void launch_scatter_tc(const float2 *rowsc, float2 *spec, int zb, const GeoDev &
     if (g.T != kT) throw Error(1, "tile size must be 16");
     if (!gd.adj_recs) throw Error(1, "adjoint geometry records missing");
     // items with samples (sorted by count, so the empty tiles, whose half
-    // planes stay zero, come last)
-    const long long nunits = (long long)zb * gd.n_adj_busy;
+    // planes stay zero, come last), times slice pairs
+    const int npairs = (zb + kZ - 1) / kZ;
+    const long long nunits = (long long)npairs * gd.n_adj_busy;
     if (nunits == 0) return;
     if (nunits > 2147483647LL) throw Error(1, "adjoint grid too large");
     static int nsm = 0;
@@ -467,9 +481,9 @@ void launch_scatter_tc(const float2 *rowsc, float2 *spec, int zb, const GeoDev &
         CUDA_CHECK(cudaGetDevice(&dev));
         CUDA_CHECK(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
     }
-    const int grid = (int)std::min<long long>(nunits, 2LL * nsm);
+    const int grid = (int)std::min<long long>(nunits, nsm);
     k_scatter_tc<<<grid, kThr, kScSmemBytes, s>>>(rowsc, spec, gd.adj_recs, gd.adj_items, gd.kmat, gd.shiftadj, g,
-                                                  zb, (int)nunits, jbase, gd.err);
+                                                  zb, npairs, (int)nunits, jbase, gd.err);
     LAUNCH_CHECK("k_scatter_tc");
 }
 
