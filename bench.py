@@ -353,10 +353,11 @@ def run_ours(args, rank, world, local_rank):
     peak, peak_kind = measured_peaks()
     achieved = bytes_.value / (ktimes[dom] * 1e-3) / 1e9
     limiter = {
-        "k_scatter_tc": "instruction issue / shared-memory latency of the per-cell ray sums (CUDA cores); "
-                        "the time-sample GEMM runs on tcgen05 (3xTF32); DRAM traffic ~= algorithmic bytes",
-        "k_gather_tc": "tcgen05 MMA issue (60 small N=32 MMAs per 16-ray chunk) and block barriers; "
-                       "TMA-staged footprints, DRAM traffic 1.4x the spectra (overlapping tile halos)",
+        "k_scatter_tc": "CUDA-core issue and shared-memory latency of the per-cell ray sums, and the "
+                        "per-batch barrier before the tcgen05 time-sample GEMM (3xTF32); DRAM traffic about "
+                        "2x the algorithmic bytes (atomic adds read back the Hermitian half planes)",
+        "k_gather_tc": "shared-memory bandwidth of the per-sample 81-tap sums and of the TMEM -> shared "
+                       "read-out of G, block barriers; TMA-staged footprints, DRAM traffic about the spectra",
         "k_graddiv": "HBM bandwidth", "k_shrink": "HBM bandwidth"}[KERNEL_NAMES[dom]]
     roofline = {"bound": "hbm", "limiter": limiter, "kernel": KERNEL_NAMES[dom], "achieved": achieved,
                 "peak": peak,

@@ -59,7 +59,7 @@ __device__ __forceinline__ void block_reduce3(double a, double b, double c, doub
 // Fused inner step (gradient, lin4, divergent of admm.cu:85-95 with tau=-0.5):
 //   u_out(v) = u_in(v) + tau sd sum_d [h_d(q-e_d) - h_d(q)],  q = v+1,
 //   h = rho (G u_in - psi) + mu.
-// One thread per voxel; blocks of 32x8 over (x, y), grid.z over (slice, t).
+// One thread per voxel; blocks of 256x1 over (x, y), grid.z over (slice, t).
 // ---------------------------------------------------------------------------
 __global__ void __launch_bounds__(256)
     k_graddiv(const float *__restrict__ uin, const float *__restrict__ uold, float *__restrict__ uout,
@@ -119,7 +119,9 @@ __global__ void __launch_bounds__(256)
 void launch_graddiv(const float *u_in, const float *u_old, float *u_out, const float *psi,
                     const float *mu, const float *rho, int c0, int nchunks_total, const TvGeo &t,
                     cudaStream_t s) {
-    dim3 bs(32, 8), gs((t.n + 31) / 32, (t.n + 7) / 8, t.nchunks * t.nzp * t.m);
+    // one row of 256 voxels per block: each of the 17 input streams is read in
+    // 1 KB runs (DRAM page locality)
+    dim3 bs(256, 1), gs((t.n + 255) / 256, t.n, t.nchunks * t.nzp * t.m);
     k_graddiv<<<gs, bs, 0, s>>>(u_in, u_old, u_out, psi, mu, rho, t, c0, nchunks_total, -0.5f);
     LAUNCH_CHECK("k_graddiv");
 }
@@ -161,7 +163,7 @@ __global__ void __launch_bounds__(256, 4)
         const bool inner_xyz = (qx >= 1 && qy >= 1 && qz >= 1);
         const float sg = t.sg, sgt = t.sg * t.lambda1;
         const float rho = *rhop;
-        const float thr = lambda0 / rho;
+        const float thr = lambda0 / rho, rinv = 1.0f / rho;
         const long long cs = t.comp_stride;
         long long q = (long long)c * t.gp + ((long long)qz * (m + 1)) * (n + 1) * (n + 1) + (long long)qy * (n + 1) + qx;
         const long long st = (long long)(n + 1) * (n + 1);
@@ -196,14 +198,15 @@ __global__ void __launch_bounds__(256, 4)
             float za2 = 0.f;
 #pragma unroll
             for (int i = 0; i < 4; ++i) {
-                ps[i] = h[i] + mv[i] / rho;  // solve_reg_ker, admm.cu:49-52
+                ps[i] = h[i] + mv[i] * rinv;  // solve_reg_ker, admm.cu:49-52
                 za2 += ps[i] * ps[i];
             }
             const float za = sqrtf(za2);
+            const float shr = (za <= thr) ? 0.f : 1.0f - thr / za;  // shrink factor of the 4-vector
             float r2 = 0.f, s2 = 0.f;
 #pragma unroll
             for (int i = 0; i < 4; ++i) {
-                ps[i] = (za <= thr) ? 0.f : ps[i] - thr * ps[i] / za;
+                ps[i] = ps[i] * shr;
                 psi[i * cs + q] = ps[i];
                 mu[i * cs + q] = mv[i] + rho * h[i] - rho * ps[i];  // lin4(mu,h2,psi,1,rho,-rho)
                 const float dr = h[i] - ps[i], ds = ho[i] - h[i];
