@@ -91,18 +91,12 @@ struct ScTcSmem {
     uint32_t tslot;
 };
 
-__device__ __forceinline__ void st32(uint32_t taddr, const float (&v)[32]) {
+__device__ __forceinline__ void st16(uint32_t taddr, const float (&v)[16]) {
     asm volatile(
         "tcgen05.st.sync.aligned.32x32b.x16.b32 [%0], {%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,%16};\n" ::"r"(
             taddr),
         "f"(v[0]), "f"(v[1]), "f"(v[2]), "f"(v[3]), "f"(v[4]), "f"(v[5]), "f"(v[6]), "f"(v[7]), "f"(v[8]), "f"(v[9]),
         "f"(v[10]), "f"(v[11]), "f"(v[12]), "f"(v[13]), "f"(v[14]), "f"(v[15])
-        : "memory");
-    asm volatile(
-        "tcgen05.st.sync.aligned.32x32b.x16.b32 [%0], {%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,%16};\n" ::"r"(
-            taddr + 16),
-        "f"(v[16]), "f"(v[17]), "f"(v[18]), "f"(v[19]), "f"(v[20]), "f"(v[21]), "f"(v[22]), "f"(v[23]), "f"(v[24]),
-        "f"(v[25]), "f"(v[26]), "f"(v[27]), "f"(v[28]), "f"(v[29]), "f"(v[30]), "f"(v[31])
         : "memory");
 }
 
@@ -340,21 +334,27 @@ __global__ void __launch_bounds__(kThr, 1)
                     if (h == 0 && r < nb && jbase + bj < g.m)
                         kv[i] = __ldg(kmat + (long long)((unsigned)rec[sm.seg_first[sb + r]].thm >> 16) * g.m + jbase + bj);
                 }
-                // ---- 1. V(c, ray) of this cell for the batch's rays ----
-                float vv[2 * kBatch];
+                // ---- 1. V(c, ray) of this cell for rays [8h, 8h + 8) of the
+                // batch, both slices of the pair (one weight load, two FMAs) ----
+                constexpr int kRH = kBatch / kZ;  // rays per half
+                float v0[2 * kRH], v1[2 * kRH];
 #pragma unroll
-                for (int r = 0; r < kBatch; ++r) {
-                    float2 v = make_float2(0.f, 0.f);
-                    if (r < nb) {  // T and wx vanish outside the stencil: no tests in the loop
-                        const int e1 = sm.rhi[hw][sb + r];
+                for (int r = 0; r < kRH; ++r) {
+                    const int rr = kRH * h + r;
+                    float2 a = make_float2(0.f, 0.f), b = make_float2(0.f, 0.f);
+                    if (rr < nb) {  // T and wx vanish outside the stencil: no tests in the loop
+                        const int e1 = sm.rhi[hw][sb + rr];
 #pragma unroll 4
-                        for (int e = sm.rlo[hw][sb + r]; e < e1; ++e) {
+                        for (int e = sm.rlo[hw][sb + rr]; e < e1; ++e) {
                             const float w = rec[e].wx[cx];
-                            v = ffma2(make_float2(w, w), sm.t[h][e][cy], v);
+                            a = ffma2(make_float2(w, w), sm.t[0][e][cy], a);
+                            b = ffma2(make_float2(w, w), sm.t[1][e][cy], b);
                         }
                     }
-                    vv[2 * r] = v.x;
-                    vv[2 * r + 1] = v.y;
+                    v0[2 * r] = a.x;
+                    v0[2 * r + 1] = a.y;
+                    v1[2 * r] = b.x;
+                    v1[2 * r + 1] = b.y;
                 }
                 // ---- previous batch's MMAs done: add its product to the cell's
                 // FP32 sums; A, B and the accumulator are then free ----
@@ -382,14 +382,19 @@ __global__ void __launch_bounds__(kThr, 1)
                         make_float4(bv[0] - tc::trunc_tf32(bv[0]), bv[1] - tc::trunc_tf32(bv[1]),
                                     bv[2] - tc::trunc_tf32(bv[2]), bv[3] - tc::trunc_tf32(bv[3]));
                 }
-                // ---- 2. A = V of this cell, hi and lo parts, into tensor memory ----
+                // ---- 2. A = V of this cell, hi and lo parts, into tensor memory:
+                // K columns 16h .. 16h + 15 (this half's rays) of both slices ----
                 {
-                    float lo[32];
+                    float lo[2 * kRH];
+                    const uint32_t ta0 = tbase + ((uint32_t)(32 * q) << 16) + mt * kK + 2 * kRH * h;
 #pragma unroll
-                    for (int i = 0; i < 32; ++i) lo[i] = vv[i] - tc::trunc_tf32(vv[i]);
-                    const uint32_t ta0 = tsl + ((uint32_t)(32 * q) << 16);
-                    st32(ta0 + kColAhi + mt * kK, vv);
-                    st32(ta0 + kColAlo + mt * kK, lo);
+                    for (int i = 0; i < 2 * kRH; ++i) lo[i] = v0[i] - tc::trunc_tf32(v0[i]);
+                    st16(ta0 + kColAhi, v0);
+                    st16(ta0 + kColAlo, lo);
+#pragma unroll
+                    for (int i = 0; i < 2 * kRH; ++i) lo[i] = v1[i] - tc::trunc_tf32(v1[i]);
+                    st16(ta0 + kSliceCols + kColAhi, v1);
+                    st16(ta0 + kSliceCols + kColAlo, lo);
                     asm volatile("tcgen05.wait::st.sync.aligned;\n" ::: "memory");
                 }
                 tc::fence_proxy_async();
