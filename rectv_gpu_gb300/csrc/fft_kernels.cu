@@ -1,0 +1,477 @@
+// Two-dimensional FFTs of the USFFT operators for P = 2n a power of two
+// (256 <= P <= 4096), written for the zero padding of the reference's grids.
+//
+// The reference pads the deapodised n x n image into the centre of a P x P
+// grid, modulates it by (-1)^(X+Y) and runs a P x P FFT (divphi, fftshift and
+// the cuFFT 2D plan, radonusfft.cu:85-90, kernels_radonusfft.cuh:4-38); the
+// adjoint runs the inverse FFT and crops the centre (radonusfft.cu:127-132).
+// Three quarters of the forward input and of the adjoint output are padding,
+// so the passes here touch only what is not:
+//
+//  forward  rows    n/2 row pairs per image: the pair's two deapodised real
+//                   rows are one complex P-point FFT (a + i b, split after the
+//                   transform), input read straight from the volume; writes
+//                   the n+1 half-plane columns of rows [n/2, 3n/2)
+//           columns n+1 columns of P points whose input rows outside
+//                   [n/2, 3n/2) are zero (not read); writes all P rows
+//  adjoint  columns n+1 inverse P-point FFTs of the Hermitian half planes;
+//                   writes only rows [n/2, 3n/2) (in place)
+//           rows    n/2 row pairs: the Hermitian extension of two half rows
+//                   as one complex inverse FFT (Re -> first row, Im -> second),
+//                   only the n centre outputs, deapodised and added into u
+//
+// Every transform is P = 16 x 16 x R3 points (R3 = P/256) computed by P/16
+// threads holding 16 values each: a 16-point DFT in registers, twiddles,
+// exchange through shared memory, a 16-point DFT, twiddles, exchange, and
+// R3-point DFTs.  Twiddles come from a table of exp(-2 pi i k/P) evaluated in
+// double precision on the host.  Results equal cuFFT's to FP32 rounding.
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <vector>
+
+#include "rectv_internal.cuh"
+
+namespace rectv {
+
+namespace {
+
+__device__ __forceinline__ float2 operator+(float2 a, float2 b) { return make_float2(a.x + b.x, a.y + b.y); }
+__device__ __forceinline__ float2 operator-(float2 a, float2 b) { return make_float2(a.x - b.x, a.y - b.y); }
+__device__ __forceinline__ float2 cmul_(float2 a, float2 b) {
+    return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+__device__ __forceinline__ float2 conj_(float2 a) { return make_float2(a.x, -a.y); }
+
+// a * exp(DIR * i pi / 2): DIR = -1 (forward) multiplies by -i, DIR = +1 by +i
+template <int DIR>
+__device__ __forceinline__ float2 rot4(float2 a) {
+    return DIR < 0 ? make_float2(a.y, -a.x) : make_float2(-a.y, a.x);
+}
+
+// a * exp(DIR * 2 pi i e / 16) for a compile-time e in [0, 16)
+template <int E, int DIR>
+__device__ __forceinline__ float2 tw16(float2 a) {
+    constexpr int e = E & 15;
+    constexpr float C1 = 0.92387953251128674f;  // cos(pi/8)
+    constexpr float S1 = 0.38268343236508977f;  // sin(pi/8)
+    constexpr float R2 = 0.70710678118654752f;  // cos(pi/4)
+    constexpr float cs[16] = {1.f, C1, R2, S1, 0.f, -S1, -R2, -C1, -1.f, -C1, -R2, -S1, 0.f, S1, R2, C1};
+    constexpr float sn[16] = {0.f, S1, R2, C1, 1.f, C1, R2, S1, 0.f, -S1, -R2, -C1, -1.f, -C1, -R2, -S1};
+    if constexpr (e == 0) {
+        return a;
+    } else if constexpr (e == 4) {
+        return rot4<DIR>(a);
+    } else if constexpr (e == 8) {
+        return make_float2(-a.x, -a.y);
+    } else if constexpr (e == 12) {
+        return rot4<-DIR>(a);
+    } else {
+        constexpr float c = cs[e], s = DIR * sn[e];
+        return make_float2(a.x * c - a.y * s, a.x * s + a.y * c);
+    }
+}
+
+template <int DIR>
+__device__ __forceinline__ void dft2(float2 &x0, float2 &x1) {
+    const float2 s = x0 + x1, d = x0 - x1;
+    x0 = s;
+    x1 = d;
+}
+
+template <int DIR>
+__device__ __forceinline__ void dft4(float2 &x0, float2 &x1, float2 &x2, float2 &x3) {
+    const float2 s02 = x0 + x2, d02 = x0 - x2, s13 = x1 + x3, d13 = rot4<DIR>(x1 - x3);
+    x0 = s02 + s13;
+    x2 = s02 - s13;
+    x1 = d02 + d13;
+    x3 = d02 - d13;
+}
+
+// in place, natural order in and out: v[k] = sum_r v[r] exp(DIR 2 pi i r k / 8)
+template <int DIR>
+__device__ __forceinline__ void dft8(float2 *v) {
+    // r = 2a + b, k = c + 4d
+    dft4<DIR>(v[0], v[2], v[4], v[6]);  // b = 0 -> y0[c] at v[0], v[2], v[4], v[6]
+    dft4<DIR>(v[1], v[3], v[5], v[7]);  // b = 1
+    v[3] = tw16<2, DIR>(v[3]);          // omega8^c = omega16^(2c)
+    v[5] = tw16<4, DIR>(v[5]);
+    v[7] = tw16<6, DIR>(v[7]);
+    float2 o[8];
+#pragma unroll
+    for (int c = 0; c < 4; ++c) {
+        o[c] = v[2 * c] + v[2 * c + 1];
+        o[c + 4] = v[2 * c] - v[2 * c + 1];
+    }
+#pragma unroll
+    for (int i = 0; i < 8; ++i) v[i] = o[i];
+}
+
+// in place, natural order in and out: v[k] = sum_r v[r] exp(DIR 2 pi i r k / 16)
+template <int DIR>
+__device__ __forceinline__ void dft16(float2 *v) {
+    // r = 4a + b, k = c + 4d: DFT4 over a for each b, twiddle omega16^(bc), DFT4 over b
+#pragma unroll
+    for (int b = 0; b < 4; ++b) dft4<DIR>(v[b], v[4 + b], v[8 + b], v[12 + b]);  // y[b][c] at v[4c + b]
+    v[4 * 1 + 1] = tw16<1, DIR>(v[5]);
+    v[4 * 1 + 2] = tw16<2, DIR>(v[6]);
+    v[4 * 1 + 3] = tw16<3, DIR>(v[7]);
+    v[4 * 2 + 1] = tw16<2, DIR>(v[9]);
+    v[4 * 2 + 2] = tw16<4, DIR>(v[10]);
+    v[4 * 2 + 3] = tw16<6, DIR>(v[11]);
+    v[4 * 3 + 1] = tw16<3, DIR>(v[13]);
+    v[4 * 3 + 2] = tw16<6, DIR>(v[14]);
+    v[4 * 3 + 3] = tw16<9, DIR>(v[15]);
+#pragma unroll
+    for (int c = 0; c < 4; ++c) dft4<DIR>(v[4 * c], v[4 * c + 1], v[4 * c + 2], v[4 * c + 3]);  // over b
+    // V[c + 4d] sits at v[4c + d]: transpose the 4x4 index
+    float2 o[16];
+#pragma unroll
+    for (int c = 0; c < 4; ++c)
+#pragma unroll
+        for (int d = 0; d < 4; ++d) o[c + 4 * d] = v[4 * c + d];
+#pragma unroll
+    for (int i = 0; i < 16; ++i) v[i] = o[i];
+}
+
+template <int R, int DIR>
+__device__ __forceinline__ void dftR(float2 *v) {
+    if constexpr (R == 2) dft2<DIR>(v[0], v[1]);
+    if constexpr (R == 4) dft4<DIR>(v[0], v[1], v[2], v[3]);
+    if constexpr (R == 8) dft8<DIR>(v);
+    if constexpr (R == 16) dft16<DIR>(v);
+}
+
+__device__ __forceinline__ float2 twiddle(const float2 *__restrict__ tw, int e, int dir) {
+    const float2 w = __ldg(tw + e);
+    return dir < 0 ? w : make_float2(w.x, -w.y);
+}
+
+// Shared-memory layouts of one transform's values at the two exchanges.
+//  INTERLEAVED (column kernels, thread = c + C t): element i of transform c
+//    at i*C + c; stage-2 output of pair p, m1 at p*Q + m1 (Q = R3+1 odd).
+//  regions (row kernels, thread = t + (P/16) c): element i of transform c at
+//    c*S + i; stage-2 output at p*R3 + ((m1 + p/(16/R3)) mod R3).
+// Both make every exchange free of bank conflicts.
+template <int N, bool INTERLEAVED, int C>
+struct FftLayout {
+    static constexpr int N1 = N / 16;
+    static constexpr int R3 = N / 256;
+    static constexpr int P1 = N1 + R3;
+    static constexpr int Q = INTERLEAVED ? (R3 == 1 ? 1 : R3 + 1) : R3;
+    static constexpr int S1 = 16 * P1;
+    static constexpr int S2 = 256 * Q;
+    static constexpr int S = (S1 > S2 ? S1 : S2) > N ? (S1 > S2 ? S1 : S2) : N;  // elements per transform
+    __device__ static __forceinline__ int a1(int c, int i) { return INTERLEAVED ? i * C + c : c * S + i; }
+    __device__ static __forceinline__ int a2(int c, int p, int m1) {
+        if constexpr (INTERLEAVED) {
+            return (p * Q + m1) * C + c;
+        } else {
+            constexpr int G = (R3 >= 16) ? 1 : 16 / R3;
+            return c * S + p * R3 + ((R3 == 1) ? 0 : ((m1 + p / G) & (R3 - 1)));
+        }
+    }
+};
+
+// One P-point FFT per transform c; thread t of the transform enters with
+// v[r] = x[t + N1 r] (r < 16) and leaves with v[q R3 + j1] = X[t + N1 q +
+// 256 j1] (q < 16/R3, j1 < R3).  All threads of the block must call it.
+template <int N, int DIR, class L>
+__device__ __forceinline__ void fft_core(float2 *v, float2 *sh, int c, int t, const float2 *__restrict__ tw) {
+    constexpr int N1 = L::N1, R3 = L::R3;
+    // stage 1: 16-point DFT over n2 of x[n1 + N1 n2], twiddle omega_N^(n1 k2)
+    dft16<DIR>(v);
+#pragma unroll
+    for (int k2 = 1; k2 < 16; ++k2) v[k2] = cmul_(v[k2], twiddle(tw, (t * k2) & (N - 1), DIR));
+#pragma unroll
+    for (int k2 = 0; k2 < 16; ++k2) sh[L::a1(c, k2 * L::P1 + t)] = v[k2];
+    __syncthreads();
+    // stage 2: thread (k2, m1), 16-point DFT over m2 of y[k2][m1 + R3 m2]
+    const int k2 = t / R3, m1 = t - k2 * R3;
+#pragma unroll
+    for (int m2 = 0; m2 < 16; ++m2) v[m2] = sh[L::a1(c, k2 * L::P1 + m1 + R3 * m2)];
+    __syncthreads();
+    dft16<DIR>(v);
+#pragma unroll
+    for (int j2 = 1; j2 < 16; ++j2) v[j2] = cmul_(v[j2], twiddle(tw, (16 * m1 * j2) & (N - 1), DIR));
+#pragma unroll
+    for (int j2 = 0; j2 < 16; ++j2) sh[L::a2(c, k2 + 16 * j2, m1)] = v[j2];
+    __syncthreads();
+    // stage 3: R3-point DFTs over m1 for the pairs p = t + N1 q
+#pragma unroll
+    for (int q = 0; q < 16 / R3; ++q)
+#pragma unroll
+        for (int i = 0; i < R3; ++i) v[q * R3 + i] = sh[L::a2(c, t + N1 * q, i)];
+    if constexpr (R3 > 1) {
+#pragma unroll
+        for (int q = 0; q < 16 / R3; ++q) dftR<R3, DIR>(v + q * R3);
+    }
+}
+
+constexpr int kRowThreads = 512;  // threads per block of the row kernels
+constexpr int kColC = 4;          // columns per block of the column kernels
+
+// ---------------------------------------------------------------------------
+// Forward rows: deapodise, pad and modulate two rows of u (rows 2 pr, 2 pr+1
+// of image img), FFT as a + i b, split into the two half spectra and store
+// them at rows Y = y + n/2 of the halo-padded forward spectra, columns 0..n.
+// ---------------------------------------------------------------------------
+template <int N>
+__global__ void __launch_bounds__(kRowThreads, 2)
+    k_fft_rows_fwd(const float *__restrict__ u, float2 *__restrict__ spec, const float *__restrict__ dp,
+                   const float2 *__restrict__ tw, UsGeo g, float inv4n2) {
+    constexpr int N1 = N / 16, RP = kRowThreads / N1;
+    using L = FftLayout<N, false, RP>;
+    extern __shared__ float2 fft_sh[];
+    const int n = N / 2;
+    const int t = threadIdx.x % N1, c = threadIdx.x / N1;
+    const int pr = blockIdx.x * RP + c;  // row pair
+    const long long img = blockIdx.y;
+    const bool ok = pr < n / 2;
+    const int ya = 2 * pr, yb = ya + 1;
+    float2 v[16];
+    {
+        const float *ua = u + (img * n + (ok ? ya : 0)) * (long long)n;
+        const float *ub = ua + n;
+        const int Ya = ya + n / 2;
+        const float sa = ok ? ((Ya & 1) ? -dp[ya] : dp[ya]) * inv4n2 : 0.f;
+        const float sb = ok ? ((Ya & 1) ? dp[yb] : -dp[yb]) * inv4n2 : 0.f;
+#pragma unroll
+        for (int r = 0; r < 16; ++r) {
+            v[r] = make_float2(0.f, 0.f);
+            if (r >= 4 && r < 12) {  // X = t + N1 r in [n/2, 3n/2)
+                const int x = t + N1 * (r - 4), X = x + n / 2;
+                const float w = (X & 1) ? -__ldg(dp + x) : __ldg(dp + x);
+                v[r] = make_float2(__ldg(ua + x) * w * sa, __ldg(ub + x) * w * sb);
+            }
+        }
+    }
+    fft_core<N, -1, L>(v, fft_sh, c, t, tw);
+    // Z in natural order, then A(k) = (Z(k) + conj Z(-k))/2, B(k) = (Z(k) - conj Z(-k))/(2i)
+    __syncthreads();
+#pragma unroll
+    for (int q = 0; q < 16 / L::R3; ++q)
+#pragma unroll
+        for (int j1 = 0; j1 < L::R3; ++j1) fft_sh[c * L::S + t + N1 * q + 256 * j1] = v[q * L::R3 + j1];
+    __syncthreads();
+    if (!ok) return;
+    float2 *ra = spec + img * g.img_fwd + g.qoff + (long long)(ya + n / 2) * g.qp;
+    float2 *rb = ra + g.qp;
+    for (int k = t; k <= n; k += N1) {
+        const float2 zk = fft_sh[c * L::S + k], zm = fft_sh[c * L::S + ((N - k) & (N - 1))];
+        ra[k] = make_float2(0.5f * (zk.x + zm.x), 0.5f * (zk.y - zm.y));
+        rb[k] = make_float2(0.5f * (zk.y + zm.y), 0.5f * (zm.x - zk.x));
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Forward columns: columns kx of the row pass output (rows [n/2, 3n/2), the
+// others are zero), P-point FFT, all P rows written back in place.
+// ---------------------------------------------------------------------------
+template <int N>
+__global__ void __launch_bounds__(kColC *(N / 16), (N <= 2048) ? 2 : 1)
+    k_fft_cols_fwd(float2 *__restrict__ spec, const float2 *__restrict__ tw, UsGeo g) {
+    constexpr int N1 = N / 16;
+    using L = FftLayout<N, true, kColC>;
+    extern __shared__ float2 fft_sh[];
+    const int n = N / 2;
+    const int c = threadIdx.x % kColC, t = threadIdx.x / kColC;
+    const int kx = blockIdx.x * kColC + c;
+    const bool ok = kx <= n;
+    float2 *col = spec + (long long)blockIdx.y * g.img_fwd + g.qoff + (ok ? kx : 0);
+    float2 v[16];
+#pragma unroll
+    for (int r = 0; r < 16; ++r) {
+        v[r] = make_float2(0.f, 0.f);
+        if (r >= 4 && r < 12 && ok) v[r] = col[(long long)(t + N1 * r) * g.qp];
+    }
+    fft_core<N, -1, L>(v, fft_sh, c, t, tw);
+    if (!ok) return;
+#pragma unroll
+    for (int q = 0; q < 16 / L::R3; ++q)
+#pragma unroll
+        for (int j1 = 0; j1 < L::R3; ++j1) col[(long long)(t + N1 * q + 256 * j1) * g.qp] = v[q * L::R3 + j1];
+}
+
+// ---------------------------------------------------------------------------
+// Adjoint columns: inverse P-point FFT of columns 0..n of the Hermitian half
+// planes [img][P][P/2+1]; only rows [n/2, 3n/2) are written back.
+// ---------------------------------------------------------------------------
+template <int N>
+__global__ void __launch_bounds__(kColC *(N / 16), (N <= 2048) ? 2 : 1)
+    k_fft_cols_inv(float2 *__restrict__ spec, const float2 *__restrict__ tw) {
+    constexpr int N1 = N / 16;
+    using L = FftLayout<N, true, kColC>;
+    extern __shared__ float2 fft_sh[];
+    const int n = N / 2, hp = n + 1;
+    const int c = threadIdx.x % kColC, t = threadIdx.x / kColC;
+    const int kx = blockIdx.x * kColC + c;
+    const bool ok = kx <= n;
+    float2 *col = spec + (long long)blockIdx.y * N * hp + (ok ? kx : 0);
+    float2 v[16];
+#pragma unroll
+    for (int r = 0; r < 16; ++r) v[r] = ok ? col[(long long)(t + N1 * r) * hp] : make_float2(0.f, 0.f);
+    fft_core<N, 1, L>(v, fft_sh, c, t, tw);
+    if (!ok) return;
+#pragma unroll
+    for (int q = 0; q < 16 / L::R3; ++q)
+#pragma unroll
+        for (int j1 = 0; j1 < L::R3; ++j1) {
+            const int Y = t + N1 * q + 256 * j1;
+            if (Y >= n / 2 && Y < n / 2 + n) col[(long long)Y * hp] = v[q * L::R3 + j1];
+        }
+}
+
+// ---------------------------------------------------------------------------
+// Adjoint rows: rows Ya = n/2 + 2 pr and Ya + 1 of the column pass output,
+// Hermitian-extended to P points, one inverse FFT as A + i B; the centre
+// outputs X in [n/2, 3n/2) are modulated, deapodised, scaled by c and added
+// into rows 2 pr, 2 pr + 1 of u.
+// ---------------------------------------------------------------------------
+template <int N>
+__global__ void __launch_bounds__(kRowThreads, 2)
+    k_fft_rows_inv(const float2 *__restrict__ spec, float *__restrict__ u, const float *__restrict__ dp,
+                   const float2 *__restrict__ tw, float cscale) {
+    constexpr int N1 = N / 16, RP = kRowThreads / N1;
+    using L = FftLayout<N, false, RP>;
+    extern __shared__ float2 fft_sh[];
+    const int n = N / 2, hp = n + 1;
+    const int t = threadIdx.x % N1, c = threadIdx.x / N1;
+    const int pr = blockIdx.x * RP + c;
+    const long long img = blockIdx.y;
+    const bool ok = pr < n / 2;
+    const int ya = 2 * pr, yb = ya + 1, Ya = ya + n / 2;
+    const float2 *ha = spec + img * N * hp + (long long)(ok ? Ya : n / 2) * hp;
+    const float2 *hb = ha + hp;
+    float2 v[16];
+#pragma unroll
+    for (int r = 0; r < 16; ++r) {
+        const int k = t + N1 * r;
+        float2 a, b;
+        if (k <= n) {
+            a = ha[k];
+            b = hb[k];
+            if (k == 0 || k == n) a.y = b.y = 0.f;
+        } else {
+            a = conj_(ha[N - k]);
+            b = conj_(hb[N - k]);
+        }
+        v[r] = make_float2(a.x - b.y, a.y + b.x);  // A + i B
+    }
+    fft_core<N, 1, L>(v, fft_sh, c, t, tw);
+    if (!ok) return;
+    float *ua = u + (img * n + ya) * (long long)n;
+    float *ub = ua + n;
+    const float sa = ((Ya & 1) ? -dp[ya] : dp[ya]) * cscale;
+    const float sb = ((Ya & 1) ? dp[yb] : -dp[yb]) * cscale;
+#pragma unroll
+    for (int q = 0; q < 16 / L::R3; ++q)
+#pragma unroll
+        for (int j1 = 0; j1 < L::R3; ++j1) {
+            const int X = t + N1 * q + 256 * j1;
+            const int x = X - n / 2;
+            if (x >= 0 && x < n) {
+                const float w = (X & 1) ? -__ldg(dp + x) : __ldg(dp + x);
+                const float2 z = v[q * L::R3 + j1];
+                ua[x] += z.x * w * sa;
+                ub[x] += z.y * w * sb;
+            }
+        }
+}
+
+template <int N>
+size_t rows_smem() {
+    return sizeof(float2) * (size_t)FftLayout<N, false, kRowThreads / (N / 16)>::S * (kRowThreads / (N / 16));
+}
+template <int N>
+size_t cols_smem() {
+    return sizeof(float2) * (size_t)FftLayout<N, true, kColC>::S * kColC;
+}
+
+template <int N>
+void set_attrs_n() {
+    CUDA_CHECK(cudaFuncSetAttribute(k_fft_rows_fwd<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)rows_smem<N>()));
+    CUDA_CHECK(cudaFuncSetAttribute(k_fft_rows_inv<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)rows_smem<N>()));
+    CUDA_CHECK(cudaFuncSetAttribute(k_fft_cols_fwd<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)cols_smem<N>()));
+    CUDA_CHECK(cudaFuncSetAttribute(k_fft_cols_inv<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)cols_smem<N>()));
+}
+
+template <int N>
+void fwd_n(const float *u, float2 *spec, int nimg, const float *deapod, const float2 *tw, const UsGeo &g,
+           cudaStream_t s) {
+    constexpr int N1 = N / 16, RP = kRowThreads / N1;
+    const int n = N / 2;
+    const float inv4n2 = (float)(1.0 / (4.0 * n * (double)n));
+    dim3 gr((n / 2 + RP - 1) / RP, nimg);
+    k_fft_rows_fwd<N><<<gr, kRowThreads, rows_smem<N>(), s>>>(u, spec, deapod, tw, g, inv4n2);
+    LAUNCH_CHECK("k_fft_rows_fwd");
+    dim3 gc((n + 1 + kColC - 1) / kColC, nimg);
+    k_fft_cols_fwd<N><<<gc, kColC * N1, cols_smem<N>(), s>>>(spec, tw, g);
+    LAUNCH_CHECK("k_fft_cols_fwd");
+}
+
+template <int N>
+void inv_n(float2 *spec, float *u, int nimg, float cscale, const float *deapod, const float2 *tw, cudaStream_t s) {
+    constexpr int N1 = N / 16, RP = kRowThreads / N1;
+    const int n = N / 2;
+    dim3 gc((n + 1 + kColC - 1) / kColC, nimg);
+    k_fft_cols_inv<N><<<gc, kColC * N1, cols_smem<N>(), s>>>(spec, tw);
+    LAUNCH_CHECK("k_fft_cols_inv");
+    dim3 gr((n / 2 + RP - 1) / RP, nimg);
+    k_fft_rows_inv<N><<<gr, kRowThreads, rows_smem<N>(), s>>>(spec, u, deapod, tw, cscale);
+    LAUNCH_CHECK("k_fft_rows_inv");
+}
+
+}  // namespace
+
+bool pad_fft_supported(int P) { return P >= 256 && P <= 4096 && (P & (P - 1)) == 0; }
+
+void pad_fft_prepare() {
+    set_attrs_n<256>();
+    set_attrs_n<512>();
+    set_attrs_n<1024>();
+    set_attrs_n<2048>();
+    set_attrs_n<4096>();
+}
+
+std::vector<float2> pad_fft_twiddles(int P) {
+    std::vector<float2> w(P);
+    const double pi = 3.14159265358979323846;
+    for (int k = 0; k < P; ++k) {
+        const double a = -2.0 * pi * (double)k / (double)P;
+        w[k] = make_float2((float)std::cos(a), (float)std::sin(a));
+    }
+    return w;
+}
+
+void launch_pad_fft_fwd(const float *u, float2 *spec, int nimg, const float *deapod, const float2 *tw,
+                        const UsGeo &g, cudaStream_t s) {
+    if (nimg > 65535) throw Error(1, "pad FFT: too many images per batch");
+    switch (g.P) {
+        case 256: fwd_n<256>(u, spec, nimg, deapod, tw, g, s); break;
+        case 512: fwd_n<512>(u, spec, nimg, deapod, tw, g, s); break;
+        case 1024: fwd_n<1024>(u, spec, nimg, deapod, tw, g, s); break;
+        case 2048: fwd_n<2048>(u, spec, nimg, deapod, tw, g, s); break;
+        case 4096: fwd_n<4096>(u, spec, nimg, deapod, tw, g, s); break;
+        default: throw Error(1, "pad FFT: unsupported grid size");
+    }
+}
+
+void launch_pad_fft_inv_accum(float2 *spec, float *u, int zb, float tau, const float *deapod, const float2 *tw,
+                              const UsGeo &g, cudaStream_t s) {
+    const int nimg = zb * g.m;
+    if (nimg > 65535) throw Error(1, "pad FFT: too many images per batch");
+    // the scale of the C2R path's crop (1/sqrt(n ntheta) / (4 n^2)) times tau
+    const double scale = 1.0 / std::sqrt((double)g.n * (double)g.ntheta);
+    const float c = (float)(tau * scale / (4.0 * g.n * (double)g.n));
+    switch (g.P) {
+        case 256: inv_n<256>(spec, u, nimg, c, deapod, tw, s); break;
+        case 512: inv_n<512>(spec, u, nimg, c, deapod, tw, s); break;
+        case 1024: inv_n<1024>(spec, u, nimg, c, deapod, tw, s); break;
+        case 2048: inv_n<2048>(spec, u, nimg, c, deapod, tw, s); break;
+        case 4096: inv_n<4096>(spec, u, nimg, c, deapod, tw, s); break;
+        default: throw Error(1, "pad FFT: unsupported grid size");
+    }
+}
+
+}  // namespace rectv

@@ -119,6 +119,10 @@ struct Handle {
     bool plans_made = false;
     int img_per_fft = 0;
     void *fft_work = nullptr;
+    // hand-written padded-grid FFTs (P a power of two in [256, 4096]) instead
+    // of cuFFT + deapodise/pad + crop passes; RECTV_CUFFT=1 selects cuFFT
+    bool pad_fft = false;
+    float2 *fft_tw = nullptr;  // [P] exp(-2 pi i k / P)
 
     // session
     bool session = false;
@@ -161,6 +165,7 @@ struct Handle {
         usfft_prepare();
         gather_tc_prepare();
         scatter_tc_prepare();
+        pad_fft_prepare();
         const int P = 2 * n;
         ug.n = n;
         ug.ntheta = ntheta;
@@ -226,6 +231,16 @@ struct Handle {
         gd.err = dalloc<int>(1, owned);
         CUDA_CHECK(cudaMemsetAsync(gd.err, 0, sizeof(int), stream));
         CUDA_CHECK(cudaMallocHost(&stats_host, sizeof(double) * 4));
+        {
+            const char *e = std::getenv("RECTV_CUFFT");
+            pad_fft = pad_fft_supported(P) && !(e && std::atoi(e) != 0);
+            if (pad_fft) {
+                const std::vector<float2> w = pad_fft_twiddles(P);
+                fft_tw = dalloc<float2>((size_t)P, owned);
+                CUDA_CHECK(cudaMemcpyAsync(fft_tw, w.data(), sizeof(float2) * P, cudaMemcpyHostToDevice, stream));
+                CUDA_CHECK(cudaStreamSynchronize(stream));
+            }
+        }
         make_fft_plans();
         CUDA_CHECK(cudaStreamSynchronize(stream));
     }
@@ -464,11 +479,15 @@ struct Handle {
     // ---- operators on one batch of zb slices ----
     // out = tau R_apr u  (residual: out = R_apr u - gb)
     void forward(const float *u, const float *gb, float *out, float tau, int residual) {
-        launch_deapod_pad(u, reinterpret_cast<float *>(spec), zb * m, gd.deapod, ug, stream);
         const int nimg = zb * m;
-        for (int i = 0; i < nimg; i += img_per_fft) {
-            cufftComplex *p = reinterpret_cast<cufftComplex *>(spec + (size_t)i * ug.img_fwd + ug.qoff);
-            CUFFT_CHECK(cufftExecR2C(p_r2c2d, reinterpret_cast<cufftReal *>(p), p));
+        if (pad_fft) {
+            launch_pad_fft_fwd(u, spec, nimg, gd.deapod, fft_tw, ug, stream);
+        } else {
+            launch_deapod_pad(u, reinterpret_cast<float *>(spec), nimg, gd.deapod, ug, stream);
+            for (int i = 0; i < nimg; i += img_per_fft) {
+                cufftComplex *p = reinterpret_cast<cufftComplex *>(spec + (size_t)i * ug.img_fwd + ug.qoff);
+                CUFFT_CHECK(cufftExecR2C(p_r2c2d, reinterpret_cast<cufftReal *>(p), p));
+            }
         }
         launch_spec_halo(spec, nimg, ug, stream);
         launch_gather_fwd(spec, rows, zb, gd, ug, &spec_tmap, stream);
@@ -490,6 +509,10 @@ struct Handle {
             const long long img_half = (long long)ug.P * (ug.P / 2 + 1);
             CUDA_CHECK(cudaMemsetAsync(spec, 0, sizeof(float2) * (size_t)nimg * img_half, stream));
             launch_scatter_adj(rows, spec, zb, gd, ug, stream);
+            if (pad_fft) {
+                launch_pad_fft_inv_accum(spec, u, zb, tau, gd.deapod, fft_tw, ug, stream);
+                return;
+            }
             for (int i = 0; i < nimg; i += img_per_fft) {
                 cufftComplex *p = reinterpret_cast<cufftComplex *>(spec + (size_t)i * img_half);
                 CUFFT_CHECK(cufftExecC2R(p_c2r2d, p, reinterpret_cast<cufftReal *>(p)));
@@ -760,8 +783,11 @@ struct Handle {
     void launch_counts(int *kern, int *ffts) const {
         const int nimg = zb * m;
         const int f2 = (nimg + img_per_fft - 1) / img_per_fft;
-        const int fwd_k = 3 + jgroups(), fwd_f = f2 + 1;
-        const int adj_k = 2 + (gd.n_split_tiles > 0 ? 1 : 0) + jgroups(), adj_f = 1 + f2;
+        // the padded-grid FFTs replace deapodise/pad (crop) and the 2D cuFFT
+        // executions by a row and a column kernel each
+        const bool own2d = pad_fft && gd.tc_scatter;
+        const int fwd_k = (pad_fft ? 4 : 3) + jgroups(), fwd_f = (pad_fft ? 0 : f2) + 1;
+        const int adj_k = (own2d ? 3 : 2) + (gd.n_split_tiles > 0 ? 1 : 0) + jgroups(), adj_f = 1 + (own2d ? 0 : f2);
         *kern = titer * nbatch * (fwd_k + 1 + adj_k) + nbatch + 1;
         *ffts = titer * nbatch * (fwd_f + adj_f);
     }

@@ -145,6 +145,17 @@ void launch_scatter_tc(const float2 *rowsc, float2 *spec, int zb, const GeoDev &
                        cudaStream_t s);
 void scatter_tc_prepare();
 void launch_adj_records(AdjRec *recs, const GeoDev &gd, const UsGeo &g, cudaStream_t s);
+// hand-written 2D FFTs of the zero-padded grids (fft_kernels.cu), P = 2n a
+// power of two in [256, 4096]: forward = deapodise/pad/modulate + R2C into
+// the halo-padded spectra (halo not filled); inverse = C2R of the Hermitian
+// half planes [img][P][P/2+1] (overwritten) + crop/deapodise, u += tau * ...
+bool pad_fft_supported(int P);
+void pad_fft_prepare();
+std::vector<float2> pad_fft_twiddles(int P);
+void launch_pad_fft_fwd(const float *u, float2 *spec, int nimg, const float *deapod, const float2 *tw,
+                        const UsGeo &g, cudaStream_t s);
+void launch_pad_fft_inv_accum(float2 *spec, float *u, int zb, float tau, const float *deapod, const float2 *tw,
+                              const UsGeo &g, cudaStream_t s);
 size_t gather_tc_smem();
 int gather_tc_table_capacity();
 size_t gather_fwd_smem(const UsGeo &g);
