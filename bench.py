@@ -37,8 +37,20 @@ SMALL = dict(n=256, nz=16, nzp=8, ntheta=720, nrot=8, m=16, titer=4, lambda0=1e-
 METRIC = "ADMM iters/s (outer iterations, titer=4) of the 4D TV reconstruction"
 # launch groups timed by rectv_launch_kernel: 0 = forward gather (k_gather_tc, plus
 # k_gather_fwd for the few items near the centre of the spectrum), 1 = adjoint
-# scatter (k_scatter_tc), 2 = fused inner TV step, 3 = shrink / dual update
-KERNEL_NAMES = {0: "k_gather_tc", 1: "k_scatter_tc", 2: "k_graddiv", 3: "k_shrink"}
+# scatter (k_scatter_tc), 2 = fused inner TV step, 3 = shrink / dual update,
+# 4 / 5 = forward / inverse padded-grid 2D FFT (when 2n is a power of two)
+KERNEL_NAMES = {0: "k_gather_tc", 1: "k_scatter_tc", 2: "k_graddiv", 3: "k_shrink",
+                4: "k_fft_rows_fwd+k_fft_cols_fwd", 5: "k_fft_cols_inv+k_fft_rows_inv"}
+
+
+def workload_of(args):
+    """The timed workload; --nz/--nzp override the slice counts (small cases for ncu captures)."""
+    w = dict(SMALL if args.small else WORKLOAD)
+    if getattr(args, "nz", None):
+        w["nz"] = args.nz
+    if getattr(args, "nzp", None):
+        w["nzp"] = args.nzp
+    return w
 
 
 def workload_name(w):
@@ -235,7 +247,7 @@ def run_reference_arm(args, rank):
     reference has no CPU path and its CUDA build cannot travel) on host cores."""
     if rank != 0:
         return 0
-    w = SMALL if args.small else WORKLOAD
+    w = workload_of(args)
     for _ in range(args.warmup):
         cpu_sample(w)
     vals, secs = [], 0.0
@@ -275,7 +287,7 @@ def run_ours(args, rank, world, local_rank):
         import torch.distributed as dist
         dist.init_process_group("nccl", device_id=dev)
 
-    w = SMALL if args.small else WORKLOAD
+    w = workload_of(args)
     n, nz, nzp, ntheta, m, titer = w["n"], w["nz"], w["nzp"], w["ntheta"], w["m"], w["titer"]
     lam0, lam1 = w["lambda0"] * w["lambda1"], w["lambda1"]
     center = n / 2
@@ -332,7 +344,8 @@ def run_ours(args, rank, world, local_rank):
     import ctypes
     reps = 3
     ktimes = {}
-    for kid in (0, 1, 2, 3):
+    kids = (0, 1, 2, 3, 4, 5) if lib.rectv_launch_kernel(obj._h, 4, 0) == 0 else (0, 1, 2, 3)
+    for kid in kids:
         lib.rectv_launch_kernel(obj._h, kid, 1)  # warm
         a = torch.cuda.Event(enable_timing=True)
         b = torch.cuda.Event(enable_timing=True)
@@ -344,8 +357,7 @@ def run_ours(args, rank, world, local_rank):
         ktimes[kid] = a.elapsed_time(b) / reps
     # launches per outer iteration of each kernel: titer*nbatch (0,1,2), nbatch (3)
     nbatch = nz // zbs[0].value if zbs[0].value else 1
-    share = {0: titer * nbatch * ktimes[0], 1: titer * nbatch * ktimes[1], 2: titer * nbatch * ktimes[2],
-             3: nbatch * ktimes[3]}
+    share = {k: (nbatch if k == 3 else titer * nbatch) * ktimes[k] for k in ktimes}
     dom = max(share, key=share.get)
     bytes_ = ctypes.c_double()
     flops = ctypes.c_double()
@@ -358,7 +370,8 @@ def run_ours(args, rank, world, local_rank):
                         "2x the algorithmic bytes (atomic adds read back the Hermitian half planes)",
         "k_gather_tc": "shared-memory bandwidth of the per-sample 81-tap sums and of the TMEM -> shared "
                        "read-out of G, block barriers; TMA-staged footprints, DRAM traffic about the spectra",
-        "k_graddiv": "HBM bandwidth", "k_shrink": "HBM bandwidth"}[KERNEL_NAMES[dom]]
+        "k_graddiv": "HBM bandwidth", "k_shrink": "HBM bandwidth",
+        KERNEL_NAMES[4]: "HBM bandwidth", KERNEL_NAMES[5]: "HBM bandwidth"}[KERNEL_NAMES[dom]]
     roofline = {"bound": "hbm", "limiter": limiter, "kernel": KERNEL_NAMES[dom], "achieved": achieved,
                 "peak": peak,
                 "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / peak,
@@ -434,6 +447,8 @@ def main():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--small", action="store_true", help="N=256 workload (quick check)")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
+    ap.add_argument("--nz", type=int, default=None, help="slices (default: the workload's); for small ncu cases")
+    ap.add_argument("--nzp", type=int, default=None, help="slices per chunk (default: the workload's)")
     args = ap.parse_args()
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))

@@ -23,8 +23,11 @@
 // Every transform is P = 16 x 16 x R3 points (R3 = P/256) computed by P/16
 // threads holding 16 values each: a 16-point DFT in registers, twiddles,
 // exchange through shared memory, a 16-point DFT, twiddles, exchange, and
-// R3-point DFTs.  Twiddles come from a table of exp(-2 pi i k/P) evaluated in
-// double precision on the host.  Results equal cuFFT's to FP32 rounding.
+// R3-point DFTs.  Twiddles come from a table evaluated in double precision on
+// the host, laid out so that the lanes of a warp read consecutive entries:
+// [k2][n1] = exp(-2 pi i n1 k2 / P) for stage 1, then [j2][m1] =
+// exp(-2 pi i 16 m1 j2 / P) for stage 2.  Results equal cuFFT's to FP32
+// rounding.
 #include <cuda_runtime.h>
 
 #include <cmath>
@@ -182,7 +185,7 @@ __device__ __forceinline__ void fft_core(float2 *v, float2 *sh, int c, int t, co
     // stage 1: 16-point DFT over n2 of x[n1 + N1 n2], twiddle omega_N^(n1 k2)
     dft16<DIR>(v);
 #pragma unroll
-    for (int k2 = 1; k2 < 16; ++k2) v[k2] = cmul_(v[k2], twiddle(tw, (t * k2) & (N - 1), DIR));
+    for (int k2 = 1; k2 < 16; ++k2) v[k2] = cmul_(v[k2], twiddle(tw, k2 * N1 + t, DIR));
 #pragma unroll
     for (int k2 = 0; k2 < 16; ++k2) sh[L::a1(c, k2 * L::P1 + t)] = v[k2];
     __syncthreads();
@@ -193,7 +196,7 @@ __device__ __forceinline__ void fft_core(float2 *v, float2 *sh, int c, int t, co
     __syncthreads();
     dft16<DIR>(v);
 #pragma unroll
-    for (int j2 = 1; j2 < 16; ++j2) v[j2] = cmul_(v[j2], twiddle(tw, (16 * m1 * j2) & (N - 1), DIR));
+    for (int j2 = 1; j2 < 16; ++j2) v[j2] = cmul_(v[j2], twiddle(tw, N + j2 * R3 + m1, DIR));
 #pragma unroll
     for (int j2 = 0; j2 < 16; ++j2) sh[L::a2(c, k2 + 16 * j2, m1)] = v[j2];
     __syncthreads();
@@ -435,12 +438,17 @@ void pad_fft_prepare() {
 }
 
 std::vector<float2> pad_fft_twiddles(int P) {
-    std::vector<float2> w(P);
+    const int N1 = P / 16, R3 = P / 256;
+    std::vector<float2> w((size_t)P + 16 * R3);
     const double pi = 3.14159265358979323846;
-    for (int k = 0; k < P; ++k) {
-        const double a = -2.0 * pi * (double)k / (double)P;
-        w[k] = make_float2((float)std::cos(a), (float)std::sin(a));
-    }
+    auto cis = [&](long long e) {
+        const double a = -2.0 * pi * (double)(e % P) / (double)P;
+        return make_float2((float)std::cos(a), (float)std::sin(a));
+    };
+    for (int k2 = 0; k2 < 16; ++k2)
+        for (int t = 0; t < N1; ++t) w[(size_t)k2 * N1 + t] = cis((long long)t * k2);
+    for (int j2 = 0; j2 < 16; ++j2)
+        for (int m1 = 0; m1 < R3; ++m1) w[(size_t)P + j2 * R3 + m1] = cis(16LL * m1 * j2);
     return w;
 }
 

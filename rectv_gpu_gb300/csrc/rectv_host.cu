@@ -236,8 +236,9 @@ struct Handle {
             pad_fft = pad_fft_supported(P) && !(e && std::atoi(e) != 0);
             if (pad_fft) {
                 const std::vector<float2> w = pad_fft_twiddles(P);
-                fft_tw = dalloc<float2>((size_t)P, owned);
-                CUDA_CHECK(cudaMemcpyAsync(fft_tw, w.data(), sizeof(float2) * P, cudaMemcpyHostToDevice, stream));
+                fft_tw = dalloc<float2>(w.size(), owned);
+                CUDA_CHECK(cudaMemcpyAsync(fft_tw, w.data(), sizeof(float2) * w.size(), cudaMemcpyHostToDevice,
+                                           stream));
                 CUDA_CHECK(cudaStreamSynchronize(stream));
             }
         }
@@ -810,16 +811,30 @@ struct Handle {
                 *bytes = (double)zb * slab * 8.0 + 2.0 * 4.0 * dpb * gp * 4.0;
                 *flops = (double)zb * slab * 60.0;
                 break;
-            default:  // shrink: u_cur, u_old in, mu in, psi and mu out
+            case 3:  // shrink: u_cur, u_old in, mu in, psi and mu out
                 *bytes = (double)zb * slab * 8.0 + 3.0 * 4.0 * dpb * gp * 4.0;
                 *flops = (double)dpb * gp * 80.0;
                 break;
+            case 4:    // padded forward FFT: u in; half rows of the n centre rows out, in again; P rows out
+            case 5: {  // padded inverse FFT: P rows in; n centre rows out, in again; u read and written
+                const double nimg = (double)zb * m, hp = (double)n + 1.0;
+                const double half_rows = (double)n * hp * 8.0;
+                *bytes = which == 4 ? nimg * (4.0 * n * n + 2.0 * half_rows + P * hp * 8.0)
+                                    : nimg * (P * hp * 8.0 + 2.0 * half_rows + 8.0 * n * n);
+                // 5 P log2 P flops per complex P-point transform: n/2 row pairs and n+1 columns
+                *flops = nimg * (n / 2 + n + 1) * 5.0 * P * std::log2(P);
+                break;
+            }
+            default:
+                throw Error(RECTV_ERR_ARG, "rectv_kernel_cost: unknown kernel id");
         }
     }
 
     void launch_kernel(int which, int reps) {
         check_live();
         if (!session) throw Error(RECTV_ERR_STATE, "rectv_launch_kernel: needs a set-up session");
+        if (which < 0 || which > 5) throw Error(RECTV_ERR_ARG, "rectv_launch_kernel: unknown kernel id");
+        if (which >= 4 && !pad_fft) throw Error(RECTV_ERR_ARG, "rectv_launch_kernel: no padded-grid FFT at this size");
         for (int r = 0; r < reps; ++r) {
             switch (which) {
                 case 0: launch_gather_fwd(spec, rows, zb, gd, ug, &spec_tmap, stream); break;
@@ -827,6 +842,12 @@ struct Handle {
                 case 2: launch_graddiv(U[cur], U[cur], U[(cur + 1) % 3], psi, mu, rho_d, 0, nchunks, tv, stream); break;
                 case 3:  // overwrites the session's dual variables
                     launch_shrink(U[cur], U[cur], psi, mu, rho_d, lambda0, 0, nchunks, tv, partials, stream);
+                    break;
+                case 4:  // padded-grid forward FFT of the batch (rows + columns)
+                    launch_pad_fft_fwd(U[cur], spec, zb * m, gd.deapod, fft_tw, ug, stream);
+                    break;
+                case 5:  // padded-grid inverse FFT (columns + rows), added into the scratch iterate
+                    launch_pad_fft_inv_accum(spec, U[(cur + 1) % 3], zb, 0.f, gd.deapod, fft_tw, ug, stream);
                     break;
                 default: throw Error(RECTV_ERR_ARG, "rectv_launch_kernel: unknown kernel id");
             }
