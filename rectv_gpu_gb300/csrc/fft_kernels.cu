@@ -212,7 +212,7 @@ __device__ __forceinline__ void fft_core(float2 *v, float2 *sh, int c, int t, co
 }
 
 constexpr int kRowThreads = 512;  // threads per block of the row kernels
-constexpr int kColC = 4;          // columns per block of the column kernels
+constexpr int kColC = 4;          // columns per block of the column kernels (32-byte row runs, two blocks per SM)
 
 // ---------------------------------------------------------------------------
 // Forward rows: deapodise, pad and modulate two rows of u (rows 2 pr, 2 pr+1
@@ -271,15 +271,15 @@ __global__ void __launch_bounds__(kRowThreads, 2)
 // Forward columns: columns kx of the row pass output (rows [n/2, 3n/2), the
 // others are zero), P-point FFT, all P rows written back in place.
 // ---------------------------------------------------------------------------
-template <int N>
-__global__ void __launch_bounds__(kColC *(N / 16), (N <= 2048) ? 2 : 1)
+template <int N, int C>
+__global__ void __launch_bounds__(C *(N / 16), (C * N <= 8192) ? 2 : 1)
     k_fft_cols_fwd(float2 *__restrict__ spec, const float2 *__restrict__ tw, UsGeo g) {
     constexpr int N1 = N / 16;
-    using L = FftLayout<N, true, kColC>;
+    using L = FftLayout<N, true, C>;
     extern __shared__ float2 fft_sh[];
     const int n = N / 2;
-    const int c = threadIdx.x % kColC, t = threadIdx.x / kColC;
-    const int kx = blockIdx.x * kColC + c;
+    const int c = threadIdx.x % C, t = threadIdx.x / C;
+    const int kx = blockIdx.x * C + c;
     const bool ok = kx <= n;
     float2 *col = spec + (long long)blockIdx.y * g.img_fwd + g.qoff + (ok ? kx : 0);
     float2 v[16];
@@ -300,15 +300,15 @@ __global__ void __launch_bounds__(kColC *(N / 16), (N <= 2048) ? 2 : 1)
 // Adjoint columns: inverse P-point FFT of columns 0..n of the Hermitian half
 // planes [img][P][P/2+1]; only rows [n/2, 3n/2) are written back.
 // ---------------------------------------------------------------------------
-template <int N>
-__global__ void __launch_bounds__(kColC *(N / 16), (N <= 2048) ? 2 : 1)
+template <int N, int C>
+__global__ void __launch_bounds__(C *(N / 16), (C * N <= 8192) ? 2 : 1)
     k_fft_cols_inv(float2 *__restrict__ spec, const float2 *__restrict__ tw) {
     constexpr int N1 = N / 16;
-    using L = FftLayout<N, true, kColC>;
+    using L = FftLayout<N, true, C>;
     extern __shared__ float2 fft_sh[];
     const int n = N / 2, hp = n + 1;
-    const int c = threadIdx.x % kColC, t = threadIdx.x / kColC;
-    const int kx = blockIdx.x * kColC + c;
+    const int c = threadIdx.x % C, t = threadIdx.x / C;
+    const int kx = blockIdx.x * C + c;
     const bool ok = kx <= n;
     float2 *col = spec + (long long)blockIdx.y * N * hp + (ok ? kx : 0);
     float2 v[16];
@@ -386,17 +386,17 @@ template <int N>
 size_t rows_smem() {
     return sizeof(float2) * (size_t)FftLayout<N, false, kRowThreads / (N / 16)>::S * (kRowThreads / (N / 16));
 }
-template <int N>
+template <int N, int C>
 size_t cols_smem() {
-    return sizeof(float2) * (size_t)FftLayout<N, true, kColC>::S * kColC;
+    return sizeof(float2) * (size_t)FftLayout<N, true, C>::S * C;
 }
 
 template <int N>
 void set_attrs_n() {
     CUDA_CHECK(cudaFuncSetAttribute(k_fft_rows_fwd<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)rows_smem<N>()));
     CUDA_CHECK(cudaFuncSetAttribute(k_fft_rows_inv<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)rows_smem<N>()));
-    CUDA_CHECK(cudaFuncSetAttribute(k_fft_cols_fwd<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)cols_smem<N>()));
-    CUDA_CHECK(cudaFuncSetAttribute(k_fft_cols_inv<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)cols_smem<N>()));
+    CUDA_CHECK(cudaFuncSetAttribute(k_fft_cols_fwd<N, kColC>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)cols_smem<N, kColC>()));
+    CUDA_CHECK(cudaFuncSetAttribute(k_fft_cols_inv<N, kColC>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)cols_smem<N, kColC>()));
 }
 
 template <int N>
@@ -409,7 +409,7 @@ void fwd_n(const float *u, float2 *spec, int nimg, const float *deapod, const fl
     k_fft_rows_fwd<N><<<gr, kRowThreads, rows_smem<N>(), s>>>(u, spec, deapod, tw, g, inv4n2);
     LAUNCH_CHECK("k_fft_rows_fwd");
     dim3 gc((n + 1 + kColC - 1) / kColC, nimg);
-    k_fft_cols_fwd<N><<<gc, kColC * N1, cols_smem<N>(), s>>>(spec, tw, g);
+    k_fft_cols_fwd<N, kColC><<<gc, kColC * N1, cols_smem<N, kColC>(), s>>>(spec, tw, g);
     LAUNCH_CHECK("k_fft_cols_fwd");
 }
 
@@ -418,7 +418,7 @@ void inv_n(float2 *spec, float *u, int nimg, float cscale, const float *deapod, 
     constexpr int N1 = N / 16, RP = kRowThreads / N1;
     const int n = N / 2;
     dim3 gc((n + 1 + kColC - 1) / kColC, nimg);
-    k_fft_cols_inv<N><<<gc, kColC * N1, cols_smem<N>(), s>>>(spec, tw);
+    k_fft_cols_inv<N, kColC><<<gc, kColC * N1, cols_smem<N, kColC>(), s>>>(spec, tw);
     LAUNCH_CHECK("k_fft_cols_inv");
     dim3 gr((n / 2 + RP - 1) / RP, nimg);
     k_fft_rows_inv<N><<<gr, kRowThreads, rows_smem<N>(), s>>>(spec, u, deapod, tw, cscale);
