@@ -59,69 +59,104 @@ __device__ __forceinline__ void block_reduce3(double a, double b, double c, doub
 // Fused inner step (gradient, lin4, divergent of admm.cu:85-95 with tau=-0.5):
 //   u_out(v) = u_in(v) + tau sd sum_d [h_d(q-e_d) - h_d(q)],  q = v+1,
 //   h = rho (G u_in - psi) + mu.
-// One thread per voxel; blocks of 256x1 over (x, y), grid.z over (slice, t).
+// One thread per (x, y, slice), marching along t: h_t(q - e_t) is the previous
+// time point's h_t(q), kept in a register, and the loads of time point t+1
+// are issued before t is computed.  Blocks of 256 x-voxels; the grid runs
+// over (x blocks, slices, rows) in that order, so the blocks that read a
+// block's z-1 and y-1 dual neighbours run at the same time (L2 hits rather
+// than second HBM reads).  Every value is computed with the same float
+// expression as the per-voxel form, so results do not depend on the order.
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(256)
+__global__ void __launch_bounds__(256, 3)
     k_graddiv(const float *__restrict__ uin, const float *__restrict__ uold, float *__restrict__ uout,
               const float *__restrict__ psi, const float *__restrict__ mu, const float *__restrict__ rhop,
               TvGeo t, int c0, int nch_total, float tau) {
     const int x = blockIdx.x * blockDim.x + threadIdx.x;
-    const int y = blockIdx.y * blockDim.y + threadIdx.y;
-    const int pl = blockIdx.z;
-    const int tt = pl % t.m;
-    const int zr = pl / t.m;
-    if (x >= t.n || y >= t.n) return;
+    const int zr = blockIdx.y;
+    const int y = blockIdx.z;
+    if (x >= t.n) return;
     const int n = t.n, m = t.m, nzp = t.nzp;
     const int c = c0 + zr / nzp, zl = zr % nzp;
-    const long long slab = t.vol_slab;
-    const long long v = ((long long)c * nzp + zl) * slab + ((long long)tt * n + y) * n + x;
-    const float f0 = uin[v];
-    const float fxp = uin[v + (x < n - 1 ? 1 : 0)], fxm = uin[v - (x > 0 ? 1 : 0)];
-    const float fyp = uin[v + (y < n - 1 ? n : 0)], fym = uin[v - (y > 0 ? n : 0)];
-    const long long nn = (long long)n * n;
-    const float ftp = uin[v + (tt < m - 1 ? nn : 0)], ftm = uin[v - (tt > 0 ? nn : 0)];
-    float fzp, fzm;
-    if (zl < nzp - 1) fzp = uin[v + slab];
-    else fzp = (c < nch_total - 1) ? uold[v + slab] : f0;
-    if (zl > 0) fzm = uin[v - slab];
-    else fzm = (c > 0) ? uold[v - slab] : f0;
-
+    const long long slab = t.vol_slab, nn = (long long)n * n;
+    const long long v0 = ((long long)c * nzp + zl) * slab + (long long)y * n + x;  // voxel (x, y, t = 0)
+    const float *u = uin + v0;
+    // z neighbours: inside the chunk, else the previous outer iterate, else replicated
+    const float *uzp = (zl < nzp - 1) ? uin + v0 + slab : ((c < nch_total - 1) ? uold + v0 + slab : u);
+    const float *uzm = (zl > 0) ? uin + v0 - slab : ((c > 0) ? uold + v0 - slab : u);
+    const int dxp = x < n - 1 ? 1 : 0, dxm = x > 0 ? 1 : 0;
+    const int dyp = y < n - 1 ? n : 0, dym = y > 0 ? n : 0;
     const float rho = *rhop;
     const long long sx = 1, sy = n + 1, st = (long long)(n + 1) * (n + 1), sz = st * (m + 1);
-    const long long q = (long long)c * t.gp + (zl + 1) * sz + (tt + 1) * st + (y + 1) * sy + (x + 1);
     const long long cs = t.comp_stride;
-    const float sg = t.sg;
-    float d;
-    {  // x
-        const float hq = rho * (sg * (fxp - f0) - psi[q]) + mu[q];
-        const float hm = rho * (sg * (f0 - fxm) - psi[q - sx]) + mu[q - sx];
-        d = hm - hq;
+    const long long q0 = (long long)c * t.gp + (zl + 1) * sz + st + (y + 1) * sy + (x + 1);  // q of t = 0
+    const float sg = t.sg, sgt = t.sg * t.lambda1;
+    // a[]: u at x+1, x-1, y+1, y-1, z+1, z-1, t+1; psi, mu at q (4 components
+    // each); psi, mu of component x at q-sx, y at q-sy, z at q-sz
+    auto load = [&](int tt, float(&a)[21]) {
+        const long long o = (long long)tt * nn;
+        const long long q = q0 + (long long)tt * st;
+        a[0] = u[o + dxp];
+        a[1] = u[o - dxm];
+        a[2] = u[o + dyp];
+        a[3] = u[o - dym];
+        a[4] = uzp[o];
+        a[5] = uzm[o];
+        a[6] = u[o + (tt < m - 1 ? nn : 0)];
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+            a[7 + i] = psi[i * cs + q];
+            a[11 + i] = mu[i * cs + q];
+        }
+        a[15] = psi[q - sx];
+        a[16] = mu[q - sx];
+        a[17] = psi[cs + q - sy];
+        a[18] = mu[cs + q - sy];
+        a[19] = psi[3 * cs + q - sz];
+        a[20] = mu[3 * cs + q - sz];
+    };
+    float cur[21];
+    load(0, cur);
+    float f0 = u[0];
+    // h_t at q - st for t = 0: the clamped backward difference is zero
+    float hmt = rho * (sgt * (f0 - f0) - psi[2 * cs + q0 - st]) + mu[2 * cs + q0 - st];
+    for (int tt = 0; tt < m; ++tt) {
+        float nxt[21];
+        if (tt + 1 < m) load(tt + 1, nxt);
+        float d;
+        {  // x
+            const float hq = rho * (sg * (cur[0] - f0) - cur[7]) + cur[11];
+            const float hm = rho * (sg * (f0 - cur[1]) - cur[15]) + cur[16];
+            d = hm - hq;
+        }
+        {  // y
+            const float hq = rho * (sg * (cur[2] - f0) - cur[8]) + cur[12];
+            const float hm = rho * (sg * (f0 - cur[3]) - cur[17]) + cur[18];
+            d += hm - hq;
+        }
+        {  // t (scaled by lambda1 in both gradient and divergence)
+            const float hq = rho * (sgt * (cur[6] - f0) - cur[9]) + cur[13];
+            d += t.lambda1 * (hmt - hq);
+            hmt = hq;
+        }
+        {  // z
+            const float hq = rho * (sg * (cur[4] - f0) - cur[10]) + cur[14];
+            const float hm = rho * (sg * (f0 - cur[5]) - cur[19]) + cur[20];
+            d += hm - hq;
+        }
+        uout[v0 + (long long)tt * nn] = f0 + tau * t.sd * d;
+        f0 = cur[6];  // u at t+1
+        if (tt + 1 < m) {
+#pragma unroll
+            for (int i = 0; i < 21; ++i) cur[i] = nxt[i];
+        }
     }
-    {  // y
-        const float hq = rho * (sg * (fyp - f0) - psi[cs + q]) + mu[cs + q];
-        const float hm = rho * (sg * (f0 - fym) - psi[cs + q - sy]) + mu[cs + q - sy];
-        d += hm - hq;
-    }
-    {  // t (scaled by lambda1 in both gradient and divergence)
-        const float sgt = sg * t.lambda1;
-        const float hq = rho * (sgt * (ftp - f0) - psi[2 * cs + q]) + mu[2 * cs + q];
-        const float hm = rho * (sgt * (f0 - ftm) - psi[2 * cs + q - st]) + mu[2 * cs + q - st];
-        d += t.lambda1 * (hm - hq);
-    }
-    {  // z
-        const float hq = rho * (sg * (fzp - f0) - psi[3 * cs + q]) + mu[3 * cs + q];
-        const float hm = rho * (sg * (f0 - fzm) - psi[3 * cs + q - sz]) + mu[3 * cs + q - sz];
-        d += hm - hq;
-    }
-    uout[v] = f0 + tau * t.sd * d;
 }
 
 void launch_graddiv(const float *u_in, const float *u_old, float *u_out, const float *psi,
                     const float *mu, const float *rho, int c0, int nchunks_total, const TvGeo &t,
                     cudaStream_t s) {
-    // one row of 256 voxels per block: each of the 17 input streams is read in
-    // 1 KB runs (DRAM page locality)
-    dim3 bs(256, 1), gs((t.n + 255) / 256, t.n, t.nchunks * t.nzp * t.m);
+    dim3 bs(256, 1), gs((t.n + 255) / 256, t.nchunks * t.nzp, t.n);
+    if (gs.y > 65535u || gs.z > 65535u) throw Error(1, "graddiv: grid too large");
     k_graddiv<<<gs, bs, 0, s>>>(u_in, u_old, u_out, psi, mu, rho, t, c0, nchunks_total, -0.5f);
     LAUNCH_CHECK("k_graddiv");
 }
