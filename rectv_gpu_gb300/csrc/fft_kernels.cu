@@ -28,12 +28,16 @@
 // [k2][n1] = exp(-2 pi i n1 k2 / P) for stage 1, then [j2][m1] =
 // exp(-2 pi i 16 m1 j2 / P) for stage 2.  Results equal cuFFT's to FP32
 // rounding.
+#include <cuda.h>
+#include <cudaTypedefs.h>
 #include <cuda_runtime.h>
 
 #include <cmath>
+#include <string>
 #include <vector>
 
 #include "rectv_internal.cuh"
+#include "tcgen05.cuh"
 
 namespace rectv {
 
@@ -267,66 +271,131 @@ __global__ void __launch_bounds__(kRowThreads, 2)
     }
 }
 
+// TMA tile copies of the column kernels: boxes of 4 columns (8 floats) x BR
+// rows of one image, landing in shared memory as [row][column].
+__device__ __forceinline__ void tma_load3(void *dst, const CUtensorMap *map, int x, int y, int z, void *bar) {
+    asm volatile(
+        "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], "
+        "[%5];\n" ::"r"(tc::smem_addr(dst)),
+        "l"((unsigned long long)map), "r"(x), "r"(y), "r"(z), "r"(tc::smem_addr(bar))
+        : "memory");
+}
+__device__ __forceinline__ void tma_store3(const CUtensorMap *map, int x, int y, int z, const void *src) {
+    asm volatile("cp.async.bulk.tensor.3d.global.shared::cta.tile.bulk_group [%0, {%1, %2, %3}], [%4];\n" ::"l"(
+                     (unsigned long long)map),
+                 "r"(x), "r"(y), "r"(z), "r"(tc::smem_addr(src))
+                 : "memory");
+}
+__device__ __forceinline__ void tma_store_drain() {
+    asm volatile("cp.async.bulk.commit_group;\ncp.async.bulk.wait_group.read 0;\n" ::: "memory");
+}
+__device__ __forceinline__ void mbar_expect(void *bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(tc::smem_addr(bar)), "r"(bytes)
+                 : "memory");
+}
+
+template <int N>
+struct ColTile {
+    static constexpr int n = N / 2;
+    static constexpr int BR = n < 256 ? n : 256;  // rows per TMA box
+};
+
 // ---------------------------------------------------------------------------
-// Forward columns: columns kx of the row pass output (rows [n/2, 3n/2), the
-// others are zero), P-point FFT, all P rows written back in place.
+// Forward columns: columns kx0 .. kx0+3 of the row pass output (rows
+// [n/2, 3n/2); the others are zero and not read), P-point FFT, all P rows
+// written back in place.  Tiles in and out by TMA (window coordinates of the
+// halo-padded spectra: x = 2 (kHalo + kx) floats, y = kHalo + row); columns
+// past n are halo cells, rewritten by the halo pass afterwards.
 // ---------------------------------------------------------------------------
 template <int N, int C>
 __global__ void __launch_bounds__(C *(N / 16), (C * N <= 8192) ? 2 : 1)
-    k_fft_cols_fwd(float2 *__restrict__ spec, const float2 *__restrict__ tw, UsGeo g) {
-    constexpr int N1 = N / 16;
+    k_fft_cols_fwd(const __grid_constant__ CUtensorMap tmap, const float2 *__restrict__ tw, int *__restrict__ err) {
+    constexpr int N1 = N / 16, n = N / 2, BR = ColTile<N>::BR;
     using L = FftLayout<N, true, C>;
-    extern __shared__ float2 fft_sh[];
-    const int n = N / 2;
+    extern __shared__ __align__(1024) float2 fft_sh[];
+    __shared__ uint64_t bar;
     const int c = threadIdx.x % C, t = threadIdx.x / C;
-    const int kx = blockIdx.x * C + c;
-    const bool ok = kx <= n;
-    float2 *col = spec + (long long)blockIdx.y * g.img_fwd + g.qoff + (ok ? kx : 0);
+    const int x = 2 * (kHalo + blockIdx.x * C), img = blockIdx.y;
+    if (threadIdx.x == 0) {
+        tc::mbar_init(&bar, 1);
+        tc::fence_mbar_init();
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        mbar_expect(&bar, (uint32_t)(n * C * sizeof(float2)));
+        for (int i = 0; i < n / BR; ++i) tma_load3(fft_sh + i * BR * C, &tmap, x, kHalo + n / 2 + i * BR, img, &bar);
+    }
+    const bool ok = tc::mbar_wait(&bar, 0u);
     float2 v[16];
 #pragma unroll
-    for (int r = 0; r < 16; ++r) {
-        v[r] = make_float2(0.f, 0.f);
-        if (r >= 4 && r < 12 && ok) v[r] = col[(long long)(t + N1 * r) * g.qp];
-    }
+    for (int r = 0; r < 16; ++r)
+        v[r] = (r >= 4 && r < 12) ? fft_sh[(t + N1 * r - n / 2) * C + c] : make_float2(0.f, 0.f);
+    __syncthreads();  // the exchange buffer reuses the landing tile
     fft_core<N, -1, L>(v, fft_sh, c, t, tw);
-    if (!ok) return;
+    __syncthreads();
 #pragma unroll
     for (int q = 0; q < 16 / L::R3; ++q)
 #pragma unroll
-        for (int j1 = 0; j1 < L::R3; ++j1) col[(long long)(t + N1 * q + 256 * j1) * g.qp] = v[q * L::R3 + j1];
+        for (int j1 = 0; j1 < L::R3; ++j1) fft_sh[(t + N1 * q + 256 * j1) * C + c] = v[q * L::R3 + j1];
+    tc::fence_proxy_async();
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        for (int i = 0; i < N / BR; ++i) tma_store3(&tmap, x, kHalo + i * BR, img, fft_sh + i * BR * C);
+        tma_store_drain();
+        if (!ok) atomicAdd(err, 1);
+    }
 }
 
 // ---------------------------------------------------------------------------
-// Adjoint columns: inverse P-point FFT of columns 0..n of the Hermitian half
-// planes [img][P][P/2+1]; only rows [n/2, 3n/2) are written back.
+// Adjoint columns: inverse P-point FFT of columns kx0 .. kx0+3 of the
+// Hermitian half planes [img][P][hpitch]; only rows [n/2, 3n/2) are written
+// back.  Tiles in and out by TMA; columns past the row pitch read as zeros
+// and are not stored.
 // ---------------------------------------------------------------------------
 template <int N, int C>
 __global__ void __launch_bounds__(C *(N / 16), (C * N <= 8192) ? 2 : 1)
-    k_fft_cols_inv(float2 *__restrict__ spec, const float2 *__restrict__ tw) {
-    constexpr int N1 = N / 16;
+    k_fft_cols_inv(const __grid_constant__ CUtensorMap tmap, const float2 *__restrict__ tw, int *__restrict__ err) {
+    constexpr int N1 = N / 16, n = N / 2, BR = ColTile<N>::BR;
     using L = FftLayout<N, true, C>;
-    extern __shared__ float2 fft_sh[];
-    const int n = N / 2, hp = n + 1;
+    extern __shared__ __align__(1024) float2 fft_sh[];
+    __shared__ uint64_t bar;
     const int c = threadIdx.x % C, t = threadIdx.x / C;
-    const int kx = blockIdx.x * C + c;
-    const bool ok = kx <= n;
-    float2 *col = spec + (long long)blockIdx.y * N * hp + (ok ? kx : 0);
+    const int x = 2 * blockIdx.x * C, img = blockIdx.y;
+    if (threadIdx.x == 0) {
+        tc::mbar_init(&bar, 1);
+        tc::fence_mbar_init();
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        mbar_expect(&bar, (uint32_t)(N * C * sizeof(float2)));
+        for (int i = 0; i < N / BR; ++i) tma_load3(fft_sh + i * BR * C, &tmap, x, i * BR, img, &bar);
+    }
+    const bool ok = tc::mbar_wait(&bar, 0u);
     float2 v[16];
 #pragma unroll
-    for (int r = 0; r < 16; ++r) v[r] = ok ? col[(long long)(t + N1 * r) * hp] : make_float2(0.f, 0.f);
+    for (int r = 0; r < 16; ++r) v[r] = fft_sh[(t + N1 * r) * C + c];
+    __syncthreads();
     fft_core<N, 1, L>(v, fft_sh, c, t, tw);
-    if (!ok) return;
+    __syncthreads();
 #pragma unroll
     for (int q = 0; q < 16 / L::R3; ++q)
 #pragma unroll
         for (int j1 = 0; j1 < L::R3; ++j1) {
             const int Y = t + N1 * q + 256 * j1;
-            if (Y >= n / 2 && Y < n / 2 + n) col[(long long)Y * hp] = v[q * L::R3 + j1];
+            if (Y >= n / 2 && Y < n / 2 + n) fft_sh[(Y - n / 2) * C + c] = v[q * L::R3 + j1];
         }
+    tc::fence_proxy_async();
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        for (int i = 0; i < n / BR; ++i) tma_store3(&tmap, x, n / 2 + i * BR, img, fft_sh + i * BR * C);
+        tma_store_drain();
+        if (!ok) atomicAdd(err, 1);
+    }
 }
 
 // ---------------------------------------------------------------------------
-// Adjoint rows: rows Ya = n/2 + 2 pr and Ya + 1 of the column pass output,
+// Adjoint rows: rows Ya = n/2 + 2 pr and Ya + 1 of the column pass output
+// (row pitch hp complex),
 // Hermitian-extended to P points, one inverse FFT as A + i B; the centre
 // outputs X in [n/2, 3n/2) are modulated, deapodised, scaled by c and added
 // into rows 2 pr, 2 pr + 1 of u.
@@ -334,11 +403,11 @@ __global__ void __launch_bounds__(C *(N / 16), (C * N <= 8192) ? 2 : 1)
 template <int N>
 __global__ void __launch_bounds__(kRowThreads, 2)
     k_fft_rows_inv(const float2 *__restrict__ spec, float *__restrict__ u, const float *__restrict__ dp,
-                   const float2 *__restrict__ tw, float cscale) {
+                   const float2 *__restrict__ tw, float cscale, int hp) {
     constexpr int N1 = N / 16, RP = kRowThreads / N1;
     using L = FftLayout<N, false, RP>;
     extern __shared__ float2 fft_sh[];
-    const int n = N / 2, hp = n + 1;
+    const int n = N / 2;
     const int t = threadIdx.x % N1, c = threadIdx.x / N1;
     const int pr = blockIdx.x * RP + c;
     const long long img = blockIdx.y;
@@ -388,20 +457,23 @@ size_t rows_smem() {
 }
 template <int N, int C>
 size_t cols_smem() {
-    return sizeof(float2) * (size_t)FftLayout<N, true, C>::S * C;
+    const size_t ex = (size_t)FftLayout<N, true, C>::S * C, tile = (size_t)N * C;
+    return sizeof(float2) * (ex > tile ? ex : tile);
 }
 
 template <int N>
 void set_attrs_n() {
     CUDA_CHECK(cudaFuncSetAttribute(k_fft_rows_fwd<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)rows_smem<N>()));
     CUDA_CHECK(cudaFuncSetAttribute(k_fft_rows_inv<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)rows_smem<N>()));
-    CUDA_CHECK(cudaFuncSetAttribute(k_fft_cols_fwd<N, kColC>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)cols_smem<N, kColC>()));
-    CUDA_CHECK(cudaFuncSetAttribute(k_fft_cols_inv<N, kColC>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)cols_smem<N, kColC>()));
+    CUDA_CHECK(cudaFuncSetAttribute(k_fft_cols_fwd<N, kColC>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    (int)cols_smem<N, kColC>()));
+    CUDA_CHECK(cudaFuncSetAttribute(k_fft_cols_inv<N, kColC>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    (int)cols_smem<N, kColC>()));
 }
 
 template <int N>
-void fwd_n(const float *u, float2 *spec, int nimg, const float *deapod, const float2 *tw, const UsGeo &g,
-           cudaStream_t s) {
+void fwd_n(const float *u, float2 *spec, int nimg, const float *deapod, const float2 *tw, const CUtensorMap &map,
+           int *err, const UsGeo &g, cudaStream_t s) {
     constexpr int N1 = N / 16, RP = kRowThreads / N1;
     const int n = N / 2;
     const float inv4n2 = (float)(1.0 / (4.0 * n * (double)n));
@@ -409,20 +481,46 @@ void fwd_n(const float *u, float2 *spec, int nimg, const float *deapod, const fl
     k_fft_rows_fwd<N><<<gr, kRowThreads, rows_smem<N>(), s>>>(u, spec, deapod, tw, g, inv4n2);
     LAUNCH_CHECK("k_fft_rows_fwd");
     dim3 gc((n + 1 + kColC - 1) / kColC, nimg);
-    k_fft_cols_fwd<N, kColC><<<gc, kColC * N1, cols_smem<N, kColC>(), s>>>(spec, tw, g);
+    k_fft_cols_fwd<N, kColC><<<gc, kColC * N1, cols_smem<N, kColC>(), s>>>(map, tw, err);
     LAUNCH_CHECK("k_fft_cols_fwd");
 }
 
 template <int N>
-void inv_n(float2 *spec, float *u, int nimg, float cscale, const float *deapod, const float2 *tw, cudaStream_t s) {
+void inv_n(float2 *spec, float *u, int nimg, float cscale, const float *deapod, const float2 *tw,
+           const CUtensorMap &map, int *err, int hpitch, cudaStream_t s) {
     constexpr int N1 = N / 16, RP = kRowThreads / N1;
     const int n = N / 2;
     dim3 gc((n + 1 + kColC - 1) / kColC, nimg);
-    k_fft_cols_inv<N, kColC><<<gc, kColC * N1, cols_smem<N, kColC>(), s>>>(spec, tw);
+    k_fft_cols_inv<N, kColC><<<gc, kColC * N1, cols_smem<N, kColC>(), s>>>(map, tw, err);
     LAUNCH_CHECK("k_fft_cols_inv");
     dim3 gr((n / 2 + RP - 1) / RP, nimg);
-    k_fft_rows_inv<N><<<gr, kRowThreads, rows_smem<N>(), s>>>(spec, u, deapod, tw, cscale);
+    k_fft_rows_inv<N><<<gr, kRowThreads, rows_smem<N>(), s>>>(spec, u, deapod, tw, cscale, hpitch);
     LAUNCH_CHECK("k_fft_rows_inv");
+}
+
+PFN_cuTensorMapEncodeTiled_v12000 tmap_encoder() {
+    static PFN_cuTensorMapEncodeTiled_v12000 encode = nullptr;
+    if (!encode) {
+        cudaDriverEntryPointQueryResult q;
+        CUDA_CHECK(cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", (void **)&encode, 12000,
+                                                    cudaEnableDefault, &q));
+        if (q != cudaDriverEntryPointSuccess || !encode) throw Error(1, "cuTensorMapEncodeTiled unavailable");
+    }
+    return encode;
+}
+
+// float view [nimg][rows][row_floats] (pitches in bytes), boxes of 8 floats x
+// min(n, 256) rows x 1 image
+void encode_cols_map(CUtensorMap *map, void *base, long long row_floats, long long rows, long long nimg,
+                     long long row_pitch, long long img_pitch, int n, const char *what) {
+    const cuuint64_t dims[3] = {(cuuint64_t)row_floats, (cuuint64_t)rows, (cuuint64_t)nimg};
+    const cuuint64_t strides[2] = {(cuuint64_t)row_pitch, (cuuint64_t)img_pitch};
+    const cuuint32_t box[3] = {2 * kColC, (cuuint32_t)(n < 256 ? n : 256), 1};
+    const cuuint32_t es[3] = {1, 1, 1};
+    const CUresult r = tmap_encoder()(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, base, dims, strides, box, es,
+                                      CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                                      CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) throw Error(1, std::string("cuTensorMapEncodeTiled failed for ") + what);
 }
 
 }  // namespace
@@ -452,32 +550,41 @@ std::vector<float2> pad_fft_twiddles(int P) {
     return w;
 }
 
+void make_pad_fft_maps(CUtensorMap *fwd, CUtensorMap *inv, float2 *spec, int nimg, const UsGeo &g) {
+    // forward: the halo-padded window [P + 2 kHalo rows][2 qp floats]
+    encode_cols_map(fwd, spec, 2LL * g.qp, g.P + 2LL * kHalo, nimg, 8LL * g.qp, 8LL * g.img_fwd, g.n,
+                    "the forward column FFT");
+    // inverse: Hermitian half planes [P rows][2 hpitch floats]
+    encode_cols_map(inv, spec, 2LL * g.hpitch, g.P, nimg, 8LL * g.hpitch, 8LL * g.P * g.hpitch, g.n,
+                    "the inverse column FFT");
+}
+
 void launch_pad_fft_fwd(const float *u, float2 *spec, int nimg, const float *deapod, const float2 *tw,
-                        const UsGeo &g, cudaStream_t s) {
+                        const CUtensorMap &map, int *err, const UsGeo &g, cudaStream_t s) {
     if (nimg > 65535) throw Error(1, "pad FFT: too many images per batch");
     switch (g.P) {
-        case 256: fwd_n<256>(u, spec, nimg, deapod, tw, g, s); break;
-        case 512: fwd_n<512>(u, spec, nimg, deapod, tw, g, s); break;
-        case 1024: fwd_n<1024>(u, spec, nimg, deapod, tw, g, s); break;
-        case 2048: fwd_n<2048>(u, spec, nimg, deapod, tw, g, s); break;
-        case 4096: fwd_n<4096>(u, spec, nimg, deapod, tw, g, s); break;
+        case 256: fwd_n<256>(u, spec, nimg, deapod, tw, map, err, g, s); break;
+        case 512: fwd_n<512>(u, spec, nimg, deapod, tw, map, err, g, s); break;
+        case 1024: fwd_n<1024>(u, spec, nimg, deapod, tw, map, err, g, s); break;
+        case 2048: fwd_n<2048>(u, spec, nimg, deapod, tw, map, err, g, s); break;
+        case 4096: fwd_n<4096>(u, spec, nimg, deapod, tw, map, err, g, s); break;
         default: throw Error(1, "pad FFT: unsupported grid size");
     }
 }
 
 void launch_pad_fft_inv_accum(float2 *spec, float *u, int zb, float tau, const float *deapod, const float2 *tw,
-                              const UsGeo &g, cudaStream_t s) {
+                              const CUtensorMap &map, int *err, const UsGeo &g, cudaStream_t s) {
     const int nimg = zb * g.m;
     if (nimg > 65535) throw Error(1, "pad FFT: too many images per batch");
     // the scale of the C2R path's crop (1/sqrt(n ntheta) / (4 n^2)) times tau
     const double scale = 1.0 / std::sqrt((double)g.n * (double)g.ntheta);
     const float c = (float)(tau * scale / (4.0 * g.n * (double)g.n));
     switch (g.P) {
-        case 256: inv_n<256>(spec, u, nimg, c, deapod, tw, s); break;
-        case 512: inv_n<512>(spec, u, nimg, c, deapod, tw, s); break;
-        case 1024: inv_n<1024>(spec, u, nimg, c, deapod, tw, s); break;
-        case 2048: inv_n<2048>(spec, u, nimg, c, deapod, tw, s); break;
-        case 4096: inv_n<4096>(spec, u, nimg, c, deapod, tw, s); break;
+        case 256: inv_n<256>(spec, u, nimg, c, deapod, tw, map, err, g.hpitch, s); break;
+        case 512: inv_n<512>(spec, u, nimg, c, deapod, tw, map, err, g.hpitch, s); break;
+        case 1024: inv_n<1024>(spec, u, nimg, c, deapod, tw, map, err, g.hpitch, s); break;
+        case 2048: inv_n<2048>(spec, u, nimg, c, deapod, tw, map, err, g.hpitch, s); break;
+        case 4096: inv_n<4096>(spec, u, nimg, c, deapod, tw, map, err, g.hpitch, s); break;
         default: throw Error(1, "pad FFT: unsupported grid size");
     }
 }

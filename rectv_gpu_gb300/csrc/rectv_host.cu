@@ -122,7 +122,8 @@ struct Handle {
     // hand-written padded-grid FFTs (P a power of two in [256, 4096]) instead
     // of cuFFT + deapodise/pad + crop passes; RECTV_CUFFT=1 selects cuFFT
     bool pad_fft = false;
-    float2 *fft_tw = nullptr;  // [P] exp(-2 pi i k / P)
+    float2 *fft_tw = nullptr;  // twiddle tables (pad_fft_twiddles)
+    CUtensorMap fft_fwd_map, fft_inv_map;  // TMA tiles of the column passes
 
     // session
     bool session = false;
@@ -172,6 +173,7 @@ struct Handle {
         ug.m = m;
         ug.P = P;
         ug.hp = P / 2 + 1;
+        ug.hpitch = P / 2 + 1;
         ug.qp = n + 2 * kHalo + (n & 1);
         ug.qoff = (long long)kHalo * ug.qp + kHalo;
         ug.img_fwd = (long long)(P + 2 * kHalo) * ug.qp;
@@ -240,6 +242,8 @@ struct Handle {
                 CUDA_CHECK(cudaMemcpyAsync(fft_tw, w.data(), sizeof(float2) * w.size(), cudaMemcpyHostToDevice,
                                            stream));
                 CUDA_CHECK(cudaStreamSynchronize(stream));
+                ug.hpitch = P / 2 + 2;  // 16-byte half-plane rows for the TMA tiles
+                make_pad_fft_maps(&fft_fwd_map, &fft_inv_map, spec, zb * m, ug);
             }
         }
         make_fft_plans();
@@ -482,7 +486,7 @@ struct Handle {
     void forward(const float *u, const float *gb, float *out, float tau, int residual) {
         const int nimg = zb * m;
         if (pad_fft) {
-            launch_pad_fft_fwd(u, spec, nimg, gd.deapod, fft_tw, ug, stream);
+            launch_pad_fft_fwd(u, spec, nimg, gd.deapod, fft_tw, fft_fwd_map, gd.err, ug, stream);
         } else {
             launch_deapod_pad(u, reinterpret_cast<float *>(spec), nimg, gd.deapod, ug, stream);
             for (int i = 0; i < nimg; i += img_per_fft) {
@@ -507,11 +511,11 @@ struct Handle {
         if (gd.tc_scatter) {
             // Re IFFT2 of the scattered grids as a C2R of their Hermitian part,
             // which the tensor-core scatter adds into zeroed half planes
-            const long long img_half = (long long)ug.P * (ug.P / 2 + 1);
+            const long long img_half = (long long)ug.P * ug.hpitch;
             CUDA_CHECK(cudaMemsetAsync(spec, 0, sizeof(float2) * (size_t)nimg * img_half, stream));
             launch_scatter_adj(rows, spec, zb, gd, ug, stream);
             if (pad_fft) {
-                launch_pad_fft_inv_accum(spec, u, zb, tau, gd.deapod, fft_tw, ug, stream);
+                launch_pad_fft_inv_accum(spec, u, zb, tau, gd.deapod, fft_tw, fft_inv_map, gd.err, ug, stream);
                 return;
             }
             for (int i = 0; i < nimg; i += img_per_fft) {
@@ -844,10 +848,11 @@ struct Handle {
                     launch_shrink(U[cur], U[cur], psi, mu, rho_d, lambda0, 0, nchunks, tv, partials, stream);
                     break;
                 case 4:  // padded-grid forward FFT of the batch (rows + columns)
-                    launch_pad_fft_fwd(U[cur], spec, zb * m, gd.deapod, fft_tw, ug, stream);
+                    launch_pad_fft_fwd(U[cur], spec, zb * m, gd.deapod, fft_tw, fft_fwd_map, gd.err, ug, stream);
                     break;
                 case 5:  // padded-grid inverse FFT (columns + rows), added into the scratch iterate
-                    launch_pad_fft_inv_accum(spec, U[(cur + 1) % 3], zb, 0.f, gd.deapod, fft_tw, ug, stream);
+                    launch_pad_fft_inv_accum(spec, U[(cur + 1) % 3], zb, 0.f, gd.deapod, fft_tw, fft_inv_map, gd.err,
+                                             ug, stream);
                     break;
                 default: throw Error(RECTV_ERR_ARG, "rectv_launch_kernel: unknown kernel id");
             }

@@ -46,6 +46,8 @@ struct UsGeo {
     int n, ntheta, m;   // detector width, projections, time samples
     int P;              // oversampled grid side 2n
     int hp;             // half-plane row length P/2+1 (complex)
+    int hpitch;         // row pitch of the adjoint's Hermitian half planes (complex):
+                        // P/2+1, or P/2+2 (16-byte rows for TMA) with the padded-grid FFTs
     // Forward spectra are stored as the window rows [-kHalo, P+kHalo) x
     // columns [-kHalo, n+kHalo) of the periodic full spectrum: the R2C output
     // (rows [0,P), columns [0,n]) plus a halo of wrapped / Hermitian-mirrored
@@ -148,14 +150,16 @@ void launch_adj_records(AdjRec *recs, const GeoDev &gd, const UsGeo &g, cudaStre
 // hand-written 2D FFTs of the zero-padded grids (fft_kernels.cu), P = 2n a
 // power of two in [256, 4096]: forward = deapodise/pad/modulate + R2C into
 // the halo-padded spectra (halo not filled); inverse = C2R of the Hermitian
-// half planes [img][P][P/2+1] (overwritten) + crop/deapodise, u += tau * ...
+// half planes [img][P][hpitch] (overwritten) + crop/deapodise, u += tau * ...
 bool pad_fft_supported(int P);
 void pad_fft_prepare();
 std::vector<float2> pad_fft_twiddles(int P);
+// TMA descriptors of the column passes over the spectra buffer (nimg images)
+void make_pad_fft_maps(CUtensorMap *fwd, CUtensorMap *inv, float2 *spec, int nimg, const UsGeo &g);
 void launch_pad_fft_fwd(const float *u, float2 *spec, int nimg, const float *deapod, const float2 *tw,
-                        const UsGeo &g, cudaStream_t s);
+                        const CUtensorMap &map, int *err, const UsGeo &g, cudaStream_t s);
 void launch_pad_fft_inv_accum(float2 *spec, float *u, int zb, float tau, const float *deapod, const float2 *tw,
-                              const UsGeo &g, cudaStream_t s);
+                              const CUtensorMap &map, int *err, const UsGeo &g, cudaStream_t s);
 size_t gather_tc_smem();
 int gather_tc_table_capacity();
 size_t gather_fwd_smem(const UsGeo &g);

@@ -440,7 +440,7 @@ __global__ void __launch_bounds__(kThr, 1)
         // depend on their order); the pre-IFFT fftshift sign is applied here ----
         const int KY = tyi * kT + cy, KX = txi * kT + cx;
         if (zok && KY < P && KX < P) {
-            const int half = P / 2, hp = half + 1;
+            const int half = P / 2, hp = g.hpitch;
             const long long img_half = (long long)P * hp;
             const float sg = ((KX + KY) & 1) ? -0.5f : 0.5f;
             const bool here = KX <= half, mirror = KX >= half || KX == 0;
