@@ -1,5 +1,5 @@
 // Two-dimensional FFTs of the USFFT operators for P = 2n a power of two
-// (256 <= P <= 4096), written for the zero padding of the reference's grids.
+// (256 <= P <= 2048), written for the zero padding of the reference's grids.
 //
 // The reference pads the deapodised n x n image into the centre of a P x P
 // grid, modulates it by (-1)^(X+Y) and runs a P x P FFT (divphi, fftshift and
@@ -32,6 +32,7 @@
 #include <cudaTypedefs.h>
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cmath>
 #include <string>
 #include <vector>
@@ -286,109 +287,112 @@ __device__ __forceinline__ void tma_store3(const CUtensorMap *map, int x, int y,
                  "r"(x), "r"(y), "r"(z), "r"(tc::smem_addr(src))
                  : "memory");
 }
-__device__ __forceinline__ void tma_store_drain() {
-    asm volatile("cp.async.bulk.commit_group;\ncp.async.bulk.wait_group.read 0;\n" ::: "memory");
+__device__ __forceinline__ void tma_store_wait_read() {
+    asm volatile("cp.async.bulk.wait_group.read 0;\n" ::: "memory");
 }
 __device__ __forceinline__ void mbar_expect(void *bar, uint32_t bytes) {
     asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(tc::smem_addr(bar)), "r"(bytes)
                  : "memory");
 }
 
-template <int N>
-struct ColTile {
+
+// ---------------------------------------------------------------------------
+// Column passes.  Persistent blocks (one per SM) take tiles of 4 columns of
+// one image round-robin, column groups fastest; the tile after the current
+// one is loaded by TMA into the second landing buffer while the current one
+// is transformed, and each output tile leaves by TMA stores from the exchange
+// buffer, which the next tile reuses once those stores have read it.
+//
+// Forward: columns kx .. kx+3 of the row pass output (rows [n/2, 3n/2); the
+// others are zero and not read), P-point FFT, all P rows written back in
+// place (window coordinates of the halo-padded spectra: x = 2 (kHalo + kx)
+// floats, y = kHalo + row; columns past n are halo cells, rewritten by the
+// halo pass afterwards).
+// Inverse: inverse P-point FFT of columns kx .. kx+3 of the Hermitian half
+// planes [img][P][hpitch]; only rows [n/2, 3n/2) are written back (columns
+// past the row pitch read as zeros and are not stored).
+// ---------------------------------------------------------------------------
+template <int N, int C, int DIR>
+struct ColPass {
     static constexpr int n = N / 2;
-    static constexpr int BR = n < 256 ? n : 256;  // rows per TMA box
+    static constexpr int BR = n < 256 ? n : 256;                // rows per TMA box
+    static constexpr int IN_ROWS = DIR < 0 ? n : N;              // rows loaded per tile
+    static constexpr int OUT_ROWS = DIR < 0 ? N : n;             // rows stored per tile
+    static constexpr int IN_Y0 = DIR < 0 ? kHalo + n / 2 : 0;    // first loaded row (map coordinates)
+    static constexpr int OUT_Y0 = DIR < 0 ? kHalo : n / 2;       // first stored row
+    static constexpr int XOFF = DIR < 0 ? kHalo : 0;             // column offset of the map window
+    using L = FftLayout<N, true, C>;
+    static constexpr size_t EX = (size_t)L::S * C > (size_t)OUT_ROWS * C ? (size_t)L::S * C : (size_t)OUT_ROWS * C;
+    static constexpr size_t LAND = (size_t)IN_ROWS * C;          // float2 per landing buffer
+    static constexpr size_t SMEM = sizeof(float2) * (EX + 2 * LAND);
 };
 
-// ---------------------------------------------------------------------------
-// Forward columns: columns kx0 .. kx0+3 of the row pass output (rows
-// [n/2, 3n/2); the others are zero and not read), P-point FFT, all P rows
-// written back in place.  Tiles in and out by TMA (window coordinates of the
-// halo-padded spectra: x = 2 (kHalo + kx) floats, y = kHalo + row); columns
-// past n are halo cells, rewritten by the halo pass afterwards.
-// ---------------------------------------------------------------------------
-template <int N, int C>
-__global__ void __launch_bounds__(C *(N / 16), (C * N <= 8192) ? 2 : 1)
-    k_fft_cols_fwd(const __grid_constant__ CUtensorMap tmap, const float2 *__restrict__ tw, int *__restrict__ err) {
-    constexpr int N1 = N / 16, n = N / 2, BR = ColTile<N>::BR;
-    using L = FftLayout<N, true, C>;
+template <int N, int C, int DIR>
+__global__ void __launch_bounds__(C *(N / 16), 1)
+    k_fft_cols(const __grid_constant__ CUtensorMap tmap, const float2 *__restrict__ tw, int ngroups, int ntiles,
+               int *__restrict__ err) {
+    using CP = ColPass<N, C, DIR>;
+    using L = typename CP::L;
+    constexpr int N1 = N / 16, n = N / 2, BR = CP::BR;
     extern __shared__ __align__(1024) float2 fft_sh[];
-    __shared__ uint64_t bar;
+    float2 *ex = fft_sh;  // exchange buffer / output tile; landing buffers follow it
+    __shared__ uint64_t bar[2];
     const int c = threadIdx.x % C, t = threadIdx.x / C;
-    const int x = 2 * (kHalo + blockIdx.x * C), img = blockIdx.y;
     if (threadIdx.x == 0) {
-        tc::mbar_init(&bar, 1);
+        tc::mbar_init(&bar[0], 1);
+        tc::mbar_init(&bar[1], 1);
         tc::fence_mbar_init();
     }
     __syncthreads();
-    if (threadIdx.x == 0) {
-        mbar_expect(&bar, (uint32_t)(n * C * sizeof(float2)));
-        for (int i = 0; i < n / BR; ++i) tma_load3(fft_sh + i * BR * C, &tmap, x, kHalo + n / 2 + i * BR, img, &bar);
-    }
-    const bool ok = tc::mbar_wait(&bar, 0u);
-    float2 v[16];
+    auto fetch = [&](int tile, int buf) {  // one thread
+        const int x = 2 * (CP::XOFF + (tile % ngroups) * C), img = tile / ngroups;
+        mbar_expect(&bar[buf], (uint32_t)(CP::LAND * sizeof(float2)));
+        for (int i = 0; i < CP::IN_ROWS / BR; ++i)
+            tma_load3(fft_sh + CP::EX + buf * CP::LAND + i * BR * C, &tmap, x, CP::IN_Y0 + i * BR, img, &bar[buf]);
+    };
+    if (threadIdx.x == 0 && (int)blockIdx.x < ntiles) fetch(blockIdx.x, 0);
+    bool ok = true;
+    int it = 0;
+    for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x, ++it) {
+        const int buf = it & 1;
+        // the other landing buffer was read in the previous iteration, before
+        // at least one block barrier: it takes the next tile
+        if (threadIdx.x == 0 && tile + (int)gridDim.x < ntiles) fetch(tile + gridDim.x, buf ^ 1);
+        ok = tc::mbar_wait(&bar[buf], (uint32_t)((it >> 1) & 1)) && ok;
+        float2 v[16];
+        const float2 *in = fft_sh + CP::EX + buf * CP::LAND;
 #pragma unroll
-    for (int r = 0; r < 16; ++r)
-        v[r] = (r >= 4 && r < 12) ? fft_sh[(t + N1 * r - n / 2) * C + c] : make_float2(0.f, 0.f);
-    __syncthreads();  // the exchange buffer reuses the landing tile
-    fft_core<N, -1, L>(v, fft_sh, c, t, tw);
-    __syncthreads();
-#pragma unroll
-    for (int q = 0; q < 16 / L::R3; ++q)
-#pragma unroll
-        for (int j1 = 0; j1 < L::R3; ++j1) fft_sh[(t + N1 * q + 256 * j1) * C + c] = v[q * L::R3 + j1];
-    tc::fence_proxy_async();
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        for (int i = 0; i < N / BR; ++i) tma_store3(&tmap, x, kHalo + i * BR, img, fft_sh + i * BR * C);
-        tma_store_drain();
-        if (!ok) atomicAdd(err, 1);
-    }
-}
-
-// ---------------------------------------------------------------------------
-// Adjoint columns: inverse P-point FFT of columns kx0 .. kx0+3 of the
-// Hermitian half planes [img][P][hpitch]; only rows [n/2, 3n/2) are written
-// back.  Tiles in and out by TMA; columns past the row pitch read as zeros
-// and are not stored.
-// ---------------------------------------------------------------------------
-template <int N, int C>
-__global__ void __launch_bounds__(C *(N / 16), (C * N <= 8192) ? 2 : 1)
-    k_fft_cols_inv(const __grid_constant__ CUtensorMap tmap, const float2 *__restrict__ tw, int *__restrict__ err) {
-    constexpr int N1 = N / 16, n = N / 2, BR = ColTile<N>::BR;
-    using L = FftLayout<N, true, C>;
-    extern __shared__ __align__(1024) float2 fft_sh[];
-    __shared__ uint64_t bar;
-    const int c = threadIdx.x % C, t = threadIdx.x / C;
-    const int x = 2 * blockIdx.x * C, img = blockIdx.y;
-    if (threadIdx.x == 0) {
-        tc::mbar_init(&bar, 1);
-        tc::fence_mbar_init();
-    }
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        mbar_expect(&bar, (uint32_t)(N * C * sizeof(float2)));
-        for (int i = 0; i < N / BR; ++i) tma_load3(fft_sh + i * BR * C, &tmap, x, i * BR, img, &bar);
-    }
-    const bool ok = tc::mbar_wait(&bar, 0u);
-    float2 v[16];
-#pragma unroll
-    for (int r = 0; r < 16; ++r) v[r] = fft_sh[(t + N1 * r) * C + c];
-    __syncthreads();
-    fft_core<N, 1, L>(v, fft_sh, c, t, tw);
-    __syncthreads();
-#pragma unroll
-    for (int q = 0; q < 16 / L::R3; ++q)
-#pragma unroll
-        for (int j1 = 0; j1 < L::R3; ++j1) {
-            const int Y = t + N1 * q + 256 * j1;
-            if (Y >= n / 2 && Y < n / 2 + n) fft_sh[(Y - n / 2) * C + c] = v[q * L::R3 + j1];
+        for (int r = 0; r < 16; ++r) {
+            if constexpr (DIR < 0)
+                v[r] = (r >= 4 && r < 12) ? in[(t + N1 * r - n / 2) * C + c] : make_float2(0.f, 0.f);
+            else
+                v[r] = in[(t + N1 * r) * C + c];
         }
-    tc::fence_proxy_async();
-    __syncthreads();
+        if (threadIdx.x == 0) tma_store_wait_read();  // the previous output tile has left the exchange buffer
+        __syncthreads();
+        fft_core<N, DIR, L>(v, ex, c, t, tw);
+        __syncthreads();
+#pragma unroll
+        for (int q = 0; q < 16 / L::R3; ++q)
+#pragma unroll
+            for (int j1 = 0; j1 < L::R3; ++j1) {
+                const int Y = t + N1 * q + 256 * j1;
+                if constexpr (DIR < 0) {
+                    ex[Y * C + c] = v[q * L::R3 + j1];
+                } else {
+                    if (Y >= n / 2 && Y < n / 2 + n) ex[(Y - n / 2) * C + c] = v[q * L::R3 + j1];
+                }
+            }
+        tc::fence_proxy_async();
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            const int x = 2 * (CP::XOFF + (tile % ngroups) * C), img = tile / ngroups;
+            for (int i = 0; i < CP::OUT_ROWS / BR; ++i) tma_store3(&tmap, x, CP::OUT_Y0 + i * BR, img, ex + i * BR * C);
+            asm volatile("cp.async.bulk.commit_group;\n" ::: "memory");
+        }
+    }
     if (threadIdx.x == 0) {
-        for (int i = 0; i < n / BR; ++i) tma_store3(&tmap, x, n / 2 + i * BR, img, fft_sh + i * BR * C);
-        tma_store_drain();
+        asm volatile("cp.async.bulk.wait_group 0;\n" ::: "memory");  // the last tiles are written
         if (!ok) atomicAdd(err, 1);
     }
 }
@@ -455,20 +459,35 @@ template <int N>
 size_t rows_smem() {
     return sizeof(float2) * (size_t)FftLayout<N, false, kRowThreads / (N / 16)>::S * (kRowThreads / (N / 16));
 }
-template <int N, int C>
-size_t cols_smem() {
-    const size_t ex = (size_t)FftLayout<N, true, C>::S * C, tile = (size_t)N * C;
-    return sizeof(float2) * (ex > tile ? ex : tile);
-}
-
 template <int N>
 void set_attrs_n() {
     CUDA_CHECK(cudaFuncSetAttribute(k_fft_rows_fwd<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)rows_smem<N>()));
     CUDA_CHECK(cudaFuncSetAttribute(k_fft_rows_inv<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)rows_smem<N>()));
-    CUDA_CHECK(cudaFuncSetAttribute(k_fft_cols_fwd<N, kColC>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                    (int)cols_smem<N, kColC>()));
-    CUDA_CHECK(cudaFuncSetAttribute(k_fft_cols_inv<N, kColC>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                    (int)cols_smem<N, kColC>()));
+    CUDA_CHECK(cudaFuncSetAttribute(k_fft_cols<N, kColC, -1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    (int)ColPass<N, kColC, -1>::SMEM));
+    CUDA_CHECK(cudaFuncSetAttribute(k_fft_cols<N, kColC, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    (int)ColPass<N, kColC, 1>::SMEM));
+}
+
+int sm_count() {
+    static int nsm = 0;
+    if (nsm == 0) {
+        int dev = 0;
+        CUDA_CHECK(cudaGetDevice(&dev));
+        CUDA_CHECK(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+    }
+    return nsm;
+}
+
+template <int N, int DIR>
+void launch_cols(const CUtensorMap &map, const float2 *tw, int nimg, int *err, cudaStream_t s) {
+    const int ngroups = (N / 2 + 1 + kColC - 1) / kColC;
+    const long long ntiles = (long long)ngroups * nimg;
+    if (ntiles > 2147483647LL) throw Error(1, "pad FFT: too many column tiles");
+    const int grid = (int)std::min<long long>(ntiles, sm_count());
+    k_fft_cols<N, kColC, DIR><<<grid, kColC * (N / 16), ColPass<N, kColC, DIR>::SMEM, s>>>(map, tw, ngroups,
+                                                                                         (int)ntiles, err);
+    LAUNCH_CHECK(DIR < 0 ? "k_fft_cols (forward)" : "k_fft_cols (inverse)");
 }
 
 template <int N>
@@ -480,9 +499,7 @@ void fwd_n(const float *u, float2 *spec, int nimg, const float *deapod, const fl
     dim3 gr((n / 2 + RP - 1) / RP, nimg);
     k_fft_rows_fwd<N><<<gr, kRowThreads, rows_smem<N>(), s>>>(u, spec, deapod, tw, g, inv4n2);
     LAUNCH_CHECK("k_fft_rows_fwd");
-    dim3 gc((n + 1 + kColC - 1) / kColC, nimg);
-    k_fft_cols_fwd<N, kColC><<<gc, kColC * N1, cols_smem<N, kColC>(), s>>>(map, tw, err);
-    LAUNCH_CHECK("k_fft_cols_fwd");
+    launch_cols<N, -1>(map, tw, nimg, err, s);
 }
 
 template <int N>
@@ -490,9 +507,7 @@ void inv_n(float2 *spec, float *u, int nimg, float cscale, const float *deapod, 
            const CUtensorMap &map, int *err, int hpitch, cudaStream_t s) {
     constexpr int N1 = N / 16, RP = kRowThreads / N1;
     const int n = N / 2;
-    dim3 gc((n + 1 + kColC - 1) / kColC, nimg);
-    k_fft_cols_inv<N, kColC><<<gc, kColC * N1, cols_smem<N, kColC>(), s>>>(map, tw, err);
-    LAUNCH_CHECK("k_fft_cols_inv");
+    launch_cols<N, 1>(map, tw, nimg, err, s);
     dim3 gr((n / 2 + RP - 1) / RP, nimg);
     k_fft_rows_inv<N><<<gr, kRowThreads, rows_smem<N>(), s>>>(spec, u, deapod, tw, cscale, hpitch);
     LAUNCH_CHECK("k_fft_rows_inv");
@@ -525,14 +540,15 @@ void encode_cols_map(CUtensorMap *map, void *base, long long row_floats, long lo
 
 }  // namespace
 
-bool pad_fft_supported(int P) { return P >= 256 && P <= 4096 && (P & (P - 1)) == 0; }
+// P <= 2048: the column passes' two landing tiles and exchange buffer fit in
+// shared memory up to that size
+bool pad_fft_supported(int P) { return P >= 256 && P <= 2048 && (P & (P - 1)) == 0; }
 
 void pad_fft_prepare() {
     set_attrs_n<256>();
     set_attrs_n<512>();
     set_attrs_n<1024>();
     set_attrs_n<2048>();
-    set_attrs_n<4096>();
 }
 
 std::vector<float2> pad_fft_twiddles(int P) {
@@ -567,7 +583,6 @@ void launch_pad_fft_fwd(const float *u, float2 *spec, int nimg, const float *dea
         case 512: fwd_n<512>(u, spec, nimg, deapod, tw, map, err, g, s); break;
         case 1024: fwd_n<1024>(u, spec, nimg, deapod, tw, map, err, g, s); break;
         case 2048: fwd_n<2048>(u, spec, nimg, deapod, tw, map, err, g, s); break;
-        case 4096: fwd_n<4096>(u, spec, nimg, deapod, tw, map, err, g, s); break;
         default: throw Error(1, "pad FFT: unsupported grid size");
     }
 }
@@ -584,7 +599,6 @@ void launch_pad_fft_inv_accum(float2 *spec, float *u, int zb, float tau, const f
         case 512: inv_n<512>(spec, u, nimg, c, deapod, tw, map, err, g.hpitch, s); break;
         case 1024: inv_n<1024>(spec, u, nimg, c, deapod, tw, map, err, g.hpitch, s); break;
         case 2048: inv_n<2048>(spec, u, nimg, c, deapod, tw, map, err, g.hpitch, s); break;
-        case 4096: inv_n<4096>(spec, u, nimg, c, deapod, tw, map, err, g.hpitch, s); break;
         default: throw Error(1, "pad FFT: unsupported grid size");
     }
 }

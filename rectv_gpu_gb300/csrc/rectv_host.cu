@@ -119,7 +119,7 @@ struct Handle {
     bool plans_made = false;
     int img_per_fft = 0;
     void *fft_work = nullptr;
-    // hand-written padded-grid FFTs (P a power of two in [256, 4096]) instead
+    // hand-written padded-grid FFTs (P a power of two in [256, 2048]) instead
     // of cuFFT + deapodise/pad + crop passes; RECTV_CUFFT=1 selects cuFFT
     bool pad_fft = false;
     float2 *fft_tw = nullptr;  // twiddle tables (pad_fft_twiddles)

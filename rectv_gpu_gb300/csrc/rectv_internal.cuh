@@ -148,7 +148,7 @@ void launch_scatter_tc(const float2 *rowsc, float2 *spec, int zb, const GeoDev &
 void scatter_tc_prepare();
 void launch_adj_records(AdjRec *recs, const GeoDev &gd, const UsGeo &g, cudaStream_t s);
 // hand-written 2D FFTs of the zero-padded grids (fft_kernels.cu), P = 2n a
-// power of two in [256, 4096]: forward = deapodise/pad/modulate + R2C into
+// power of two in [256, 2048]: forward = deapodise/pad/modulate + R2C into
 // the halo-padded spectra (halo not filled); inverse = C2R of the Hermitian
 // half planes [img][P][hpitch] (overwritten) + crop/deapodise, u += tau * ...
 bool pad_fft_supported(int P);
