@@ -419,11 +419,37 @@ struct Handle {
         gd.split_tiles = (int *)up(hp.split_tiles.data(), hp.split_tiles.size() * 4);
         gd.n_split_tiles = (int)hp.split_tiles.size();
         gd.tc_scatter = tc_scatter;
+        std::vector<int> tab_base(1, 0);  // uploaded asynchronously: kept until the stream sync below
+        std::vector<int4> tabs;
         if (tc_scatter) {
             void *p = nullptr;
             CUDA_CHECK(cudaMalloc(&p, std::max<size_t>(hp.adj_pts.size() * sizeof(AdjRec), 16)));
             geo_owned.push_back(p);
             gd.adj_recs = (AdjRec *)p;
+            // tables of the busy items and the size of their ray segmentation
+            const int cap = scatter_tc_table_capacity();
+            long long words = 0;
+            for (int i = 0; i < gd.n_adj_busy; ++i) {
+                const int4 it = hp.adj_items[i];
+                for (int c0 = 0; c0 < it.z; c0 += cap) {
+                    const int cnt = std::min(cap, it.z - c0);
+                    const uint32_t *pts = hp.adj_pts.data() + it.y + c0;
+                    int nseg = 1;
+                    for (int e = 1; e < cnt; ++e) nseg += (pts[e] / (uint32_t)n != pts[e - 1] / (uint32_t)n) ? 1 : 0;
+                    const int w = scatter_tc_info_words(nseg);
+                    tabs.push_back(make_int4(it.y + c0, cnt, (int)words, w));
+                    words += w;
+                    if (words > 2147483647LL) throw Error(RECTV_ERR_ARG, "rectv: adjoint plan too large");
+                }
+                tab_base.push_back((int)tabs.size());
+            }
+            gd.n_adj_tabs = (int)tabs.size();
+            gd.adj_tabs = (int4 *)up(tabs.data(), tabs.size() * sizeof(int4));
+            gd.adj_tab_base = (int *)up(tab_base.data(), tab_base.size() * sizeof(int));
+            void *q = nullptr;
+            CUDA_CHECK(cudaMalloc(&q, std::max<size_t>((size_t)words * 4, 16)));
+            geo_owned.push_back(q);
+            gd.adj_info = (uint32_t *)q;
         }
         if (gd.n_fwd_items > 2147483647 || gd.n_adj_items > 2147483647)
             throw Error(RECTV_ERR_ARG, "rectv: plan too large");
@@ -469,7 +495,10 @@ struct Handle {
             dp[x] = (float)std::exp((double)mu_us * d * d);
         }
         gd.deapod = (float *)up(dp.data(), n * sizeof(float));
-        if (gd.tc_scatter) launch_adj_records(gd.adj_recs, gd, ug, stream);
+        if (gd.tc_scatter) {
+            launch_adj_records(gd.adj_recs, gd, ug, stream);
+            launch_adj_tabinfo(gd, stream);
+        }
         CUDA_CHECK(cudaStreamSynchronize(stream));  // host vectors go out of scope
         geo_theta.assign(theta_h, theta_h + ntheta);
         geo_phi.assign(phi_h, phi_h + nphi);

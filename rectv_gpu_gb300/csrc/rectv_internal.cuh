@@ -97,6 +97,14 @@ struct GeoDev {
     bool tc_scatter = false;     // adjoint time-sample mixing on the tensor cores (k_scatter_tc)
     AdjRec *adj_recs = nullptr;  // geometry records of adj_pts (tensor-core scatter only)
     int n_adj_busy = 0;          // leading adj_items with samples (items are sorted by count)
+    // tensor-core scatter tables: each busy item's entries in runs of
+    // scatter_tc_table_capacity(); item i owns tables [adj_tab_base[i],
+    // adj_tab_base[i+1]); adj_tabs = (first entry, count, segmentation offset
+    // and size in 32-bit words); adj_info = the tables' ray segmentation
+    int4 *adj_tabs = nullptr;
+    int *adj_tab_base = nullptr;
+    uint32_t *adj_info = nullptr;
+    int n_adj_tabs = 0;
 };
 
 // Host-side angle plan (built in plan.cpp).
@@ -147,6 +155,12 @@ void launch_scatter_tc(const float2 *rowsc, float2 *spec, int zb, const GeoDev &
                        cudaStream_t s);
 void scatter_tc_prepare();
 void launch_adj_records(AdjRec *recs, const GeoDev &gd, const UsGeo &g, cudaStream_t s);
+// entries per scatter table, and the 32-bit words of a table's segmentation
+// with nseg rays (count, per-warp sample ranges, ray starts)
+int scatter_tc_table_capacity();
+int scatter_tc_info_words(int nseg);
+// fill adj_info from the records (after launch_adj_records)
+void launch_adj_tabinfo(const GeoDev &gd, cudaStream_t s);
 // hand-written 2D FFTs of the zero-padded grids (fft_kernels.cu), P = 2n a
 // power of two in [256, 2048]: forward = deapodise/pad/modulate + R2C into
 // the halo-padded spectra (halo not filled); inverse = C2R of the Hermitian

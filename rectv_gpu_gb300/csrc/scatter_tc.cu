@@ -73,19 +73,20 @@ __device__ __forceinline__ int off32(int row, int kk) {
     return (row >> 3) * 256 + (kk >> 2) * 32 + (row & 7) * 4 + (kk & 3);
 }
 
+// 32-bit words of a table's ray segmentation: [0] nseg, [4 + 8 s + w] the
+// table rows [lo, hi) of ray s that cover rows 2w, 2w+1 of the tile (lo |
+// hi << 16; empty: lo = kTab, hi = 0), then the first row of every ray and
+// the table size as 16-bit values; padded to 16 bytes
+__host__ __device__ constexpr int info_words(int nseg) { return (4 + 8 * nseg + (nseg + 2) / 2 + 3) & ~3; }
+constexpr int kInfoMax = info_words(kTab);
+
 struct ScTcSmem {
     AdjRec rec[2][kTab];          // geometry records of this table and the next (bulk copies)
-    float2 t[kZ][kTab][kT];       // T_p(cy) = E(p) wy_p(cy), per slice of the pair
-    float2 e[kZ][kTab];           // E(p)
+    uint32_t info[2][kInfoMax];   // their ray segmentation (bulk copies)
+    float2 t[kZ][kT][kTab];       // T_p(cy) = E(p) wy_p(cy), per slice of the pair
     float2 rnext[kZ][kTab];       // row spectrum values of the next table's samples (cp.async)
     float bhi[kN * kK];           // B = conj K' of the batch's rays, FP32: rows 0..31 of the MMA's B
     float blo[kN * kK];           // B - trunc(B): rows 32..63 (contiguous with bhi)
-    int seg_first[kTab + 1];
-    // per warp (of a half) and ray: the table rows [lo, hi) from the first to
-    // the last sample whose stencil covers one of the warp's two tile rows
-    // (the others in between contribute zero weight); empty: lo = kTab, hi = 0
-    int rlo[kHW][kTab], rhi[kHW][kTab];
-    int wsum[kHW];
     unsigned long long bar;      // MMA batch done (both slices)
     unsigned long long rbar[2];  // record buffer landed
     uint32_t tslot;
@@ -159,10 +160,101 @@ void launch_adj_records(AdjRec *recs, const GeoDev &gd, const UsGeo &g, cudaStre
     LAUNCH_CHECK("k_adj_records");
 }
 
+// ---------------------------------------------------------------------------
+// Ray segmentation of every scatter table (geometry only, so computed once):
+// the rays (runs of equal theta, records are theta-major), their first rows,
+// and per ray and warp of a block half the rows [lo, hi) from the first to
+// the last sample whose stencil covers the warp's two tile rows, from the
+// samples where a covered run starts or ends.  One block per table.
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(kTab)
+    k_adj_tabinfo(const AdjRec *__restrict__ recs, const int4 *__restrict__ tabs, uint32_t *__restrict__ info) {
+    __shared__ int seg_first[kTab + 1];
+    __shared__ int rlo[kHW][kTab], rhi[kHW][kTab];
+    __shared__ int wsum[kTab / 32];
+    const int4 tb = tabs[blockIdx.x];  // (first entry, count, word offset, words)
+    const int ct = threadIdx.x, lane = ct & 31, w = ct >> 5, cnt = tb.y;
+    int thm = 0, thp = 0, thn = 0;
+    if (ct < cnt) {
+        thm = recs[(long long)tb.x + ct].thm;
+        if (ct > 0) thp = recs[(long long)tb.x + ct - 1].thm;
+        if (ct + 1 < cnt) thn = recs[(long long)tb.x + ct + 1].thm;
+    }
+    const unsigned th = (unsigned)thm >> 16;
+    const int flag = (ct < cnt && (ct == 0 || ((unsigned)thp >> 16) != th)) ? 1 : 0;
+    int incl = flag;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const int y = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += y;
+    }
+    if (lane == 31) wsum[w] = incl;
+    __syncthreads();
+    int base = 0, nseg = 0;
+#pragma unroll
+    for (int i = 0; i < kTab / 32; ++i) {
+        base += (i < w) ? wsum[i] : 0;
+        nseg += wsum[i];
+    }
+    const int seg = incl + base - 1;
+    if (ct < cnt && flag) {
+        seg_first[seg] = ct;
+#pragma unroll
+        for (int i = 0; i < kHW; ++i) {
+            rlo[i][seg] = kTab;
+            rhi[i][seg] = 0;
+        }
+    }
+    if (ct == 0) seg_first[nseg] = cnt;
+    __syncthreads();
+    if (ct < cnt) {
+        const int msk = thm & 0xffff;
+        const int mprev = flag ? 0 : (thp & 0xffff);
+        const bool last = ct + 1 == cnt || ((unsigned)thn >> 16) != th;
+        const int mnext = last ? 0 : (thn & 0xffff);
+#pragma unroll
+        for (int i = 0; i < kHW; ++i) {
+            const int bits = 3 << (2 * i);
+            if (msk & bits) {
+                if (!(mprev & bits)) atomicMin(&rlo[i][seg], ct);
+                if (!(mnext & bits)) atomicMax(&rhi[i][seg], ct + 1);
+            }
+        }
+    }
+    __syncthreads();
+    uint32_t *out = info + tb.z;
+    const int nw = min(info_words(nseg), tb.w);  // the host sized the slot from the same rays
+    for (int i = ct; i < nw; i += kTab) {
+        uint32_t v = 0;
+        if (i == 0) {
+            v = (uint32_t)nseg;
+        } else if (i >= 4 && i < 4 + 8 * nseg) {
+            const int sg = (i - 4) >> 3, ww = (i - 4) & 7;
+            v = (uint32_t)rlo[ww][sg] | ((uint32_t)rhi[ww][sg] << 16);
+        } else if (i >= 4 + 8 * nseg) {
+            const int j = 2 * (i - 4 - 8 * nseg);  // 16-bit ray starts j, j+1
+            if (j <= nseg) v = (uint32_t)seg_first[j];
+            if (j + 1 <= nseg) v |= (uint32_t)seg_first[j + 1] << 16;
+        }
+        out[i] = v;
+    }
+}
+
+int scatter_tc_table_capacity() { return kTab; }
+int scatter_tc_info_words(int nseg) { return info_words(nseg); }
+
+void launch_adj_tabinfo(const GeoDev &gd, cudaStream_t s) {
+    if (gd.n_adj_tabs == 0) return;
+    k_adj_tabinfo<<<gd.n_adj_tabs, kTab, 0, s>>>(gd.adj_recs, gd.adj_tabs, gd.adj_info);
+    LAUNCH_CHECK("k_adj_tabinfo");
+}
+
 __global__ void __launch_bounds__(kThr, 1)
     k_scatter_tc(const float2 *__restrict__ rowsc, float2 *__restrict__ spec, const AdjRec *__restrict__ recs,
-                 const int4 *__restrict__ items, const float2 *__restrict__ kmat, const float2 *__restrict__ shifta,
-                 UsGeo g, int zb, int npairs, int nunits, int jbase, int *__restrict__ err) {
+                 const int4 *__restrict__ items, const int4 *__restrict__ tabs, const int *__restrict__ tab_base,
+                 const uint32_t *__restrict__ info, const float2 *__restrict__ kmat,
+                 const float2 *__restrict__ shifta, UsGeo g, int zb, int npairs, int nunits, int jbase,
+                 int *__restrict__ err) {
     extern __shared__ __align__(1024) unsigned char sc_smem_raw[];
     ScTcSmem &sm = *reinterpret_cast<ScTcSmem *>(sc_smem_raw);
     const int P = g.P, hn = g.n / 2 + 1;
@@ -190,15 +282,26 @@ __global__ void __launch_bounds__(kThr, 1)
     // Thread 0's copy cursor: the next table (unit, first entry) to fetch, in
     // the order the tables are consumed; a table is fetched while the one
     // before it is processed.
-    int fu = blockIdx.x, fc0 = 0;
-    auto fetch = [&](int slot) {
+    int fu = blockIdx.x, ft = 0;
+    auto fetch = [&](int slot) {  // records and segmentation of table ft of unit fu
         if (fu >= nunits) return;
-        const int4 fit = __ldg(items + fu / npairs);
-        const uint32_t bytes = (uint32_t)min(kTab, fit.z - fc0) * (uint32_t)sizeof(AdjRec);
-        tc::bulk_g2s(sm.rec[slot], recs + (long long)fit.y + fc0, bytes, &sm.rbar[slot]);
-        fc0 += kTab;
-        if (fc0 >= fit.z) {
-            fc0 = 0;
+        const int item = fu / npairs;
+        const int tb0 = __ldg(tab_base + item), tb1 = __ldg(tab_base + item + 1);
+        const int4 tb = __ldg(tabs + tb0 + ft);
+        const uint32_t rbytes = (uint32_t)tb.y * (uint32_t)sizeof(AdjRec), ibytes = (uint32_t)tb.w * 4u;
+        const uint32_t bar = tc::smem_addr(&sm.rbar[slot]);
+        asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(bar), "r"(rbytes + ibytes)
+                     : "memory");
+        asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];\n" ::"r"(
+                         tc::smem_addr(sm.rec[slot])),
+                     "l"(recs + tb.x), "r"(rbytes), "r"(bar)
+                     : "memory");
+        asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];\n" ::"r"(
+                         tc::smem_addr(sm.info[slot])),
+                     "l"(info + tb.z), "r"(ibytes), "r"(bar)
+                     : "memory");
+        if (++ft >= tb1 - tb0) {
+            ft = 0;
             fu += gridDim.x;
         }
     };
@@ -231,66 +334,26 @@ __global__ void __launch_bounds__(kThr, 1)
             ok = tc::mbar_wait(&sm.rbar[buf], (uint32_t)((seq >> 1) & 1)) && ok;
             ++seq;
             const AdjRec *rec = sm.rec[buf];
-            // ---- E = (-1)^(k+1) shiftadj(k) FFT(row)(k) (pi/mu)/n, then T_p(cy) = E(p) wy_p(cy) ----
+            const uint32_t *inf = sm.info[buf];
+            const int nseg = min((int)inf[0], cnt);  // (clamps keep every index inside the table)
+            const uint16_t *segf = reinterpret_cast<const uint16_t *>(inf + 4 + 8 * nseg);  // ray starts
+            // ---- E = (-1)^(k+1) shiftadj(k) FFT(row)(k) (pi/mu)/n and T_p(cy) = E(p) wy_p(cy),
+            // stored [row][entry] so that this thread writes its own entry's column ----
             if (have_next) asm volatile("cp.async.wait_all;\n" ::: "memory");  // this thread's own entry
             if (ct < cnt) {
                 const int th = (unsigned)rec[ct].thm >> 16, k = rec[ct].k;
                 float2 R = make_float2(0.f, 0.f);
                 if (zok) R = have_next ? sm.rnext[h][ct] : __ldg(rz + (long long)th * hn + (k <= g.n / 2 ? k : g.n - k));
                 if (k > g.n / 2) R.y = -R.y;
-                sm.e[h][ct] = cmul(R, rec[ct].sf);
-            }
-            __syncthreads();
-            for (int i = ct; i < cnt * kT; i += kHalf) {
-                const int e = i >> 4, row = i & 15;
-                const float2 E = sm.e[h][e];
-                const float w = rec[e].wy[row];
-                sm.t[h][e][row] = make_float2(E.x * w, E.y * w);
-            }
-            // ---- first table row of each ray: scan of ray starts (half 0) ----
-            int flag = 0;
-            if (h == 0 && ct < cnt) flag = (ct == 0 || (rec[ct].thm >> 16) != (rec[ct - 1].thm >> 16)) ? 1 : 0;
-            int incl = flag;
+                const float2 E = cmul(R, rec[ct].sf);
+                const float4 *wy4 = reinterpret_cast<const float4 *>(rec[ct].wy);
 #pragma unroll
-            for (int o = 1; o < 32; o <<= 1) {
-                const int y = __shfl_up_sync(0xffffffffu, incl, o);
-                if (lane >= o) incl += y;
-            }
-            if (h == 0 && lane == 31) sm.wsum[hw] = incl;
-            __syncthreads();
-            int base = 0, nseg = 0;
-#pragma unroll
-            for (int w = 0; w < kHW; ++w) {
-                const int v = sm.wsum[w];
-                base += (w < hw) ? v : 0;
-                nseg += v;
-            }
-            incl += base;
-            const int seg = incl - 1;  // ray (segment) of this thread's sample (half 0)
-            if (h == 0 && ct < cnt && flag) {
-                sm.seg_first[seg] = ct;
-#pragma unroll
-                for (int w = 0; w < kHW; ++w) {
-                    sm.rlo[w][seg] = kTab;
-                    sm.rhi[w][seg] = 0;
-                }
-            }
-            if (tid == 0) sm.seg_first[nseg] = cnt;
-            __syncthreads();  // ray starts, empty ranges and T written
-            // ---- per warp and ray: first and last sample covering the warp's
-            // rows, from the samples where a covered run starts or ends ----
-            if (h == 0 && ct < cnt) {
-                const int msk = rec[ct].thm & 0xffff;
-                const int mprev = flag ? 0 : (rec[ct - 1].thm & 0xffff);
-                const bool last = ct + 1 == cnt || (rec[ct + 1].thm >> 16) != (rec[ct].thm >> 16);
-                const int mnext = last ? 0 : (rec[ct + 1].thm & 0xffff);
-#pragma unroll
-                for (int w = 0; w < kHW; ++w) {
-                    const int bits = 3 << (2 * w);
-                    if (msk & bits) {
-                        if (!(mprev & bits)) atomicMin(&sm.rlo[w][seg], ct);
-                        if (!(mnext & bits)) atomicMax(&sm.rhi[w][seg], ct + 1);
-                    }
+                for (int q4 = 0; q4 < kT / 4; ++q4) {
+                    const float4 w = wy4[q4];
+                    sm.t[h][4 * q4 + 0][ct] = make_float2(E.x * w.x, E.y * w.x);
+                    sm.t[h][4 * q4 + 1][ct] = make_float2(E.x * w.y, E.y * w.y);
+                    sm.t[h][4 * q4 + 2][ct] = make_float2(E.x * w.z, E.y * w.z);
+                    sm.t[h][4 * q4 + 3][ct] = make_float2(E.x * w.w, E.y * w.w);
                 }
             }
             // ---- the next table's row spectrum values, copied while this
@@ -332,7 +395,8 @@ __global__ void __launch_bounds__(kThr, 1)
                     const int r = 2 * bq4 + i;
                     kv[i] = make_float2(0.f, 0.f);
                     if (h == 0 && r < nb && jbase + bj < g.m)
-                        kv[i] = __ldg(kmat + (long long)((unsigned)rec[sm.seg_first[sb + r]].thm >> 16) * g.m + jbase + bj);
+                        kv[i] = __ldg(kmat + (long long)((unsigned)rec[min((int)segf[sb + r], cnt - 1)].thm >> 16) * g.m +
+                                      jbase + bj);
                 }
                 // ---- 1. V(c, ray) of this cell for rays [8h, 8h + 8) of the
                 // batch, both slices of the pair (one weight load, two FMAs) ----
@@ -343,12 +407,13 @@ __global__ void __launch_bounds__(kThr, 1)
                     const int rr = kRH * h + r;
                     float2 a = make_float2(0.f, 0.f), b = make_float2(0.f, 0.f);
                     if (rr < nb) {  // T and wx vanish outside the stencil: no tests in the loop
-                        const int e1 = sm.rhi[hw][sb + rr];
+                        const uint32_t lohi = inf[4 + 8 * (sb + rr) + hw];
+                        const int e1 = min((int)(lohi >> 16), cnt);
 #pragma unroll 4
-                        for (int e = sm.rlo[hw][sb + rr]; e < e1; ++e) {
+                        for (int e = (int)(lohi & 0xffffu); e < e1; ++e) {
                             const float w = rec[e].wx[cx];
-                            a = ffma2(make_float2(w, w), sm.t[0][e][cy], a);
-                            b = ffma2(make_float2(w, w), sm.t[1][e][cy], b);
+                            a = ffma2(make_float2(w, w), sm.t[0][cy][e], a);
+                            b = ffma2(make_float2(w, w), sm.t[1][cy][e], b);
                         }
                     }
                     v0[2 * r] = a.x;
@@ -487,8 +552,10 @@ void launch_scatter_tc(const float2 *rowsc, float2 *spec, int zb, const GeoDev &
         CUDA_CHECK(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
     }
     const int grid = (int)std::min<long long>(nunits, nsm);
-    k_scatter_tc<<<grid, kThr, kScSmemBytes, s>>>(rowsc, spec, gd.adj_recs, gd.adj_items, gd.kmat, gd.shiftadj, g,
-                                                  zb, npairs, (int)nunits, jbase, gd.err);
+    if (!gd.adj_tabs || !gd.adj_info) throw Error(1, "adjoint table segmentation missing");
+    k_scatter_tc<<<grid, kThr, kScSmemBytes, s>>>(rowsc, spec, gd.adj_recs, gd.adj_items, gd.adj_tabs,
+                                                  gd.adj_tab_base, gd.adj_info, gd.kmat, gd.shiftadj, g, zb, npairs,
+                                                  (int)nunits, jbase, gd.err);
     LAUNCH_CHECK("k_scatter_tc");
 }
 
