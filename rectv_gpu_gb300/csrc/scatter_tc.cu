@@ -356,31 +356,6 @@ __global__ void __launch_bounds__(kThr, 1)
                     sm.t[h][4 * q4 + 3][ct] = make_float2(E.x * w.w, E.y * w.w);
                 }
             }
-            // ---- the next table's row spectrum values, copied while this
-            // table's batches run (its records were fetched at this table's start) ----
-            {
-                int nc0 = c0 + kTab, nu = u;
-                if (nc0 >= it.z) {
-                    nc0 = 0;
-                    nu = u + gridDim.x;
-                }
-                have_next = nu < nunits;
-                if (have_next) {
-                    const int4 nit = nu == u ? it : __ldg(items + nu / npairs);
-                    const int nz = 2 * (nu % npairs) + h;
-                    ok = tc::mbar_wait(&sm.rbar[buf ^ 1], (uint32_t)((seq >> 1) & 1)) && ok;
-                    if (nz < zb && ct < min(kTab, nit.z - nc0)) {
-                        const float2 *nrz = rowsc + (long long)nz * g.ntheta * hn;
-                        const AdjRec &nr = sm.rec[buf ^ 1][ct];
-                        const int th = (unsigned)nr.thm >> 16, k = nr.k;
-                        const float2 *src = nrz + (long long)th * hn + (k <= g.n / 2 ? k : g.n - k);
-                        asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(tc::smem_addr(&sm.rnext[h][ct])),
-                                     "l"(src)
-                                     : "memory");
-                        asm volatile("cp.async.commit_group;\n" ::: "memory");
-                    }
-                }
-            }
             __syncthreads();
 
             for (int sb = 0; sb < nseg; sb += kBatch) {
@@ -420,6 +395,32 @@ __global__ void __launch_bounds__(kThr, 1)
                     v0[2 * r + 1] = a.y;
                     v1[2 * r] = b.x;
                     v1[2 * r + 1] = b.y;
+                }
+                // ---- the next table's row spectrum values, copied while this
+                // table's batches run: after the first batch's ray sums, by
+                // which time the next records (fetched at this table's start) have landed ----
+                if (sb == 0) {
+                    int nc0 = c0 + kTab, nu = u;
+                    if (nc0 >= it.z) {
+                        nc0 = 0;
+                        nu = u + gridDim.x;
+                    }
+                    have_next = nu < nunits;
+                    if (have_next) {
+                        const int4 nit = nu == u ? it : __ldg(items + nu / npairs);
+                        const int nz = 2 * (nu % npairs) + h;
+                        ok = tc::mbar_wait(&sm.rbar[buf ^ 1], (uint32_t)((seq >> 1) & 1)) && ok;
+                        if (nz < zb && ct < min(kTab, nit.z - nc0)) {
+                            const float2 *nrz = rowsc + (long long)nz * g.ntheta * hn;
+                            const AdjRec &nr = sm.rec[buf ^ 1][ct];
+                            const int th = (unsigned)nr.thm >> 16, k = nr.k;
+                            const float2 *src = nrz + (long long)th * hn + (k <= g.n / 2 ? k : g.n - k);
+                            asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(tc::smem_addr(&sm.rnext[h][ct])),
+                                         "l"(src)
+                                         : "memory");
+                            asm volatile("cp.async.commit_group;\n" ::: "memory");
+                        }
+                    }
                 }
                 // ---- previous batch's MMAs done: add its product to the cell's
                 // FP32 sums; A, B and the accumulator are then free ----
