@@ -83,7 +83,7 @@ constexpr int kInfoMax = info_words(kTab);
 struct ScTcSmem {
     AdjRec rec[2][kTab];          // geometry records of this table and the next (bulk copies)
     uint32_t info[2][kInfoMax];   // their ray segmentation (bulk copies)
-    float2 t[kZ][kT][kTab];       // T_p(cy) = E(p) wy_p(cy), per slice of the pair
+    float4 t[kT][kTab];           // T_p(cy) = E(p) wy_p(cy) of both slices of the pair (x, y | z, w)
     float2 rnext[kZ][kTab];       // row spectrum values of the next table's samples (cp.async)
     float bhi[kN * kK];           // B = conj K' of the batch's rays, FP32: rows 0..31 of the MMA's B
     float blo[kN * kK];           // B - trunc(B): rows 32..63 (contiguous with bhi)
@@ -350,10 +350,10 @@ __global__ void __launch_bounds__(kThr, 1)
 #pragma unroll
                 for (int q4 = 0; q4 < kT / 4; ++q4) {
                     const float4 w = wy4[q4];
-                    sm.t[h][4 * q4 + 0][ct] = make_float2(E.x * w.x, E.y * w.x);
-                    sm.t[h][4 * q4 + 1][ct] = make_float2(E.x * w.y, E.y * w.y);
-                    sm.t[h][4 * q4 + 2][ct] = make_float2(E.x * w.z, E.y * w.z);
-                    sm.t[h][4 * q4 + 3][ct] = make_float2(E.x * w.w, E.y * w.w);
+                    reinterpret_cast<float2 *>(&sm.t[4 * q4 + 0][ct])[h] = make_float2(E.x * w.x, E.y * w.x);
+                    reinterpret_cast<float2 *>(&sm.t[4 * q4 + 1][ct])[h] = make_float2(E.x * w.y, E.y * w.y);
+                    reinterpret_cast<float2 *>(&sm.t[4 * q4 + 2][ct])[h] = make_float2(E.x * w.z, E.y * w.z);
+                    reinterpret_cast<float2 *>(&sm.t[4 * q4 + 3][ct])[h] = make_float2(E.x * w.w, E.y * w.w);
                 }
             }
             __syncthreads();
@@ -374,7 +374,7 @@ __global__ void __launch_bounds__(kThr, 1)
                                       jbase + bj);
                 }
                 // ---- 1. V(c, ray) of this cell for rays [8h, 8h + 8) of the
-                // batch, both slices of the pair (one weight load, two FMAs) ----
+                // batch, both slices of the pair (one weight load, one T load, two FMAs) ----
                 constexpr int kRH = kBatch / kZ;  // rays per half
                 float v0[2 * kRH], v1[2 * kRH];
 #pragma unroll
@@ -387,8 +387,9 @@ __global__ void __launch_bounds__(kThr, 1)
 #pragma unroll 4
                         for (int e = (int)(lohi & 0xffffu); e < e1; ++e) {
                             const float w = rec[e].wx[cx];
-                            a = ffma2(make_float2(w, w), sm.t[0][cy][e], a);
-                            b = ffma2(make_float2(w, w), sm.t[1][cy][e], b);
+                            const float4 tv = sm.t[cy][e];  // both slices in one load
+                            a = ffma2(make_float2(w, w), make_float2(tv.x, tv.y), a);
+                            b = ffma2(make_float2(w, w), make_float2(tv.z, tv.w), b);
                         }
                     }
                     v0[2 * r] = a.x;
