@@ -48,6 +48,8 @@ constexpr int kT = 16;                       // floor tile side
 constexpr int kFW = kT + 2 * kR;             // footprint side (24)
 constexpr int kBoxW = kFW + 2;               // box width: even start column of a mirrored footprint
 constexpr int kCells = kFW * kFW;            // 576
+constexpr int kGP = kFW + 1;                 // row pitch of G in shared memory (25: the four threads
+                                             // of a sample read rows 8 B x 25 apart, on distinct banks)
 constexpr int kMT = (kCells + 127) / 128;    // M tiles of 128 cells (5)
 constexpr int kRays = 16;                    // rays per chunk
 constexpr int kN = 2 * kRays;                // MMA N (32)
@@ -70,7 +72,7 @@ __device__ __forceinline__ int off32(int row, int kk) {
 
 struct TcSmem {
     float2 box[16][kFW][kBoxW];          // TMA destination: 16 time samples x 24 rows x 26 cells
-    float2 g[kRays][kCells];             // G of the current chunk's rays
+    float2 g[kRays][kFW * kGP];          // G of the current chunk's rays, cell (row, col) at row * kGP + col
     float bhi[2][kN * kK];               // B = K' rows, FP32 (double-buffered)
     float blo[2][kN * kK];               // B - trunc(B)
     float wx[kTab][12];                  // (-1)^b w_b of the 9 x taps
@@ -165,7 +167,7 @@ __global__ void __launch_bounds__(kThr, 1)
             atomicAdd(err, 1);
             sm.pos[e] = -1;
         } else {
-            sm.pos[e] = ly0 * kFW + lx0;
+            sm.pos[e] = ly0 * kGP + lx0;
         }
         sm.th[e] = th;
         sm.k[e] = k;
@@ -337,20 +339,20 @@ __global__ void __launch_bounds__(kThr, 1)
                 const int mt = wid >> 2;
                 float v[32];
                 tc::ld32(tbase + ((uint32_t)(32 * q) << 16) + kColD + mt * kN, v);
-                const int cell = mt * 128 + 32 * q + lane;
+                const int cell = mt * 128 + 32 * q + lane, gc = cell + cell / kFW;
 #pragma unroll
                 for (int r = 0; r < kRays; ++r)
-                    if (r < nr) sm.g[r][cell] = make_float2(v[2 * r], v[2 * r + 1]);
+                    if (r < nr) sm.g[r][gc] = make_float2(v[2 * r], v[2 * r + 1]);
             }
             static_assert(kMT == 5 && kCells - 4 * 128 <= 64 && kWarps == 16, "G read-out split");
             if (q < 2) {
                 const int r0 = 4 * (wid >> 2);  // rays r0 .. r0 + 3
                 float v[8];
                 tc::ld8(tbase + ((uint32_t)(32 * q) << 16) + kColD + 4 * kN + 2 * r0, v);
-                const int cell = 4 * 128 + 32 * q + lane;
+                const int cell = 4 * 128 + 32 * q + lane, gc = cell + cell / kFW;
 #pragma unroll
                 for (int r = 0; r < 4; ++r)
-                    if (r0 + r < nr) sm.g[r0 + r][cell] = make_float2(v[2 * r], v[2 * r + 1]);
+                    if (r0 + r < nr) sm.g[r0 + r][gc] = make_float2(v[2 * r], v[2 * r + 1]);
             }
             tc::fence_before();
             __syncthreads();
@@ -385,7 +387,7 @@ __global__ void __launch_bounds__(kThr, 1)
                     for (int i = 0; i < 3; ++i) {
                         const int a = part + 4 * i;
                         if (a < kTaps) {
-                            const float2 *gr = gp + a * kFW;
+                            const float2 *gr = gp + a * kGP;
                             float2 rr = make_float2(0.f, 0.f);
 #pragma unroll
                             for (int b = 0; b < kTaps; ++b) rr = ffma2(make_float2(ex[b], ex[b]), gr[b], rr);
