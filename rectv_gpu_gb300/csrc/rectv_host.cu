@@ -429,17 +429,28 @@ struct Handle {
             // tables of the busy items and the size of their ray segmentation
             const int cap = scatter_tc_table_capacity();
             long long words = 0;
+            // a table holds whole rays (runs of equal theta), at most one MMA
+            // batch of them (scatter_tc_batch_rays()) and at most cap entries
+            const int max_rays = scatter_tc_batch_rays();
             for (int i = 0; i < gd.n_adj_busy; ++i) {
                 const int4 it = hp.adj_items[i];
-                for (int c0 = 0; c0 < it.z; c0 += cap) {
-                    const int cnt = std::min(cap, it.z - c0);
-                    const uint32_t *pts = hp.adj_pts.data() + it.y + c0;
-                    int nseg = 1;
-                    for (int e = 1; e < cnt; ++e) nseg += (pts[e] / (uint32_t)n != pts[e - 1] / (uint32_t)n) ? 1 : 0;
+                const uint32_t *pts = hp.adj_pts.data() + it.y;
+                int c0 = 0;
+                while (c0 < it.z) {
+                    int c1 = c0, nseg = 0;
+                    while (c1 < it.z) {
+                        int r = c1 + 1;  // end of the ray starting at c1
+                        while (r < it.z && pts[r] / (uint32_t)n == pts[c1] / (uint32_t)n) ++r;
+                        if (nseg > 0 && (nseg == max_rays || r - c0 > cap)) break;
+                        if (r - c0 > cap) r = c0 + cap;  // a ray longer than a table is split
+                        c1 = r;
+                        ++nseg;
+                    }
                     const int w = scatter_tc_info_words(nseg);
-                    tabs.push_back(make_int4(it.y + c0, cnt, (int)words, w));
+                    tabs.push_back(make_int4(it.y + c0, c1 - c0, (int)words, w));
                     words += w;
                     if (words > 2147483647LL) throw Error(RECTV_ERR_ARG, "rectv: adjoint plan too large");
+                    c0 = c1;
                 }
                 tab_base.push_back((int)tabs.size());
             }

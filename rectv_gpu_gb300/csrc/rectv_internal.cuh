@@ -97,8 +97,9 @@ struct GeoDev {
     bool tc_scatter = false;     // adjoint time-sample mixing on the tensor cores (k_scatter_tc)
     AdjRec *adj_recs = nullptr;  // geometry records of adj_pts (tensor-core scatter only)
     int n_adj_busy = 0;          // leading adj_items with samples (items are sorted by count)
-    // tensor-core scatter tables: each busy item's entries in runs of
-    // scatter_tc_table_capacity(); item i owns tables [adj_tab_base[i],
+    // tensor-core scatter tables: each busy item's entries in runs of whole
+    // rays (at most one MMA batch of rays and scatter_tc_table_capacity()
+    // entries); item i owns tables [adj_tab_base[i],
     // adj_tab_base[i+1]); adj_tabs = (first entry, count, segmentation offset
     // and size in 32-bit words); adj_info = the tables' ray segmentation
     int4 *adj_tabs = nullptr;
@@ -158,6 +159,7 @@ void launch_adj_records(AdjRec *recs, const GeoDev &gd, const UsGeo &g, cudaStre
 // entries per scatter table, and the 32-bit words of a table's segmentation
 // with nseg rays (count, per-warp sample ranges, ray starts)
 int scatter_tc_table_capacity();
+int scatter_tc_batch_rays();  // rays per tensor-core batch
 int scatter_tc_info_words(int nseg);
 // fill adj_info from the records (after launch_adj_records)
 void launch_adj_tabinfo(const GeoDev &gd, cudaStream_t s);

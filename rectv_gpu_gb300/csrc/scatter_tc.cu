@@ -241,6 +241,7 @@ __global__ void __launch_bounds__(kTab)
 }
 
 int scatter_tc_table_capacity() { return kTab; }
+int scatter_tc_batch_rays() { return kBatch; }
 int scatter_tc_info_words(int nseg) { return info_words(nseg); }
 
 void launch_adj_tabinfo(const GeoDev &gd, cudaStream_t s) {
@@ -323,8 +324,9 @@ __global__ void __launch_bounds__(kThr, 1)
 #pragma unroll
         for (int i = 0; i < 32; ++i) acc[i] = 0.f;
 
-        for (int c0 = 0; c0 < it.z; c0 += kTab) {
-            const int cnt = min(kTab, it.z - c0);
+        const int tb0 = __ldg(tab_base + u / npairs), tb1 = __ldg(tab_base + u / npairs + 1);
+        for (int ti = tb0; ti < tb1; ++ti) {
+            const int cnt = __ldg(tabs + ti).y;
             const int buf = seq & 1;
             __syncthreads();  // previous table consumed: its buffer takes the next one
             if (tid == 0) {
@@ -401,17 +403,17 @@ __global__ void __launch_bounds__(kThr, 1)
                 // table's batches run: after the first batch's ray sums, by
                 // which time the next records (fetched at this table's start) have landed ----
                 if (sb == 0) {
-                    int nc0 = c0 + kTab, nu = u;
-                    if (nc0 >= it.z) {
-                        nc0 = 0;
+                    int nti = ti + 1, nu = u;
+                    if (nti >= tb1) {
                         nu = u + gridDim.x;
+                        nti = nu < nunits ? __ldg(tab_base + nu / npairs) : 0;
                     }
                     have_next = nu < nunits;
                     if (have_next) {
-                        const int4 nit = nu == u ? it : __ldg(items + nu / npairs);
+                        const int ncnt = __ldg(tabs + nti).y;
                         const int nz = 2 * (nu % npairs) + h;
                         ok = tc::mbar_wait(&sm.rbar[buf ^ 1], (uint32_t)((seq >> 1) & 1)) && ok;
-                        if (nz < zb && ct < min(kTab, nit.z - nc0)) {
+                        if (nz < zb && ct < ncnt) {
                             const float2 *nrz = rowsc + (long long)nz * g.ntheta * hn;
                             const AdjRec &nr = sm.rec[buf ^ 1][ct];
                             const int th = (unsigned)nr.thm >> 16, k = nr.k;
