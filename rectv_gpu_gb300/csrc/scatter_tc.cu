@@ -328,7 +328,8 @@ __global__ void __launch_bounds__(kThr, 1)
         for (int ti = tb0; ti < tb1; ++ti) {
             const int cnt = __ldg(tabs + ti).y;
             const int buf = seq & 1;
-            __syncthreads();  // previous table consumed: its buffer takes the next one
+            // the other record buffer and T are free: every thread has passed
+            // the barrier in front of the previous table's MMAs, after its ray sums
             if (tid == 0) {
                 tc::fence_proxy_async();
                 fetch(buf ^ 1);
