@@ -470,9 +470,10 @@ __global__ void __launch_bounds__(kThr, 1)
                 tc::fence_proxy_async();
                 tc::fence_before();
                 __syncthreads();
-                // one issuing thread per (slice, M tile) accumulator chain, two
-                // rotating warps per half, so that no warp carries all issues
-                const int iw = (2 * nmma) % kHW;
+                // one issuing thread per (slice, M tile) accumulator chain: lane 0
+                // of the last two warps of each half, whose table entries (rows
+                // 192-255) are idle in the next table's E/T phase for most tables
+                constexpr int iw = kHW - 2;
                 if (lane == 0 && (hw == iw || hw == iw + 1)) {
                     tc::fence_after();
                     // D = [Ahi Bhi, Ahi Blo] + [Alo Bhi, Alo Blo]: both halves summed when read
