@@ -91,6 +91,7 @@ struct Handle {
     float *U[3] = {nullptr, nullptr, nullptr};
     float *gdata = nullptr;
     float *psi = nullptr, *mu = nullptr;
+    float *wdual = nullptr;  // w = mu - rho psi of the current outer iteration (psi's layout)
     float *h1 = nullptr;
     float2 *spec = nullptr;
     float2 *rows = nullptr;
@@ -207,6 +208,8 @@ struct Handle {
         gdata = dalloc<float>((size_t)nz * ntheta * n, owned);
         psi = dalloc<float>((size_t)4 * nchunks * gp, owned);
         mu = dalloc<float>((size_t)4 * nchunks * gp, owned);
+        wdual = dalloc<float>((size_t)4 * nchunks * gp, owned);
+        CUDA_CHECK(cudaMemsetAsync(wdual, 0, sizeof(float) * (size_t)4 * nchunks * gp, stream));
         h1 = dalloc<float>((size_t)zb * ntheta * n, owned);
         // spectra; also the float4 gradient scratch of check_adjoints
         const size_t spec_elems = std::max<size_t>(
@@ -585,7 +588,9 @@ struct Handle {
                 const long long z0 = (long long)bb * zb;
                 const int c0 = bb * dpb;
                 forward(U[src] + z0 * slab, gdata + z0 * ntheta * n, h1, 1.0f, 1);
-                launch_graddiv(U[src], U[old], U[dst], psi, mu, rho_d, c0, nchunks, tv, stream);
+                // first inner step: psi, mu in, w = mu - rho psi out; later steps: w in
+                const int gmode = titer > 1 ? (k == 0 ? 1 : 2) : 0;
+                launch_graddiv(U[src], U[old], U[dst], psi, mu, wdual, gmode, rho_d, c0, nchunks, tv, stream);
                 adjoint(h1, U[dst] + z0 * slab, -0.5f);
             }
             src = dst;
@@ -883,7 +888,10 @@ struct Handle {
             switch (which) {
                 case 0: launch_gather_fwd(spec, rows, zb, gd, ug, &spec_tmap, stream); break;
                 case 1: launch_scatter_adj(rows, spec, zb, gd, ug, stream); break;
-                case 2: launch_graddiv(U[cur], U[cur], U[(cur + 1) % 3], psi, mu, rho_d, 0, nchunks, tv, stream); break;
+                case 2:  // the inner steps after the first (w = mu - rho psi as stored by the last iteration)
+                    launch_graddiv(U[cur], U[cur], U[(cur + 1) % 3], psi, mu, wdual, titer > 1 ? 2 : 0, rho_d, 0,
+                                   nchunks, tv, stream);
+                    break;
                 case 3:  // overwrites the session's dual variables
                     launch_shrink(U[cur], U[cur], psi, mu, rho_d, lambda0, 0, nchunks, tv, partials, stream);
                     break;

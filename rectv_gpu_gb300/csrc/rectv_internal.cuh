@@ -194,10 +194,12 @@ struct TvGeo {
     float lambda1;
 };
 
-// u_out = u_in - 0.5 * div(rho (G u_in - psi) + mu) for chunks [c0, c0+nchunks)
+// u_out = u_in - 0.5 * div(rho (G u_in - psi) + mu) for chunks [c0, c0+nchunks);
+// mode 0 reads psi and mu, mode 1 also stores w = mu - rho psi (psi's layout),
+// mode 2 reads w only (psi, mu and rho unchanged since the mode-1 step)
 void launch_graddiv(const float *u_in, const float *u_old, float *u_out, const float *psi,
-                    const float *mu, const float *rho, int c0, int nchunks_total, const TvGeo &t,
-                    cudaStream_t s);
+                    const float *mu, float *w, int mode, const float *rho, int c0, int nchunks_total,
+                    const TvGeo &t, cudaStream_t s);
 // shrink + dual update + residual sums into per-block partials
 int launch_shrink(const float *u_cur, const float *u_old, float *psi, float *mu, const float *rho,
                   float lambda0, int c0, int nchunks_total, const TvGeo &t, double *partials,

@@ -58,19 +58,23 @@ __device__ __forceinline__ void block_reduce3(double a, double b, double c, doub
 // ---------------------------------------------------------------------------
 // Fused inner step (gradient, lin4, divergent of admm.cu:85-95 with tau=-0.5):
 //   u_out(v) = u_in(v) + tau sd sum_d [h_d(q-e_d) - h_d(q)],  q = v+1,
-//   h = rho (G u_in - psi) + mu.
+//   h = rho (G u_in - psi) + mu = rho G u_in + w,  w = mu - rho psi.
+// psi, mu and rho change only at the end of an outer iteration, so the first
+// inner step (MODE 1) reads psi and mu and also stores w for every dual point
+// the step reads, and the later ones (MODE 2) read w alone (half the dual
+// bytes); MODE 0 reads psi and mu only.
 // One thread per (x, y, slice), marching along t: h_t(q - e_t) is the previous
 // time point's h_t(q), kept in a register, and the loads of time point t+1
 // are issued before t is computed.  Blocks of 256 x-voxels; the grid runs
 // over (x blocks, slices, rows) in that order, so the blocks that read a
 // block's z-1 and y-1 dual neighbours run at the same time (L2 hits rather
-// than second HBM reads).  Every value is computed with the same float
-// expression as the per-voxel form, so results do not depend on the order.
+// than second HBM reads).
 // ---------------------------------------------------------------------------
+template <int MODE>
 __global__ void __launch_bounds__(256, 3)
     k_graddiv(const float *__restrict__ uin, const float *__restrict__ uold, float *__restrict__ uout,
-              const float *__restrict__ psi, const float *__restrict__ mu, const float *__restrict__ rhop,
-              TvGeo t, int c0, int nch_total, float tau) {
+              const float *__restrict__ psi, const float *__restrict__ mu, float *__restrict__ w,
+              const float *__restrict__ rhop, TvGeo t, int c0, int nch_total, float tau) {
     const int x = blockIdx.x * blockDim.x + threadIdx.x;
     const int zr = blockIdx.y;
     const int y = blockIdx.z;
@@ -90,8 +94,10 @@ __global__ void __launch_bounds__(256, 3)
     const long long cs = t.comp_stride;
     const long long q0 = (long long)c * t.gp + (zl + 1) * sz + st + (y + 1) * sy + (x + 1);  // q of t = 0
     const float sg = t.sg, sgt = t.sg * t.lambda1;
-    // a[]: u at x+1, x-1, y+1, y-1, z+1, z-1, t+1; psi, mu at q (4 components
-    // each); psi, mu of component x at q-sx, y at q-sy, z at q-sz
+    // a[]: u at x+1, x-1, y+1, y-1, z+1, z-1, t+1; then the dual values: at q
+    // (4 components) and of component x at q-sx, y at q-sy, z at q-sz, as
+    // (psi, mu) pairs (MODE 0, 1: a[7..10] psi, a[11..14] mu, a[15..20]
+    // psi/mu pairs) or w alone (MODE 2: a[7..10] w, a[15], a[17], a[19])
     auto load = [&](int tt, float(&a)[21]) {
         const long long o = (long long)tt * nn;
         const long long q = q0 + (long long)tt * st;
@@ -102,45 +108,75 @@ __global__ void __launch_bounds__(256, 3)
         a[4] = uzp[o];
         a[5] = uzm[o];
         a[6] = u[o + (tt < m - 1 ? nn : 0)];
+        if constexpr (MODE == 2) {
 #pragma unroll
-        for (int i = 0; i < 4; ++i) {
-            a[7 + i] = psi[i * cs + q];
-            a[11 + i] = mu[i * cs + q];
+            for (int i = 0; i < 4; ++i) a[7 + i] = w[i * cs + q];
+            a[15] = w[q - sx];
+            a[17] = w[cs + q - sy];
+            a[19] = w[3 * cs + q - sz];
+        } else {
+#pragma unroll
+            for (int i = 0; i < 4; ++i) {
+                a[7 + i] = psi[i * cs + q];
+                a[11 + i] = mu[i * cs + q];
+            }
+            a[15] = psi[q - sx];
+            a[16] = mu[q - sx];
+            a[17] = psi[cs + q - sy];
+            a[18] = mu[cs + q - sy];
+            a[19] = psi[3 * cs + q - sz];
+            a[20] = mu[3 * cs + q - sz];
         }
-        a[15] = psi[q - sx];
-        a[16] = mu[q - sx];
-        a[17] = psi[cs + q - sy];
-        a[18] = mu[cs + q - sy];
-        a[19] = psi[3 * cs + q - sz];
-        a[20] = mu[3 * cs + q - sz];
+    };
+    // h of one component from the gradient term g and the dual values
+    auto hval = [&](float g, const float(&a)[21], int ip, int im) {
+        if constexpr (MODE == 2)
+            return rho * g + a[ip];
+        else
+            return rho * (g - a[ip]) + a[im];
     };
     float cur[21];
     load(0, cur);
     float f0 = u[0];
     // h_t at q - st for t = 0: the clamped backward difference is zero
-    float hmt = rho * (sgt * (f0 - f0) - psi[2 * cs + q0 - st]) + mu[2 * cs + q0 - st];
+    float hmt;
+    if constexpr (MODE == 2) {
+        hmt = rho * (sgt * (f0 - f0)) + w[2 * cs + q0 - st];
+    } else {
+        const float p0 = psi[2 * cs + q0 - st], m0 = mu[2 * cs + q0 - st];
+        hmt = rho * (sgt * (f0 - f0) - p0) + m0;
+        if constexpr (MODE == 1) w[2 * cs + q0 - st] = m0 - rho * p0;
+    }
     for (int tt = 0; tt < m; ++tt) {
         float nxt[21];
         if (tt + 1 < m) load(tt + 1, nxt);
+        if constexpr (MODE == 1) {  // w at q, and at the lower boundary planes this voxel reads
+            const long long q = q0 + (long long)tt * st;
+#pragma unroll
+            for (int i = 0; i < 4; ++i) w[i * cs + q] = cur[11 + i] - rho * cur[7 + i];
+            if (x == 0) w[q - sx] = cur[16] - rho * cur[15];
+            if (y == 0) w[cs + q - sy] = cur[18] - rho * cur[17];
+            if (zl == 0) w[3 * cs + q - sz] = cur[20] - rho * cur[19];
+        }
         float d;
         {  // x
-            const float hq = rho * (sg * (cur[0] - f0) - cur[7]) + cur[11];
-            const float hm = rho * (sg * (f0 - cur[1]) - cur[15]) + cur[16];
+            const float hq = hval(sg * (cur[0] - f0), cur, 7, 11);
+            const float hm = hval(sg * (f0 - cur[1]), cur, 15, 16);
             d = hm - hq;
         }
         {  // y
-            const float hq = rho * (sg * (cur[2] - f0) - cur[8]) + cur[12];
-            const float hm = rho * (sg * (f0 - cur[3]) - cur[17]) + cur[18];
+            const float hq = hval(sg * (cur[2] - f0), cur, 8, 12);
+            const float hm = hval(sg * (f0 - cur[3]), cur, 17, 18);
             d += hm - hq;
         }
         {  // t (scaled by lambda1 in both gradient and divergence)
-            const float hq = rho * (sgt * (cur[6] - f0) - cur[9]) + cur[13];
+            const float hq = hval(sgt * (cur[6] - f0), cur, 9, 13);
             d += t.lambda1 * (hmt - hq);
             hmt = hq;
         }
         {  // z
-            const float hq = rho * (sg * (cur[4] - f0) - cur[10]) + cur[14];
-            const float hm = rho * (sg * (f0 - cur[5]) - cur[19]) + cur[20];
+            const float hq = hval(sg * (cur[4] - f0), cur, 10, 14);
+            const float hm = hval(sg * (f0 - cur[5]), cur, 19, 20);
             d += hm - hq;
         }
         uout[v0 + (long long)tt * nn] = f0 + tau * t.sd * d;
@@ -153,11 +189,17 @@ __global__ void __launch_bounds__(256, 3)
 }
 
 void launch_graddiv(const float *u_in, const float *u_old, float *u_out, const float *psi,
-                    const float *mu, const float *rho, int c0, int nchunks_total, const TvGeo &t,
-                    cudaStream_t s) {
+                    const float *mu, float *w, int mode, const float *rho, int c0, int nchunks_total,
+                    const TvGeo &t, cudaStream_t s) {
     dim3 bs(256, 1), gs((t.n + 255) / 256, t.nchunks * t.nzp, t.n);
     if (gs.y > 65535u || gs.z > 65535u) throw Error(1, "graddiv: grid too large");
-    k_graddiv<<<gs, bs, 0, s>>>(u_in, u_old, u_out, psi, mu, rho, t, c0, nchunks_total, -0.5f);
+    if (mode != 0 && !w) throw Error(1, "graddiv: no w buffer");
+    if (mode == 1)
+        k_graddiv<1><<<gs, bs, 0, s>>>(u_in, u_old, u_out, psi, mu, w, rho, t, c0, nchunks_total, -0.5f);
+    else if (mode == 2)
+        k_graddiv<2><<<gs, bs, 0, s>>>(u_in, u_old, u_out, psi, mu, w, rho, t, c0, nchunks_total, -0.5f);
+    else
+        k_graddiv<0><<<gs, bs, 0, s>>>(u_in, u_old, u_out, psi, mu, w, rho, t, c0, nchunks_total, -0.5f);
     LAUNCH_CHECK("k_graddiv");
 }
 
