@@ -128,7 +128,8 @@ int rectv_set_graphs(rectv_handle *h, int enable);
  *   divergence step, 3 shrink + dual update + residual sums, 4 forward
  *   padded-grid 2D FFT (row and column kernels), 5 inverse padded-grid 2D FFT
  *   (column and row kernels; 4 and 5 exist when 2n is a power of two in
- *   [256, 2048]).
+ *   [256, 2048]), 6 fused gradient-divergence step of the first inner
+ *   iteration (2 is then the step of the later inner iterations).
  * ------------------------------------------------------------------------- */
 
 /* Enqueue `reps` launches of one kernel over one batch of slices on the

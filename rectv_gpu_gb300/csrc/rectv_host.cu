@@ -856,8 +856,12 @@ struct Handle {
                          (gd.tc_scatter ? (double)zb * m * P * (P / 2 + 1) * 8.0 : (double)zb * m * P * P * 8.0);
                 *flops = npts * (81.0 * 2.0 * m * 2.0 + 8.0 * m + 18.0 * 4.0);
                 break;
-            case 2:  // graddiv: u in, u out, psi and mu in
-                *bytes = (double)zb * slab * 8.0 + 2.0 * 4.0 * dpb * gp * 4.0;
+            case 2:  // graddiv after the first inner step: u in, u out, w in (psi and mu when titer = 1)
+                *bytes = (double)zb * slab * 8.0 + (titer > 1 ? 1.0 : 2.0) * 4.0 * dpb * gp * 4.0;
+                *flops = (double)zb * slab * 60.0;
+                break;
+            case 6:  // graddiv of the first inner step: u in, u out, psi and mu in, w out
+                *bytes = (double)zb * slab * 8.0 + (titer > 1 ? 3.0 : 2.0) * 4.0 * dpb * gp * 4.0;
                 *flops = (double)zb * slab * 60.0;
                 break;
             case 3:  // shrink: u_cur, u_old in, mu in, psi and mu out
@@ -882,8 +886,9 @@ struct Handle {
     void launch_kernel(int which, int reps) {
         check_live();
         if (!session) throw Error(RECTV_ERR_STATE, "rectv_launch_kernel: needs a set-up session");
-        if (which < 0 || which > 5) throw Error(RECTV_ERR_ARG, "rectv_launch_kernel: unknown kernel id");
-        if (which >= 4 && !pad_fft) throw Error(RECTV_ERR_ARG, "rectv_launch_kernel: no padded-grid FFT at this size");
+        if (which < 0 || which > 6) throw Error(RECTV_ERR_ARG, "rectv_launch_kernel: unknown kernel id");
+        if ((which == 4 || which == 5) && !pad_fft)
+            throw Error(RECTV_ERR_ARG, "rectv_launch_kernel: no padded-grid FFT at this size");
         for (int r = 0; r < reps; ++r) {
             switch (which) {
                 case 0: launch_gather_fwd(spec, rows, zb, gd, ug, &spec_tmap, stream); break;
@@ -897,6 +902,10 @@ struct Handle {
                     break;
                 case 4:  // padded-grid forward FFT of the batch (rows + columns)
                     launch_pad_fft_fwd(U[cur], spec, zb * m, gd.deapod, fft_tw, fft_fwd_map, gd.err, ug, stream);
+                    break;
+                case 6:  // the first inner step (psi, mu in; stores w = mu - rho psi, unchanged values)
+                    launch_graddiv(U[cur], U[cur], U[(cur + 1) % 3], psi, mu, wdual, titer > 1 ? 1 : 0, rho_d, 0,
+                                   nchunks, tv, stream);
                     break;
                 case 5:  // padded-grid inverse FFT (columns + rows), added into the scratch iterate
                     launch_pad_fft_inv_accum(spec, U[(cur + 1) % 3], zb, 0.f, gd.deapod, fft_tw, fft_inv_map, gd.err,
