@@ -459,8 +459,93 @@ template <int N>
 size_t rows_smem() {
     return sizeof(float2) * (size_t)FftLayout<N, false, kRowThreads / (N / 16)>::S * (kRowThreads / (N / 16));
 }
+
+// ---------------------------------------------------------------------------
+// Residual rows of the inner step, fused: for two gathered rows a, b (rows of
+// n complex values, already multiplied by (-1)^(k+1) shift(k) (pi/mu)/n):
+//   x = Re IFFT_n(row)                                  (radonusfft.cu:98-102)
+//   r(s) = x(s) (-1)^(s+1) / sqrt(n ntheta) - g(s)      (residual, admm.cu:92)
+//   w(s) = (-1)^(s+1) r(s)                              (fftshift of adjR, radonusfft.cu:115)
+//   R = FFT_n(w), k = 0 .. n/2                          (the adjoint's row transform)
+// Re IFFT(a) + i Re IFFT(b) is the inverse FFT of Ha + i Hb (H = Hermitian
+// part), and FFT(wa + i wb) splits into the two half spectra, so a row pair
+// costs one inverse and one forward n-point FFT; the residual never goes to
+// memory.  Rows are the flattened (slice, angle) index; N = n.
+// ---------------------------------------------------------------------------
+template <int N>
+__global__ void __launch_bounds__(kRowThreads, 2)
+    k_resid_rows(const float2 *__restrict__ rows, const float *__restrict__ gdata, float2 *__restrict__ out,
+                 const float2 *__restrict__ tw, long long nrows, float scale) {
+    constexpr int N1 = N / 16, RP = kRowThreads / N1;
+    using L = FftLayout<N, false, RP>;
+    extern __shared__ float2 fft_sh[];
+    const int t = threadIdx.x % N1, c = threadIdx.x / N1;
+    const long long ra = 2 * ((long long)blockIdx.x * RP + c), rb = ra + 1;
+    const bool oka = ra < nrows, okb = rb < nrows;
+    const float2 *ga = rows + (oka ? ra : 0) * N, *gb = rows + (okb ? rb : 0) * N;
+    float2 v[16];
+#pragma unroll
+    for (int r = 0; r < 16; ++r) {  // Ha + i Hb at k = t + N1 r
+        const int k = t + N1 * r, km = (N - k) & (N - 1);
+        float2 a = make_float2(0.f, 0.f), b = make_float2(0.f, 0.f);
+        if (oka) {
+            const float2 p = ga[k], q = ga[km];
+            a = make_float2(0.5f * (p.x + q.x), 0.5f * (p.y - q.y));
+        }
+        if (okb) {
+            const float2 p = gb[k], q = gb[km];
+            b = make_float2(0.5f * (p.x + q.x), 0.5f * (p.y - q.y));
+        }
+        v[r] = make_float2(a.x - b.y, a.y + b.x);
+    }
+    fft_core<N, 1, L>(v, fft_sh, c, t, tw);
+    __syncthreads();
+#pragma unroll
+    for (int q = 0; q < 16 / L::R3; ++q)
+#pragma unroll
+        for (int j1 = 0; j1 < L::R3; ++j1) fft_sh[c * L::S + t + N1 * q + 256 * j1] = v[q * L::R3 + j1];
+    __syncthreads();
+    const float *da = gdata + (oka ? ra : 0) * N, *db = gdata + (okb ? rb : 0) * N;
+#pragma unroll
+    for (int r = 0; r < 16; ++r) {
+        const int sidx = t + N1 * r;
+        const float2 x = fft_sh[c * L::S + sidx];
+        const float sg = (sidx & 1) ? 1.f : -1.f;
+        // as the separate passes: v = x (+-scale), r = v - g, w = (+-) r
+        const float wa = oka ? sg * (sg * (x.x * scale) - da[sidx]) : 0.f;
+        const float wb = okb ? sg * (sg * (x.y * scale) - db[sidx]) : 0.f;
+        v[r] = make_float2(wa, wb);
+    }
+    __syncthreads();
+    fft_core<N, -1, L>(v, fft_sh, c, t, tw);
+    __syncthreads();
+#pragma unroll
+    for (int q = 0; q < 16 / L::R3; ++q)
+#pragma unroll
+        for (int j1 = 0; j1 < L::R3; ++j1) fft_sh[c * L::S + t + N1 * q + 256 * j1] = v[q * L::R3 + j1];
+    __syncthreads();
+    constexpr int HN = N / 2 + 1;
+    for (int k = t; k < HN; k += N1) {
+        const float2 zk = fft_sh[c * L::S + k], zm = fft_sh[c * L::S + ((N - k) & (N - 1))];
+        if (oka) out[ra * HN + k] = make_float2(0.5f * (zk.x + zm.x), 0.5f * (zk.y - zm.y));
+        if (okb) out[rb * HN + k] = make_float2(0.5f * (zk.y + zm.y), 0.5f * (zm.x - zk.x));
+    }
+}
+
+template <int N>
+void resid_n(const float2 *rows, const float *gdata, float2 *out, const float2 *tw, long long nrows, float scale,
+             cudaStream_t s) {
+    constexpr int N1 = N / 16, RP = kRowThreads / N1;
+    const long long npairs = (nrows + 1) / 2;
+    const long long nblk = (npairs + RP - 1) / RP;
+    if (nblk > 2147483647LL) throw Error(1, "residual rows: too many rows");
+    k_resid_rows<N><<<(unsigned)nblk, kRowThreads, rows_smem<N>(), s>>>(rows, gdata, out, tw, nrows, scale);
+    LAUNCH_CHECK("k_resid_rows");
+}
+
 template <int N>
 void set_attrs_n() {
+    CUDA_CHECK(cudaFuncSetAttribute(k_resid_rows<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)rows_smem<N>()));
     CUDA_CHECK(cudaFuncSetAttribute(k_fft_rows_fwd<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)rows_smem<N>()));
     CUDA_CHECK(cudaFuncSetAttribute(k_fft_rows_inv<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)rows_smem<N>()));
     CUDA_CHECK(cudaFuncSetAttribute(k_fft_cols<N, kColC, -1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -584,6 +669,21 @@ void launch_pad_fft_fwd(const float *u, float2 *spec, int nimg, const float *dea
         case 1024: fwd_n<1024>(u, spec, nimg, deapod, tw, map, err, g, s); break;
         case 2048: fwd_n<2048>(u, spec, nimg, deapod, tw, map, err, g, s); break;
         default: throw Error(1, "pad FFT: unsupported grid size");
+    }
+}
+
+bool resid_rows_supported(int n) { return n >= 256 && n <= 1024 && (n & (n - 1)) == 0; }
+
+// tw_n: the twiddle table of the n-point transforms, pad_fft_twiddles(n)
+void launch_resid_rows(const float2 *rows, const float *gdata, float2 *out, const float2 *tw_n, int zb,
+                       const UsGeo &g, cudaStream_t s) {
+    const long long nrows = (long long)zb * g.ntheta;
+    const float scale = (float)(1.0 / std::sqrt((double)g.n * (double)g.ntheta));
+    switch (g.n) {
+        case 256: resid_n<256>(rows, gdata, out, tw_n, nrows, scale, s); break;
+        case 512: resid_n<512>(rows, gdata, out, tw_n, nrows, scale, s); break;
+        case 1024: resid_n<1024>(rows, gdata, out, tw_n, nrows, scale, s); break;
+        default: throw Error(1, "residual rows: unsupported detector width");
     }
 }
 

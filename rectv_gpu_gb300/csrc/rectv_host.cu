@@ -124,6 +124,10 @@ struct Handle {
     // of cuFFT + deapodise/pad + crop passes; RECTV_CUFFT=1 selects cuFFT
     bool pad_fft = false;
     float2 *fft_tw = nullptr;  // twiddle tables (pad_fft_twiddles)
+    // fused residual rows (inverse row FFT, residual, R2C in one kernel)
+    bool fused_rows = false;
+    float2 *fft_tw_n = nullptr;  // twiddles of the n-point row transforms
+    float2 *rows_adj = nullptr;  // the adjoint's row spectra [zb][ntheta][n/2+1]
     CUtensorMap fft_fwd_map, fft_inv_map;  // TMA tiles of the column passes
 
     // session
@@ -247,6 +251,15 @@ struct Handle {
                 CUDA_CHECK(cudaStreamSynchronize(stream));
                 ug.hpitch = P / 2 + 2;  // 16-byte half-plane rows for the TMA tiles
                 make_pad_fft_maps(&fft_fwd_map, &fft_inv_map, spec, zb * m, ug);
+                fused_rows = resid_rows_supported(n);
+                if (fused_rows) {
+                    const std::vector<float2> wn = pad_fft_twiddles(n);
+                    fft_tw_n = dalloc<float2>(wn.size(), owned);
+                    CUDA_CHECK(cudaMemcpyAsync(fft_tw_n, wn.data(), sizeof(float2) * wn.size(),
+                                               cudaMemcpyHostToDevice, stream));
+                    rows_adj = dalloc<float2>((size_t)zb * ntheta * (size_t)(n / 2 + 1), owned);
+                    CUDA_CHECK(cudaStreamSynchronize(stream));
+                }
             }
         }
         make_fft_plans();
@@ -527,6 +540,14 @@ struct Handle {
     // ---- operators on one batch of zb slices ----
     // out = tau R_apr u  (residual: out = R_apr u - gb)
     void forward(const float *u, const float *gb, float *out, float tau, int residual) {
+        forward_rows(u);
+        CUFFT_CHECK(cufftExecC2C(p_rows_c2c, reinterpret_cast<cufftComplex *>(rows),
+                                 reinterpret_cast<cufftComplex *>(rows), CUFFT_INVERSE));
+        launch_finish_fwd(rows, gb, out, zb, tau, residual, ug, stream);
+    }
+
+    // the gathered row spectra of R_apr u (before the inverse row FFT) in rows
+    void forward_rows(const float *u) {
         const int nimg = zb * m;
         if (pad_fft) {
             launch_pad_fft_fwd(u, spec, nimg, gd.deapod, fft_tw, fft_fwd_map, gd.err, ug, stream);
@@ -539,9 +560,6 @@ struct Handle {
         }
         launch_spec_halo(spec, nimg, ug, stream);
         launch_gather_fwd(spec, rows, zb, gd, ug, &spec_tmap, stream);
-        CUFFT_CHECK(cufftExecC2C(p_rows_c2c, reinterpret_cast<cufftComplex *>(rows),
-                                 reinterpret_cast<cufftComplex *>(rows), CUFFT_INVERSE));
-        launch_finish_fwd(rows, gb, out, zb, tau, residual, ug, stream);
     }
 
     // u += tau R_apr^T h
@@ -550,13 +568,18 @@ struct Handle {
         CUFFT_CHECK(cufftExecR2C(p_rows_r2c, reinterpret_cast<cufftReal *>(rows),
                                  reinterpret_cast<cufftComplex *>(rows)));
         if (row_filter) launch_filter_rows(rows, row_filter, (long long)zb * ntheta, n, stream);
+        adjoint_rows(rows, u, tau);
+    }
+
+    // u += tau R_apr^T of the row spectra rowsc [zb][ntheta][n/2+1]
+    void adjoint_rows(const float2 *rowsc, float *u, float tau) {
         const int nimg = zb * m;
         if (gd.tc_scatter) {
             // Re IFFT2 of the scattered grids as a C2R of their Hermitian part,
             // which the tensor-core scatter adds into zeroed half planes
             const long long img_half = (long long)ug.P * ug.hpitch;
             CUDA_CHECK(cudaMemsetAsync(spec, 0, sizeof(float2) * (size_t)nimg * img_half, stream));
-            launch_scatter_adj(rows, spec, zb, gd, ug, stream);
+            launch_scatter_adj(rowsc, spec, zb, gd, ug, stream);
             if (pad_fft) {
                 launch_pad_fft_inv_accum(spec, u, zb, tau, gd.deapod, fft_tw, fft_inv_map, gd.err, ug, stream);
                 return;
@@ -569,7 +592,7 @@ struct Handle {
             return;
         }
         launch_zero_split(spec, zb, gd, ug, stream);
-        launch_scatter_adj(rows, spec, zb, gd, ug, stream);
+        launch_scatter_adj(rowsc, spec, zb, gd, ug, stream);
         for (int i = 0; i < nimg; i += img_per_fft) {
             cufftComplex *p = reinterpret_cast<cufftComplex *>(spec + (size_t)i * ug.img_adj);
             CUFFT_CHECK(cufftExecC2C(p_c2c2d, p, p, CUFFT_INVERSE));
@@ -587,11 +610,19 @@ struct Handle {
             for (int bb = 0; bb < nbatch; ++bb) {
                 const long long z0 = (long long)bb * zb;
                 const int c0 = bb * dpb;
-                forward(U[src] + z0 * slab, gdata + z0 * ntheta * n, h1, 1.0f, 1);
+                if (fused_rows) {  // residual rows straight into the adjoint's row spectra
+                    forward_rows(U[src] + z0 * slab);
+                    launch_resid_rows(rows, gdata + z0 * ntheta * n, rows_adj, fft_tw_n, zb, ug, stream);
+                } else {
+                    forward(U[src] + z0 * slab, gdata + z0 * ntheta * n, h1, 1.0f, 1);
+                }
                 // first inner step: psi, mu in, w = mu - rho psi out; later steps: w in
                 const int gmode = titer > 1 ? (k == 0 ? 1 : 2) : 0;
                 launch_graddiv(U[src], U[old], U[dst], psi, mu, wdual, gmode, rho_d, c0, nchunks, tv, stream);
-                adjoint(h1, U[dst] + z0 * slab, -0.5f);
+                if (fused_rows)
+                    adjoint_rows(rows_adj, U[dst] + z0 * slab, -0.5f);
+                else
+                    adjoint(h1, U[dst] + z0 * slab, -0.5f);
             }
             src = dst;
         }
@@ -836,8 +867,11 @@ struct Handle {
         // the padded-grid FFTs replace deapodise/pad (crop) and the 2D cuFFT
         // executions by a row and a column kernel each
         const bool own2d = pad_fft && gd.tc_scatter;
-        const int fwd_k = (pad_fft ? 4 : 3) + jgroups(), fwd_f = (pad_fft ? 0 : f2) + 1;
-        const int adj_k = (own2d ? 3 : 2) + (gd.n_split_tiles > 0 ? 1 : 0) + jgroups(), adj_f = 1 + (own2d ? 0 : f2);
+        // with the fused residual rows the row FFTs, the residual and the
+        // adjoint's row preparation are one kernel
+        const int fwd_k = (pad_fft ? 4 : 3) + jgroups(), fwd_f = (pad_fft ? 0 : f2) + (fused_rows ? 0 : 1);
+        const int adj_k = (own2d ? 3 : 2) + (gd.n_split_tiles > 0 ? 1 : 0) + jgroups() - (fused_rows ? 1 : 0);
+        const int adj_f = (fused_rows ? 0 : 1) + (own2d ? 0 : f2);
         *kern = titer * nbatch * (fwd_k + 1 + adj_k) + nbatch + 1;
         *ffts = titer * nbatch * (fwd_f + adj_f);
     }
@@ -892,7 +926,7 @@ struct Handle {
         for (int r = 0; r < reps; ++r) {
             switch (which) {
                 case 0: launch_gather_fwd(spec, rows, zb, gd, ug, &spec_tmap, stream); break;
-                case 1: launch_scatter_adj(rows, spec, zb, gd, ug, stream); break;
+                case 1: launch_scatter_adj(fused_rows ? rows_adj : rows, spec, zb, gd, ug, stream); break;
                 case 2:  // the inner steps after the first (w = mu - rho psi as stored by the last iteration)
                     launch_graddiv(U[cur], U[cur], U[(cur + 1) % 3], psi, mu, wdual, titer > 1 ? 2 : 0, rho_d, 0,
                                    nchunks, tv, stream);

@@ -176,6 +176,12 @@ void launch_pad_fft_fwd(const float *u, float2 *spec, int nimg, const float *dea
                         const CUtensorMap &map, int *err, const UsGeo &g, cudaStream_t s);
 void launch_pad_fft_inv_accum(float2 *spec, float *u, int zb, float tau, const float *deapod, const float2 *tw,
                               const CUtensorMap &map, int *err, const UsGeo &g, cudaStream_t s);
+// fused residual rows of the inner step (fft_kernels.cu), n a power of two in
+// [256, 1024]: gathered rows [z][theta][n] and data g -> the adjoint's row
+// spectra [z][theta][n/2+1] (inverse row FFT, residual, fftshift, R2C)
+bool resid_rows_supported(int n);
+void launch_resid_rows(const float2 *rows, const float *gdata, float2 *out, const float2 *tw_n, int zb,
+                       const UsGeo &g, cudaStream_t s);
 size_t gather_tc_smem();
 int gather_tc_table_capacity();
 size_t gather_fwd_smem(const UsGeo &g);
