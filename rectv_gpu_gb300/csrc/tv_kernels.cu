@@ -71,7 +71,7 @@ __device__ __forceinline__ void block_reduce3(double a, double b, double c, doub
 // than second HBM reads).
 // ---------------------------------------------------------------------------
 template <int MODE>
-__global__ void __launch_bounds__(256, 3)
+__global__ void __launch_bounds__(256, MODE == 2 ? 4 : 3)  // MODE 2 loads less: 32 warps per SM
     k_graddiv(const float *__restrict__ uin, const float *__restrict__ uold, float *__restrict__ uout,
               const float *__restrict__ psi, const float *__restrict__ mu, float *__restrict__ w,
               const float *__restrict__ rhop, TvGeo t, int c0, int nch_total, float tau) {
