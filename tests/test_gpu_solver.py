@@ -2,7 +2,7 @@
 of rectv::check_adjoints against the FP64 oracle.
 
 Tolerance: reconstructions within 1e-4 relative L2 of the FP64 oracle on the
-same seeded inputs (the spec accuracy bar).
+same seeded inputs.
 """
 
 import numpy as np
