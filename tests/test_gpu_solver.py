@@ -116,14 +116,15 @@ def test_config1_recon_matches_golden(Solver):
     np.testing.assert_allclose(h["rho"], gold["rho"])
 
 
-def test_recon_padded_fft_and_fused_rows_match_cufft_path(Solver, monkeypatch):
-    """At n = 256 (2n a power of two) the reconstruction runs the hand-written
-    padded-grid FFTs and the fused residual-row kernel (inverse row FFT,
-    residual and the adjoint's row transform in one pass); RECTV_CUFFT=1 runs
-    the same iterations through cuFFT and the separate passes.  Both must agree
-    to FP32 rounding accumulated over the iterations, and give the same rho
-    sequence."""
-    n, ntheta, m, nz, nzp, niter, titer = 256, 360, 8, 2, 2, 2, 3
+@pytest.mark.parametrize("case", [(256, 360, 8, 2, 2, 2, 3), (1024, 720, 16, 2, 1, 2, 2)])
+def test_recon_padded_fft_and_fused_rows_match_cufft_path(Solver, monkeypatch, case):
+    """With 2n a power of two (n = 256, and n = 1024 as in the benchmark) the
+    reconstruction runs the hand-written padded-grid FFTs and the fused
+    residual-row kernel (inverse row FFT, residual and the adjoint's row
+    transform in one pass); RECTV_CUFFT=1 runs the same iterations through
+    cuFFT and the separate passes.  Both must agree to FP32 rounding
+    accumulated over the iterations, and give the same rho sequence."""
+    n, ntheta, m, nz, nzp, niter, titer = case
     lam0, lam1 = 1e-3, 4.0
     theta = scan_angles(ntheta, 4)
     phi = orc.takephi(ntheta, m)
