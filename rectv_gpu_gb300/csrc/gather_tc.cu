@@ -18,7 +18,7 @@
 // where hi is the TF32 part (the tensor core truncates FP32 input to TF32)
 // and lo = x - trunc(x), itself truncated to TF32 (relative error < 2^-20).
 //
-// One block (512 threads, one per SM) per (work item, 32 slices):
+// One block (512 threads, one per SM) per (work item, 64 slices):
 //  * once: the sample table (stencil origin, separable Gaussian weights with
 //    the fftshift signs, row factor) and the item's rays; the B operands
 //    (K' rows) when the item has at most two chunks of rays;
@@ -57,7 +57,7 @@ constexpr int kK = 32;                       // 16 time samples x (re, im)
 constexpr int kTab = 256;                    // samples per work item
 constexpr int kThr = 512;
 constexpr int kWarps = kThr / 32;
-constexpr int kZPer = 32;                    // slices per block
+constexpr int kZPer = 64;                    // slices per block
 constexpr uint32_t kTmemCols = 512;
 constexpr uint32_t kColAhi = 0;              // TMEM columns: A hi [mt*32, +32)
 constexpr uint32_t kColAlo = kMT * kK;       //               A lo
