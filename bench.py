@@ -416,7 +416,7 @@ def run_ours(args, rank, world, local_rank):
         "data": "synthetic: 10 moving ellipsoids, forward-projected with this library + 1% Gaussian noise",
         "config": {"workload": workload_name(w), "lambda0": w["lambda0"], "lambda1": lam1, "center": center,
                    "chunks": nz // nzp, "batch_slices": zbs[0].value,
-                   "l2": "inputs larger than L2 (iterate 4.3 GB, dual variables 2x19 GB)",
+                   "l2": "inputs larger than L2 (iterate 4.3 GB, dual variables 3x19 GB)",
                    "parallelism": "replicas" if world > 1 else "single"},
         "voxel_updates_per_s": value * voxels,
         "e2e": {"value": whole_job_rate(args.steps, world, e2e_s * 1e3), "unit": "iter/s", "h2d_bytes_per_step": h2d / args.steps,
