@@ -84,7 +84,8 @@ struct ScTcSmem {
     AdjRec rec[2][kTab];          // geometry records of this table and the next (bulk copies)
     uint32_t info[2][kInfoMax];   // their ray segmentation (bulk copies)
     float4 t[kT][kTab];           // T_p(cy) = E(p) wy_p(cy) of both slices of the pair (x, y | z, w)
-    float2 rnext[kZ][kTab];       // row spectrum values of the next table's samples (cp.async)
+    float4 rnext[kZ][kTab];       // row spectrum values of the next table's samples, both slices (cp.async;
+                                  // each half copies its own, so a thread reads only its own copies)
     float bhi[kN * kK];           // B = conj K' of the batch's rays, FP32: rows 0..31 of the MMA's B
     float blo[kN * kK];           // B - trunc(B): rows 32..63 (contiguous with bhi)
     unsigned long long bar;      // MMA batch done (both slices)
@@ -307,7 +308,7 @@ __global__ void __launch_bounds__(kThr, 1)
         }
     };
     if (tid == 0) fetch(0);
-    bool have_next = false;  // rnext holds the current table's row spectrum values
+    bool have_next = false;  // rnext holds the current table's row spectrum values (both slices)
 
     // persistent: units (tile item, slice pair) round-robin, pairs fastest, so
     // the blocks in flight share their items' records in L2; all units hold
@@ -318,7 +319,6 @@ __global__ void __launch_bounds__(kThr, 1)
         const bool zok = z < zb;  // the last pair of an odd batch has one slice
         const int4 it = __ldg(items + u / npairs);
         const int tyi = it.x / g.NT, txi = it.x - tyi * g.NT;
-        const float2 *rz = rowsc + (long long)min(z, zb - 1) * g.ntheta * hn;
         int nbu = 0;    // MMA batches of this unit
         float acc[32];  // F of this cell: 16 time samples x (re, im)
 #pragma unroll
@@ -340,23 +340,44 @@ __global__ void __launch_bounds__(kThr, 1)
             const uint32_t *inf = sm.info[buf];
             const int nseg = min((int)inf[0], cnt);  // (clamps keep every index inside the table)
             const uint16_t *segf = reinterpret_cast<const uint16_t *>(inf + 4 + 8 * nseg);  // ray starts
-            // ---- E = (-1)^(k+1) shiftadj(k) FFT(row)(k) (pi/mu)/n and T_p(cy) = E(p) wy_p(cy),
-            // stored [row][entry] so that this thread writes its own entry's column ----
-            if (have_next) asm volatile("cp.async.wait_all;\n" ::: "memory");  // this thread's own entry
+            // ---- E = (-1)^(k+1) shiftadj(k) FFT(row)(k) (pi/mu)/n of both slices and
+            // T_p(cy) = E(p) wy_p(cy), stored [row][entry] as float4 (slice 0 | slice 1):
+            // thread (h, e) writes rows 8h .. 8h+7 of entry e ----
+            if (have_next) asm volatile("cp.async.wait_all;\n" ::: "memory");  // this thread's own copies
             if (ct < cnt) {
                 const int th = (unsigned)rec[ct].thm >> 16, k = rec[ct].k;
-                float2 R = make_float2(0.f, 0.f);
-                if (zok) R = have_next ? sm.rnext[h][ct] : __ldg(rz + (long long)th * hn + (k <= g.n / 2 ? k : g.n - k));
-                if (k > g.n / 2) R.y = -R.y;
-                const float2 E = cmul(R, rec[ct].sf);
-                const float4 *wy4 = reinterpret_cast<const float4 *>(rec[ct].wy);
+                float4 R = make_float4(0.f, 0.f, 0.f, 0.f);
+                if (have_next) {
+                    R = sm.rnext[h][ct];
+                } else {
+                    const long long o = (long long)th * hn + (k <= g.n / 2 ? k : g.n - k);
+                    const int z0 = 2 * (u % npairs);
+                    if (z0 < zb) {
+                        const float2 r0 = __ldg(rowsc + (long long)z0 * g.ntheta * hn + o);
+                        R.x = r0.x;
+                        R.y = r0.y;
+                    }
+                    if (z0 + 1 < zb) {
+                        const float2 r1 = __ldg(rowsc + (long long)(z0 + 1) * g.ntheta * hn + o);
+                        R.z = r1.x;
+                        R.w = r1.y;
+                    }
+                }
+                if (k > g.n / 2) {
+                    R.y = -R.y;
+                    R.w = -R.w;
+                }
+                const float2 sf = rec[ct].sf;
+                const float2 E0 = cmul(make_float2(R.x, R.y), sf), E1 = cmul(make_float2(R.z, R.w), sf);
+                const float4 *wy4 = reinterpret_cast<const float4 *>(rec[ct].wy) + 2 * h;  // rows 8h ..
 #pragma unroll
-                for (int q4 = 0; q4 < kT / 4; ++q4) {
+                for (int q4 = 0; q4 < 2; ++q4) {
                     const float4 w = wy4[q4];
-                    reinterpret_cast<float2 *>(&sm.t[4 * q4 + 0][ct])[h] = make_float2(E.x * w.x, E.y * w.x);
-                    reinterpret_cast<float2 *>(&sm.t[4 * q4 + 1][ct])[h] = make_float2(E.x * w.y, E.y * w.y);
-                    reinterpret_cast<float2 *>(&sm.t[4 * q4 + 2][ct])[h] = make_float2(E.x * w.z, E.y * w.z);
-                    reinterpret_cast<float2 *>(&sm.t[4 * q4 + 3][ct])[h] = make_float2(E.x * w.w, E.y * w.w);
+                    const int r0 = 8 * h + 4 * q4;
+                    sm.t[r0 + 0][ct] = make_float4(E0.x * w.x, E0.y * w.x, E1.x * w.x, E1.y * w.x);
+                    sm.t[r0 + 1][ct] = make_float4(E0.x * w.y, E0.y * w.y, E1.x * w.y, E1.y * w.y);
+                    sm.t[r0 + 2][ct] = make_float4(E0.x * w.z, E0.y * w.z, E1.x * w.z, E1.y * w.z);
+                    sm.t[r0 + 3][ct] = make_float4(E0.x * w.w, E0.y * w.w, E1.x * w.w, E1.y * w.w);
                 }
             }
             __syncthreads();
@@ -412,16 +433,25 @@ __global__ void __launch_bounds__(kThr, 1)
                     have_next = nu < nunits;
                     if (have_next) {
                         const int ncnt = __ldg(tabs + nti).y;
-                        const int nz = 2 * (nu % npairs) + h;
+                        const int nz0 = 2 * (nu % npairs);  // both slices of the next unit's pair
                         ok = tc::mbar_wait(&sm.rbar[buf ^ 1], (uint32_t)((seq >> 1) & 1)) && ok;
-                        if (nz < zb && ct < ncnt) {
-                            const float2 *nrz = rowsc + (long long)nz * g.ntheta * hn;
+                        if (ct < ncnt) {
                             const AdjRec &nr = sm.rec[buf ^ 1][ct];
                             const int th = (unsigned)nr.thm >> 16, k = nr.k;
-                            const float2 *src = nrz + (long long)th * hn + (k <= g.n / 2 ? k : g.n - k);
-                            asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(tc::smem_addr(&sm.rnext[h][ct])),
-                                         "l"(src)
-                                         : "memory");
+                            const long long o = (long long)th * hn + (k <= g.n / 2 ? k : g.n - k);
+                            float2 *dst = reinterpret_cast<float2 *>(&sm.rnext[h][ct]);
+                            if (nz0 < zb)
+                                asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(tc::smem_addr(dst)),
+                                             "l"(rowsc + (long long)nz0 * g.ntheta * hn + o)
+                                             : "memory");
+                            else
+                                dst[0] = make_float2(0.f, 0.f);
+                            if (nz0 + 1 < zb)
+                                asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(tc::smem_addr(dst + 1)),
+                                             "l"(rowsc + (long long)(nz0 + 1) * g.ntheta * hn + o)
+                                             : "memory");
+                            else
+                                dst[1] = make_float2(0.f, 0.f);
                             asm volatile("cp.async.commit_group;\n" ::: "memory");
                         }
                     }
