@@ -20,6 +20,10 @@
 //                   as one complex inverse FFT (Re -> first row, Im -> second),
 //                   only the n centre outputs, deapodised and added into u
 //
+// The same transform core also runs the n-point row transforms between the
+// gather and the scatter (k_resid_rows: inverse row FFT, residual, fftshift
+// and the adjoint's row R2C in one pass, n a power of two in [256, 1024]).
+//
 // Every transform is P = 16 x 16 x R3 points (R3 = P/256) computed by P/16
 // threads holding 16 values each: a 16-point DFT in registers, twiddles,
 // exchange through shared memory, a 16-point DFT, twiddles, exchange, and
@@ -160,7 +164,8 @@ __device__ __forceinline__ float2 twiddle(const float2 *__restrict__ tw, int e, 
 //    at i*C + c; stage-2 output of pair p, m1 at p*Q + m1 (Q = R3+1 odd).
 //  regions (row kernels, thread = t + (P/16) c): element i of transform c at
 //    c*S + i; stage-2 output at p*R3 + ((m1 + p/(16/R3)) mod R3).
-// Both make every exchange free of bank conflicts.
+// Both make the exchanges free of bank conflicts for P >= 1024 (at P = 512
+// one exchange of the column kernels keeps a two-way conflict).
 template <int N, bool INTERLEAVED, int C>
 struct FftLayout {
     static constexpr int N1 = N / 16;
@@ -399,8 +404,8 @@ __global__ void __launch_bounds__(C *(N / 16), 1)
 
 // ---------------------------------------------------------------------------
 // Adjoint rows: rows Ya = n/2 + 2 pr and Ya + 1 of the column pass output
-// (row pitch hp complex),
-// Hermitian-extended to P points, one inverse FFT as A + i B; the centre
+// (row pitch hp complex), Hermitian-extended to P points, one inverse FFT as
+// A + i B; the centre
 // outputs X in [n/2, 3n/2) are modulated, deapodised, scaled by c and added
 // into rows 2 pr, 2 pr + 1 of u.
 // ---------------------------------------------------------------------------
