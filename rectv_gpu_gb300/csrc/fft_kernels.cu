@@ -405,9 +405,8 @@ __global__ void __launch_bounds__(C *(N / 16), 1)
 // ---------------------------------------------------------------------------
 // Adjoint rows: rows Ya = n/2 + 2 pr and Ya + 1 of the column pass output
 // (row pitch hp complex), Hermitian-extended to P points, one inverse FFT as
-// A + i B; the centre
-// outputs X in [n/2, 3n/2) are modulated, deapodised, scaled by c and added
-// into rows 2 pr, 2 pr + 1 of u.
+// A + i B; the centre outputs X in [n/2, 3n/2) are modulated, deapodised,
+// scaled by c and added into rows 2 pr, 2 pr + 1 of u.
 // ---------------------------------------------------------------------------
 template <int N>
 __global__ void __launch_bounds__(kRowThreads, 2)
