@@ -109,7 +109,9 @@ int rectv_get_result_device(rectv_handle *h, float *d_f);
 /* The CUDA stream (cudaStream_t) all work of this handle is queued on. */
 int rectv_get_stream(rectv_handle *h, void **stream);
 
-/* Waits for the handle's stream. */
+/* Waits for the handle's stream; returns RECTV_ERR_STATE if a kernel recorded
+ * an error on the device since the handle was created (a host/device plan
+ * disagreement, or a bounded TMA / tensor-core wait that gave up). */
 int rectv_synchronize(rectv_handle *h);
 
 /* Per-outer-iteration statistics of the last run/iterate calls, host arrays of

@@ -776,10 +776,19 @@ struct Handle {
         }
         for (auto &e : ev) cudaEventDestroy(e);
         iters_done += niter;
+        check_device_errors();
+    }
+
+    // Waits for the stream and raises if a kernel recorded an error on the
+    // device since the handle was created: a host/device plan disagreement
+    // or a bounded TMA / tensor-core wait that gave up.
+    void check_device_errors() {
         int errs = 0;
         CUDA_CHECK(cudaMemcpyAsync(&errs, gd.err, sizeof(int), cudaMemcpyDeviceToHost, stream));
         CUDA_CHECK(cudaStreamSynchronize(stream));
-        if (errs) throw Error(RECTV_ERR_STATE, "rectv: internal kernel error (plan/stencil mismatch or tensor-core wait timeout)");
+        if (errs)
+            throw Error(RECTV_ERR_STATE,
+                        "rectv: internal kernel error (plan/stencil mismatch or a TMA / tensor-core wait timed out)");
     }
 
     // ---- operator API helpers: any number of slices via zero-padded batches ----
@@ -1155,7 +1164,7 @@ int rectv_get_stream(rectv_handle *h, void **stream) {
 }
 
 int rectv_synchronize(rectv_handle *h) {
-    return guarded([&] { CUDA_CHECK(cudaStreamSynchronize(live(h)->stream)); });
+    return guarded([&] { live(h)->check_device_errors(); });
 }
 
 int rectv_get_history(rectv_handle *h, double *rdiff, double *rho, double *r, double *s, int *count) {
