@@ -368,11 +368,11 @@ def run_ours(args, rank, world, local_rank):
     achieved = bytes_.value / (ktimes[dom] * 1e-3) / 1e9
     limiter = {
         "k_scatter_tc": "block barriers and the per-cell ray sums on the CUDA cores (shared-memory loads), "
-                        "the tcgen05 time-sample GEMM (3xTF32) at ~14% of the tensor pipe; DRAM traffic 4.1x "
+                        "the tcgen05 time-sample GEMM (3xTF32) at ~14% of the tensor pipe; DRAM traffic 4.0x "
                         "the algorithmic bytes (float2 atomics read and write every Hermitian half-plane cell "
                         "twice) at 13% of the DRAM peak, so not DRAM-bound",
         "k_gather_tc": "shared-memory bandwidth of the per-sample 81-tap sums and of the TMEM -> shared "
-                       "read-out of G, block barriers; TMA-staged footprints, DRAM traffic 2.6x the spectra "
+                       "read-out of G, block barriers; TMA-staged footprints, DRAM traffic 3.0x the spectra "
                        "(overlapping footprints) at 8% of the DRAM peak",
         "k_graddiv": "HBM bandwidth", "k_shrink": "HBM bandwidth",
         KERNEL_NAMES[4]: "HBM bandwidth", KERNEL_NAMES[5]: "HBM bandwidth"}[KERNEL_NAMES[dom]]
