@@ -14,15 +14,22 @@
 // stencil), the ray, the detector index and a mask of the tile rows the
 // stencil covers.
 //
+// Tables.  A tile's entries are cut into tables of whole rays, at most one
+// MMA batch of rays (16) and 256 entries each (host plan); the ray
+// segmentation of a table (its rays, their first rows, and per ray and warp
+// the rows covering the warp's two tile rows) is geometry too, computed once
+// by k_adj_tabinfo.
+//
 // Persistent blocks of 512 threads, one per SM, take the (tile, slice pair)
 // units with samples round-robin; each block half (256 threads, thread =
 // cell) works on one slice of the pair, and the halves share what does not
-// depend on the slice: the records, the ray starts and sample ranges, K' (the
-// MMA's B) and the barriers.  The records of the next table of samples are
+// depend on the slice: the records, the segmentation, K' (the MMA's B) and
+// the barriers.  The records and segmentation of the next table are
 // bulk-copied into a second shared buffer (TMA engine, mbarrier) while the
 // current one is processed.  Per unit and table:
-//  * per sample: E(p) (the row spectrum value times (-1)^(k+1) shiftadj(k)
-//    (pi/mu)/n) and T_p(cy) = E(p) wy_p(cy) for the tile's 16 rows;
+//  * per entry: E(p) (the row spectrum value times (-1)^(k+1) shiftadj(k)
+//    (pi/mu)/n) of both slices and T_p(cy) = E(p) wy_p(cy) for the tile's 16
+//    rows, both slices in one float4;
 //  * per batch of 16 rays: every cell sums its value of each ray's grid
 //    V(c, theta) = sum_p T_p(cy) wx_p(cx) over the ray's samples (plan order,
 //    so sums are reproducible; a warp skips samples that miss its two rows);
@@ -31,10 +38,11 @@
 //    [32 x 32] real on the tensor cores with TF32 parts for FP32 accuracy
 //    (the tensor core truncates FP32 input to TF32; lo = x - trunc(x)):
 //    the MMA's B holds [Khi | Klo] as 64 columns, so Vhi B + Vlo B gives
-//    Vhi Khi + Vhi Klo + Vlo Khi (+ the negligible Vlo Klo) in 16 MMAs.  Each batch's product is added to the cell's
-//    FP32 sums in registers (the tensor core's own FP32 accumulation rounds
-//    differently and would drift over the many batches of central tiles),
-//    and the next batch's grids are formed while the MMAs run.
+//    Vhi Khi + Vhi Klo + Vlo Khi (+ the negligible Vlo Klo) in 16 MMAs.
+//    Each batch's product is added to the cell's FP32 sums in registers (the
+//    tensor core's own FP32 accumulation rounds differently and would drift
+//    over the many batches of central tiles), and the next table's E and T
+//    and ray sums are formed while the MMAs run.
 // The tile is added once per unit into the Hermitian half plane that the
 // C2R inverse transform takes (see the epilogue).
 #include <cuda.h>
