@@ -873,15 +873,26 @@ struct Handle {
     void launch_counts(int *kern, int *ffts) const {
         const int nimg = zb * m;
         const int f2 = (nimg + img_per_fft - 1) / img_per_fft;
+        const int ng = jgroups();
         // the padded-grid FFTs replace deapodise/pad (crop) and the 2D cuFFT
         // executions by a row and a column kernel each
         const bool own2d = pad_fft && gd.tc_scatter;
-        // with the fused residual rows the row FFTs, the residual and the
-        // adjoint's row preparation are one kernel
-        const int fwd_k = (pad_fft ? 4 : 3) + jgroups(), fwd_f = (pad_fft ? 0 : f2) + (fused_rows ? 0 : 1);
-        const int adj_k = (own2d ? 3 : 2) + (gd.n_split_tiles > 0 ? 1 : 0) + jgroups() - (fused_rows ? 1 : 0);
+        // forward: [rows + columns | deapodise/pad], halo, zeroing of the k = 0
+        // samples, per group of 16 time samples the tensor-core gather (9+ time
+        // samples) and the direct one (items with few samples per ray), then the
+        // fused residual rows or the forward epilogue
+        const int gather_k =
+            1 + ng * (((m > 8 && gd.n_fwd_tc_items > 0) ? 1 : 0) + (gd.n_fwd_items > 0 ? 1 : 0));
+        const int fwd_k = (pad_fft ? 2 : 1) + 1 + gather_k + 1;
+        const int fwd_f = (pad_fft ? 0 : f2) + (fused_rows ? 0 : 1);
+        // adjoint: [row preparation], the zeroing of split tiles (direct scatter),
+        // one scatter per group, then [columns + rows | crop]
+        const int adj_k = (fused_rows ? 0 : 1) + ((!gd.tc_scatter && gd.n_split_tiles > 0) ? 1 : 0) + ng +
+                          (own2d ? 2 : 1);
         const int adj_f = (fused_rows ? 0 : 1) + (own2d ? 0 : f2);
-        *kern = titer * nbatch * (fwd_k + 1 + adj_k) + nbatch + 1;
+        // per outer iteration: titer inner steps per batch (forward, graddiv,
+        // adjoint), one shrink per batch, the two-stage rho reduction
+        *kern = titer * nbatch * (fwd_k + 1 + adj_k) + nbatch + 2;
         *ffts = titer * nbatch * (fwd_f + adj_f);
     }
 
