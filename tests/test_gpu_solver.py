@@ -116,7 +116,11 @@ def test_config1_recon_matches_golden(Solver):
     np.testing.assert_allclose(h["rho"], gold["rho"])
 
 
-@pytest.mark.parametrize("case", [(256, 360, 8, 2, 2, 2, 3), (1024, 720, 16, 2, 1, 2, 2)])
+@pytest.mark.parametrize("case", [
+    (256, 360, 8, 2, 2, 2, 3),
+    (1024, 720, 16, 2, 1, 2, 2),   # the benchmark's grid, two chunks
+    (512, 361, 12, 1, 1, 2, 2),    # odd number of rows (a row pair with one row), one slice (a slice pair with one slice)
+])
 def test_recon_padded_fft_and_fused_rows_match_cufft_path(Solver, monkeypatch, case):
     """With 2n a power of two (n = 256, and n = 1024 as in the benchmark) the
     reconstruction runs the hand-written padded-grid FFTs and the fused
