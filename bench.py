@@ -242,6 +242,51 @@ def cpu_sample(w, angle_stride=30):
     return 1.0 / t_iter, t6 - t0 + (t4 - t3), sample, workers
 
 
+def fp64_accuracy(torch, w, g_h, theta, phi, iters, nsub=2):
+    """Relative L2 error of the GPU reconstruction against the FP64 oracle
+    after every outer iteration, on a subset of the workload: `nsub` middle
+    slices of the same data, solved as one chunk of the same geometry (N,
+    Ntheta, M, titer, lambdas).  The FP64 side is the PyTorch transcription of
+    the oracle in float64 on the GPU, run in lockstep; it follows its own rho
+    rule, and whether both sides took the same rho decisions is reported."""
+    from oracle import rectv_oracle_torch as ort
+    from rectv_gpu_gb300 import rectv
+    n, ntheta, m, nz, titer = w["n"], w["ntheta"], w["m"], w["nz"], w["titer"]
+    lam0, lam1 = w["lambda0"] * w["lambda1"], w["lambda1"]
+    z0 = nz // 2 - nsub // 2
+    g = np.ascontiguousarray(g_h[z0:z0 + nsub].numpy())
+    dev = torch.device("cuda", torch.cuda.current_device())
+    t0 = time.perf_counter()
+    obj = rectv(n, ntheta, m, nsub, nsub, 1)
+    obj.set_verbose(False)
+    dg = torch.from_numpy(g).to(dev)
+    dth = torch.from_numpy(theta).to(dev)
+    dph = torch.from_numpy(phi).to(dev)
+    out = torch.empty((nsub, m, n, n), dtype=torch.float32, device=dev)
+    torch.cuda.synchronize()
+    obj.setup_device(dg.data_ptr(), dth.data_ptr(), dph.data_ptr(), n / 2, lam0, lam1, titer)
+    errs = []
+
+    def step(it, f):
+        obj.iterate(1)
+        obj.result_device(out.data_ptr())
+        obj.synchronize()
+        errs.append(float(torch.linalg.vector_norm(out.to(torch.float64) - f) / torch.linalg.vector_norm(f)))
+
+    try:
+        _, h64 = ort.run(g, theta, phi, n / 2, lam0, lam1, iters, titer, nsub, device=dev, return_history=True,
+                         callback=step)
+        hist = obj.history()
+    finally:
+        obj.free()
+    return {"max": max(errs), "final": errs[-1], "iterations": iters, "per_iteration": errs,
+            "subset": "slices %d-%d of the workload's data as one chunk (Nz=Nzp=%d), same N, Ntheta, M, titer, "
+                      "lambdas; FP64 oracle (PyTorch transcription, float64 on the GPU) in lockstep"
+                      % (z0, z0 + nsub - 1, nsub),
+            "same_rho_decisions": list(hist["rho"]) == [x["rho"] for x in h64],
+            "seconds": time.perf_counter() - t0}
+
+
 def run_reference_arm(args, rank):
     """--impl reference: the reference's algorithm (FP64 oracle restatement; the
     reference has no CPU path and its CUDA build cannot travel) on host cores."""
@@ -402,6 +447,10 @@ def run_ours(args, rank, world, local_rank):
     d2h = f_h.numel() * 4
     finite = bool(np.isfinite(f_h[:, :, ::64, ::64].numpy()).all())
 
+    acc = None
+    if rank == 0 and world == 1 and args.acc_iters > 0:
+        acc = fp64_accuracy(torch, w, g_h, theta, phi, args.acc_iters)
+
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
         v, s, sample, workers = cpu_sample(w)
@@ -427,6 +476,7 @@ def run_ours(args, rank, world, local_rank):
         "gpu_launches": launches_per_iter * args.steps,
         "cufft_execs": ffts[0].value * args.steps,
         "rho_final": float(hist["rho"][-1]) if len(hist["rho"]) else None,
+        "rel_err_vs_fp64": acc,
         "result_finite": finite,
     }
     obj.free()
@@ -451,6 +501,8 @@ def main():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--small", action="store_true", help="N=256 workload (quick check)")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
+    ap.add_argument("--acc-iters", type=int, default=64,
+                    help="outer iterations of the FP64 accuracy check on a 2-slice subset (0: skip)")
     ap.add_argument("--nz", type=int, default=None, help="slices (default: the workload's); for small ncu cases")
     ap.add_argument("--nzp", type=int, default=None, help="slices per chunk (default: the workload's)")
     args = ap.parse_args()
