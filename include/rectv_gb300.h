@@ -148,6 +148,15 @@ int rectv_kernel_cost(rectv_handle *h, int which, double *bytes, double *flops);
  * executions; and the batch size in slices. */
 int rectv_get_launch_counts(rectv_handle *h, int *kernels, int *fft_execs, int *batch_slices);
 
+/* Self-test of the bounded waits of the tensor-core and TMA kernels: queues
+ * on the handle's stream one block that waits on an mbarrier nothing arrives
+ * on, first for limit_cycles SM cycles, then nwait - 1 more times with the
+ * short limit the kernels use after an expired wait, and records the expiry
+ * in the handle's device error counter.  Afterwards rectv_synchronize returns
+ * RECTV_ERR_STATE for this handle (the counter is never cleared), and the
+ * CUDA context stays usable. */
+int rectv_selftest_wait(rectv_handle *h, long long limit_cycles, int nwait);
+
 /* ---------------------------------------------------------------------------
  * Filtered backprojection and warm start (no counterpart run by the
  * reference: its ramp filter applyfilter and mask circ,
@@ -202,10 +211,13 @@ int rectv_preprocess(float *out, const void *data, const void *dark, const void 
  * Its only scratch (FP64 per-block partial sums and the rho value) is a fixed
  * static device array of 1.5 MiB that every GPU loading this library holds
  * until the process exits.  Limit: ceil((n+1)/32)*ceil((n+1)/8)*nchunks*
- * (nzp+1) <= 65536 thread blocks (e.g. n=1024, nzp=8, nchunks=1, any m);
- * larger problems are rejected with RECTV_ERR_ARG.  The first call on a
- * device looks up the array's device address, so make that first call before
- * any stream capture.  All calls share the array, which keeps the last call's
+ * (nzp+1) <= 65536 thread blocks (e.g. n=1024, nzp=8, nchunks=1, any m)
+ * and nchunks*(nzp+1) <= 65535; larger problems are rejected with
+ * RECTV_ERR_ARG.  `stream` must belong to the current device.  The first
+ * call on a device looks up the array's device address, so make that first
+ * call before any stream capture; the address is kept for the process's
+ * life, so after cudaDeviceReset of a device do not call this entry point on
+ * that device again.  All calls share the array, which keeps the last call's
  * contents; each call writes every entry it reads before reading it, so
  * nothing needs clearing.  Calls that can run at the same time on one device
  * (for example on different streams) race on the array. */

@@ -41,6 +41,7 @@ SIGNATURES = {
     "rectv_launch_kernel": (_I, [_P, _I, _I]),
     "rectv_kernel_cost": (_I, [_P, _I, _P, _P]),
     "rectv_get_launch_counts": (_I, [_P, _IP, _IP, _IP]),
+    "rectv_selftest_wait": (_I, [_P, ctypes.c_longlong, _I]),
     "rectv_shrink_noalloc": (_I, [_P, _P, _P, _P, _I, _I, _I, _I, _F, _F, _F, _P, _P]),
     "rectv_preprocess": (_I, [_P, _P, _P, _P, _I, _I, _I, _I, _I, _I]),
     "rectv_fbp": (_I, [_P, _P, _P, _P, _F]),

@@ -363,7 +363,7 @@ __global__ void __launch_bounds__(C *(N / 16), 1)
         // the other landing buffer was read in the previous iteration, before
         // at least one block barrier: it takes the next tile
         if (threadIdx.x == 0 && tile + (int)gridDim.x < ntiles) fetch(tile + gridDim.x, buf ^ 1);
-        ok = tc::mbar_wait(&bar[buf], (uint32_t)((it >> 1) & 1)) && ok;
+        ok = tc::mbar_wait(&bar[buf], (uint32_t)((it >> 1) & 1), ok) && ok;
         float2 v[16];
         const float2 *in = fft_sh + CP::EX + buf * CP::LAND;
 #pragma unroll

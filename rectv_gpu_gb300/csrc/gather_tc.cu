@@ -283,7 +283,7 @@ __global__ void __launch_bounds__(kThr, 1)
 
     // footprint box of slice z -> A operand in tensor memory (thread = cell)
     auto convert = [&](int z) {
-        ok = tc::mbar_wait(&sm.bar_tma, (uint32_t)((z - z0) & 1)) && ok;
+        ok = tc::mbar_wait(&sm.bar_tma, (uint32_t)((z - z0) & 1), ok) && ok;
         for (int mt = wid >> 2; mt < kMT; mt += kWarps / 4) {
             const int cell = mt * 128 + 32 * q + lane;
             float hi[32], lo[32];
@@ -322,14 +322,14 @@ __global__ void __launch_bounds__(kThr, 1)
     };
 
     if (nch == 0) {  // no samples: only the first box is in flight
-        ok = tc::mbar_wait(&sm.bar_tma, 0u) && ok;
+        ok = tc::mbar_wait(&sm.bar_tma, 0u, ok) && ok;
     } else {
         convert(z0);
     }
     for (int z = z0; z < z1 && nch > 0; ++z) {
         for (int ch = 0; ch < nch; ++ch) {
             const int nr = min(kRays, nseg - ch * kRays);
-            ok = tc::mbar_wait(&sm.bar_mma, mma_par) && ok;
+            ok = tc::mbar_wait(&sm.bar_mma, mma_par, ok) && ok;
             mma_par ^= 1u;
             tc::fence_after();
             // ---- accumulator -> G (warp w reads TMEM lanes 32 (w % 4) ..):

@@ -27,6 +27,7 @@
 
 #include "rectv_gb300.h"
 #include "rectv_internal.cuh"
+#include "tcgen05.cuh"
 
 namespace rectv {
 
@@ -1299,6 +1300,39 @@ int rectv_kernel_cost(rectv_handle *h, int which, double *bytes, double *flops) 
     });
 }
 
+}  // extern "C"
+
+namespace rectv {
+// One block waits on an mbarrier that nothing arrives on: first for `limit`
+// cycles, then nwait - 1 more times as the kernels' later waits do after an
+// expiry (healthy = false), and records the expiry in the handle's device
+// error counter, as the kernels do.  Nothing is in flight, so the context
+// stays usable.
+__global__ void k_wait_probe(int *err, long long limit, int nwait) {
+    __shared__ __align__(8) uint64_t bar;
+    if (threadIdx.x == 0) {
+        tc::mbar_init(&bar, 1);
+        tc::fence_mbar_init();
+    }
+    __syncthreads();
+    bool ok = tc::mbar_wait(&bar, 0u, true, limit);
+    for (int i = 1; i < nwait; ++i) ok = tc::mbar_wait(&bar, 0u, ok) && ok;
+    if (!ok && threadIdx.x == 0) atomicAdd(err, 1);
+}
+}  // namespace rectv
+
+extern "C" {
+
+int rectv_selftest_wait(rectv_handle *h, long long limit_cycles, int nwait) {
+    return guarded([&] {
+        rectv::Handle *H = live(h);
+        if (limit_cycles < 1 || limit_cycles > rectv::tc::kWaitLong || nwait < 1 || nwait > 100000)
+            throw rectv::Error(RECTV_ERR_ARG, "rectv_selftest_wait: 1 <= limit_cycles <= 2e9, 1 <= nwait <= 1e5");
+        rectv::k_wait_probe<<<1, 32, 0, H->stream>>>(H->gd.err, limit_cycles, nwait);
+        LAUNCH_CHECK("k_wait_probe");
+    });
+}
+
 int rectv_get_launch_counts(rectv_handle *h, int *kernels, int *fft_execs, int *batch_slices) {
     return guarded([&] {
         rectv::Handle *H = live(h);
@@ -1340,9 +1374,20 @@ double *g_noalloc_ptr[kNoAllocMaxDevices] = {};
 // Device address of g_noalloc_scratch on the current device.  The first call
 // on a device looks it up (host code cannot use the symbol itself as a device
 // address); that first call should therefore come before any stream capture.
-double *noalloc_scratch() {
+// The address is kept for the life of the process: it belongs to the
+// device's primary context, so after a cudaDeviceReset of that device it is
+// stale and this entry point must not be used on that device again.
+double *noalloc_scratch(cudaStream_t s) {
     int dev = 0;
     CUDA_CHECK(cudaGetDevice(&dev));
+    if (s) {
+        int sdev = -1;
+        CUDA_CHECK(cudaStreamGetDevice(s, &sdev));
+        if (sdev != dev)
+            throw Error(RECTV_ERR_ARG, "rectv_shrink_noalloc: the stream belongs to device " + std::to_string(sdev) +
+                                           ", the current device is " + std::to_string(dev) +
+                                           "; make the stream's device current");
+    }
     if (dev < 0 || dev >= kNoAllocMaxDevices) throw Error(RECTV_ERR_ARG, "rectv_shrink_noalloc: device ordinal out of range");
     std::lock_guard<std::mutex> lk(g_noalloc_mu);
     if (!g_noalloc_ptr[dev]) {
@@ -1358,7 +1403,11 @@ double *noalloc_scratch() {
 
 __global__ void k_noalloc_set_rho(float *dst, float rho) { *dst = rho; }
 
-// Fixed-order FP64 sum of the partials (same order as k_reduce_rho).
+// Fixed-order FP64 sum of the partials: one block, each thread sums a strided
+// share, then a tree over the threads.  The order differs from rectv_iterate's
+// two-stage reduction (k_sum_stage1 over contiguous shares, then
+// k_reduce_rho), so the sums agree with its history to FP64 rounding, not
+// bit for bit.
 __global__ void k_noalloc_sum3(const double *__restrict__ partials, int nparts, double *out) {
     __shared__ double sh[3][256];
     double a = 0, b = 0, c = 0;
@@ -1409,16 +1458,20 @@ extern "C" int rectv_shrink_noalloc(const float *d_u_cur, const float *d_u_old, 
         t.lambda1 = lambda1;
         t.sg = (float)(1.0 / (2.0 * std::cbrt(2.0) * ((double)lambda1 / 2.0)));
         t.sd = (float)(1.0 / (4.0 * std::cbrt(2.0) * ((double)lambda1 / 2.0)));
-        const long long nblocks = (long long)rectv::shrink_blocks(t, nchunks);
+        const long long gz = (long long)nchunks * (nzp + 1);
+        if (gz > 65535)
+            throw rectv::Error(RECTV_ERR_ARG, "rectv_shrink_noalloc: nchunks*(nzp+1) = " + std::to_string(gz) +
+                                                  " exceeds the grid limit of 65535");
+        const long long nblocks = (long long)((n + 1 + 31) / 32) * (long long)((n + 1 + 7) / 8) * gz;
         if (nblocks > rectv::kNoAllocMaxBlocks)
             throw rectv::Error(RECTV_ERR_ARG,
                                "rectv_shrink_noalloc: problem needs " + std::to_string(nblocks) +
                                    " thread blocks; the static scratch holds at most " +
                                    std::to_string(rectv::kNoAllocMaxBlocks) +
                                    " (ceil((n+1)/32)*ceil((n+1)/8)*nchunks*(nzp+1))");
-        double *scratch = rectv::noalloc_scratch();
-        float *rho_d = reinterpret_cast<float *>(scratch + rectv::kNoAllocRhoSlot);
         cudaStream_t s = static_cast<cudaStream_t>(stream);
+        double *scratch = rectv::noalloc_scratch(s);
+        float *rho_d = reinterpret_cast<float *>(scratch + rectv::kNoAllocRhoSlot);
         rectv::k_noalloc_set_rho<<<1, 1, 0, s>>>(rho_d, rho);
         LAUNCH_CHECK("k_noalloc_set_rho");
         const int nparts = rectv::launch_shrink(d_u_cur, d_u_old, d_psi, d_mu, rho_d, lambda0, 0, nchunks, t,

@@ -342,7 +342,7 @@ __global__ void __launch_bounds__(kThr, 1)
                 tc::fence_proxy_async();
                 fetch(buf ^ 1);
             }
-            ok = tc::mbar_wait(&sm.rbar[buf], (uint32_t)((seq >> 1) & 1)) && ok;
+            ok = tc::mbar_wait(&sm.rbar[buf], (uint32_t)((seq >> 1) & 1), ok) && ok;
             ++seq;
             const AdjRec *rec = sm.rec[buf];
             const uint32_t *inf = sm.info[buf];
@@ -442,7 +442,7 @@ __global__ void __launch_bounds__(kThr, 1)
                     if (have_next) {
                         const int ncnt = __ldg(tabs + nti).y;
                         const int nz0 = 2 * (nu % npairs);  // both slices of the next unit's pair
-                        ok = tc::mbar_wait(&sm.rbar[buf ^ 1], (uint32_t)((seq >> 1) & 1)) && ok;
+                        ok = tc::mbar_wait(&sm.rbar[buf ^ 1], (uint32_t)((seq >> 1) & 1), ok) && ok;
                         if (ct < ncnt) {
                             const AdjRec &nr = sm.rec[buf ^ 1][ct];
                             const int th = (unsigned)nr.thm >> 16, k = nr.k;
@@ -467,7 +467,7 @@ __global__ void __launch_bounds__(kThr, 1)
                 // ---- previous batch's MMAs done: add its product to the cell's
                 // FP32 sums; A, B and the accumulator are then free ----
                 if (nbu > 0) {
-                    ok = tc::mbar_wait(&sm.bar, (uint32_t)((nmma - 1) & 1)) && ok;
+                    ok = tc::mbar_wait(&sm.bar, (uint32_t)((nmma - 1) & 1), ok) && ok;
                     tc::fence_after();
                     float v[32], w2[32];
                     tc::ld32(tsl + ((uint32_t)(32 * q) << 16) + kColD + mt * kNP, v);
@@ -534,7 +534,7 @@ __global__ void __launch_bounds__(kThr, 1)
         }
         // ---- the unit's last product ----
         if (nbu > 0) {
-            ok = tc::mbar_wait(&sm.bar, (uint32_t)((nmma - 1) & 1)) && ok;
+            ok = tc::mbar_wait(&sm.bar, (uint32_t)((nmma - 1) & 1), ok) && ok;
             tc::fence_after();
             float v[32], w2[32];
             tc::ld32(tsl + ((uint32_t)(32 * q) << 16) + kColD + mt * kNP, v);

@@ -12,7 +12,12 @@
 //    word (the low 13 mantissa bits are ignored, i.e. truncated), so an FP32
 //    array is its own TF32 "high" part and x - trunc13(x) is the exact rest.
 //  * every wait is bounded by a clock limit; on expiry the caller records an
-//    error and carries on through its barriers, so no block can hang.
+//    error and carries on through its barriers.  A thread whose wait has
+//    expired once passes healthy = false to its later waits, which then give
+//    up after kWaitShort cycles instead of kWaitLong: a lost arrival costs
+//    one long wait per thread plus short ones, so a persistent block that
+//    waits thousands of times still ends promptly, and the short waits still
+//    let copies that are merely late land before the block moves on.
 #pragma once
 
 #include <cstdint>
@@ -84,9 +89,16 @@ __device__ __forceinline__ void bulk_g2s(void *dst, const void *src, uint32_t by
         : "memory");
 }
 
-// Wait for phase `parity` of the mbarrier; false after about one second.
-__device__ __forceinline__ bool mbar_wait(void *bar, uint32_t parity) {
+// Wait limits in SM clock cycles: about one second, and about 0.1 ms.
+constexpr long long kWaitLong = 2000000000LL;
+constexpr long long kWaitShort = 200000LL;
+
+// Wait for phase `parity` of the mbarrier; false when it has not completed
+// within kWaitLong cycles (kWaitShort when `healthy` is false, i.e. after an
+// earlier wait of this thread gave up), or within `limit` cycles if given.
+__device__ __forceinline__ bool mbar_wait(void *bar, uint32_t parity, bool healthy = true, long long limit = 0) {
     const uint32_t a = smem_addr(bar);
+    if (limit <= 0) limit = healthy ? kWaitLong : kWaitShort;
     const long long t0 = clock64();
     for (;;) {
         uint32_t done;
@@ -96,7 +108,7 @@ __device__ __forceinline__ bool mbar_wait(void *bar, uint32_t parity) {
             : "r"(a), "r"(parity)
             : "memory");
         if (done) return true;
-        if (clock64() - t0 > 2000000000LL) return false;
+        if (clock64() - t0 > limit) return false;
     }
 }
 

@@ -192,3 +192,27 @@ def test_geometry_cache_across_runs(lib_built, torch_cuda):
     assert np.array_equal(c, c2)
     ref = orc.run(g, theta, phi, n / 2, 1e-3 * 2.0, 2.0, 3, 2, nzp)
     assert np.linalg.norm(a - ref) / np.linalg.norm(ref) < 1e-4
+
+
+def test_bounded_wait_expires_promptly_and_is_reported(mods):
+    """A wait that runs out (an mbarrier that nothing arrives on, nothing in
+    flight) ends the kernel promptly, later waits of the same thread give up
+    after the short limit instead of a full one each, the expiry is reported
+    by rectv_synchronize, and the CUDA context stays usable."""
+    import time
+    torch, r, lib = mods
+    s = r.rectv(32, 64, 4, 2, 2, 1)
+    try:
+        s.synchronize()
+        t0 = time.perf_counter()
+        # 2e6 cycles (~1 ms) for the first wait, then 1000 short waits (~0.1 ms each)
+        lib.check(lib.load().rectv_selftest_wait(s._h, 2000000, 1000))
+        with pytest.raises(lib.RectvError) as e:
+            s.synchronize()
+        elapsed = time.perf_counter() - t0
+        assert e.value.code == 4  # RECTV_ERR_STATE
+        assert elapsed < 2.0, elapsed
+    finally:
+        s.free()
+    x = torch.arange(10, device="cuda", dtype=torch.float32)
+    assert float(x.sum()) == 45.0
