@@ -157,6 +157,77 @@ int rectv_get_launch_counts(rectv_handle *h, int *kernels, int *fft_execs, int *
  * CUDA context stays usable. */
 int rectv_selftest_wait(rectv_handle *h, long long limit_cycles, int nwait);
 
+/* Launch-shape autotuner (no reference counterpart; the reference launches
+ * every kernel with fixed 32x32 blocks, rectv.cu:32-33, radonusfft.cu:47-48).
+ * On a handle with a set-up session, times the candidate launch shapes of the
+ * tensor-core USFFT kernels -- slices per block of the gather (64, 32, 16, 8)
+ * and persistent blocks of the scatter (1, 3/4, 1/2 of the SMs) -- applies
+ * the fastest and reports them (zper, sc_grid; sc_grid 0 = one block per
+ * SM).  Results do not depend on these shapes.  Cached per (device, n,
+ * ntheta, m, slices per launch) for the process unless force != 0. */
+int rectv_autotune(rectv_handle *h, int force, int *zper, int *sc_grid);
+
+/* Device memory held by the handle (buffers and geometry), in bytes. */
+int rectv_get_device_bytes(rectv_handle *h, double *bytes);
+
+/* Estimated device memory of a handle with these dimensions (before creating
+ * it), in bytes: the figure the engine admits jobs by. */
+int rectv_estimate_bytes(int n, int ntheta, int m, int nz, int nzp, double *bytes);
+
+/* ---------------------------------------------------------------------------
+ * Multi-problem engine: the batched form and the serving loop (no reference
+ * counterpart: the reference solves one problem per rectv::run and re-zeroes
+ * f, fn, psi, mu at its start, rectv.cu:119-122).
+ *
+ * A job is one reconstruction with its own (n, ntheta, m, nz, nzp) and the
+ * arguments of rectv_run; its host buffers (g, theta, phi in; fres out) must
+ * stay valid until rectv_engine_run returns (pinned memory lets the copies
+ * overlap).  Jobs are admitted in order of arrival when their estimated device
+ * memory fits the budget and fewer than max_resident jobs run; an admitted
+ * job's state (u, psi, mu, rho, geometry, captured iteration graphs) stays
+ * resident until its last iteration, all its iterations are queued on its
+ * own stream, and the kernels of all running jobs overlap on the GPU.  A
+ * finished job's handle is kept for reuse by a later job of the same
+ * dimensions unless RECTV_ENGINE_NO_REUSE, and freed when memory is needed.
+ * Each job's result equals what rectv_run computes for it alone.
+ * ------------------------------------------------------------------------- */
+typedef struct rectv_engine rectv_engine;
+
+enum {
+    RECTV_ENGINE_NO_REUSE = 1,      /* free each job's handle when it finishes */
+    RECTV_ENGINE_AUTOTUNE = 2,      /* rectv_autotune each job's launch shapes (cached) */
+    RECTV_ENGINE_LARGEST_FIRST = 4  /* among equal arrival times, admit the most work first */
+};
+
+/* hbm_budget_bytes <= 0: the free device memory minus 4 GiB; max_resident <= 0:
+ * no limit on concurrently running jobs. */
+int rectv_engine_create(double hbm_budget_bytes, int max_resident, int flags, rectv_engine **out);
+
+/* Queues a job that arrives arrival_s seconds after rectv_engine_run starts.
+ * lambda0 is used as given (as rectv_run).  *job_id receives its index. */
+int rectv_engine_submit(rectv_engine *e, int n, int ntheta, int m, int nz, int nzp, const float *g,
+                        const float *theta, const float *phi, float center, float lambda0, float lambda1, int niter,
+                        int titer, double arrival_s, float *fres, int *job_id);
+
+/* Runs every submitted job to completion (or failure) and returns. */
+int rectv_engine_run(rectv_engine *e);
+
+/* Per job: times[3] = (arrival, admission, completion) in seconds after the
+ * run started, bytes[2] = (estimated, allocated) device memory,
+ * rho_rdiff[2] = last rho and ||f(k+1)-f(k)||^2, tune[2] = (gather slices per
+ * block, scatter blocks), *status = 0 waiting, 1 running, 2 done, 3 failed.
+ * Any output may be NULL. */
+int rectv_engine_job_info(rectv_engine *e, int job_id, double *times, double *bytes, double *rho_rdiff,
+                          int *tune, int *status);
+
+/* Failure message of a job ("" unless failed), truncated to len bytes. */
+int rectv_engine_job_error(rectv_engine *e, int job_id, char *buf, int len);
+
+/* stats[4] = (makespan s, peak device bytes admitted, budget, peak running jobs). */
+int rectv_engine_stats(rectv_engine *e, double *stats);
+
+void rectv_engine_destroy(rectv_engine *e);
+
 /* ---------------------------------------------------------------------------
  * Filtered backprojection and warm start (no counterpart run by the
  * reference: its ramp filter applyfilter and mask circ,

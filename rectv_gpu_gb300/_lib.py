@@ -15,6 +15,7 @@ LIB_PATH = os.path.join(_HERE, "librectv_gb300.so")
 _P = ctypes.c_void_p
 _I = ctypes.c_int
 _F = ctypes.c_float
+_D = ctypes.c_double
 _IP = ctypes.POINTER(ctypes.c_int)
 SIGNATURES = {
     "rectv_last_error": (ctypes.c_char_p, []),
@@ -42,6 +43,16 @@ SIGNATURES = {
     "rectv_kernel_cost": (_I, [_P, _I, _P, _P]),
     "rectv_get_launch_counts": (_I, [_P, _IP, _IP, _IP]),
     "rectv_selftest_wait": (_I, [_P, ctypes.c_longlong, _I]),
+    "rectv_autotune": (_I, [_P, _I, _IP, _IP]),
+    "rectv_get_device_bytes": (_I, [_P, _P]),
+    "rectv_estimate_bytes": (_I, [_I, _I, _I, _I, _I, _P]),
+    "rectv_engine_create": (_I, [_D, _I, _I, ctypes.POINTER(_P)]),
+    "rectv_engine_submit": (_I, [_P, _I, _I, _I, _I, _I, _P, _P, _P, _F, _F, _F, _I, _I, _D, _P, _IP]),
+    "rectv_engine_run": (_I, [_P]),
+    "rectv_engine_job_info": (_I, [_P, _I, _P, _P, _P, _IP, _IP]),
+    "rectv_engine_job_error": (_I, [_P, _I, ctypes.c_char_p, _I]),
+    "rectv_engine_stats": (_I, [_P, _P]),
+    "rectv_engine_destroy": (None, [_P]),
     "rectv_shrink_noalloc": (_I, [_P, _P, _P, _P, _I, _I, _I, _I, _F, _F, _F, _P, _P]),
     "rectv_preprocess": (_I, [_P, _P, _P, _P, _I, _I, _I, _I, _I, _I]),
     "rectv_fbp": (_I, [_P, _P, _P, _P, _F]),

@@ -57,7 +57,7 @@ constexpr int kK = 32;                       // 16 time samples x (re, im)
 constexpr int kTab = 256;                    // samples per work item
 constexpr int kThr = 512;
 constexpr int kWarps = kThr / 32;
-constexpr int kZPer = 64;                    // slices per block
+constexpr int kZPer = 64;                    // slices per block at most (UsGeo::zper)
 constexpr uint32_t kTmemCols = 512;
 constexpr uint32_t kColAhi = 0;              // TMEM columns: A hi [mt*32, +32)
 constexpr uint32_t kColAlo = kMT * kK;       //               A lo
@@ -123,7 +123,8 @@ __global__ void __launch_bounds__(kThr, 1)
     TcSmem &sm = *reinterpret_cast<TcSmem *>(tc_smem_raw);
     const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
     const int4 it = items[blockIdx.x];
-    const int z0 = blockIdx.y * kZPer, z1 = min(zb, z0 + kZPer);
+    const int zper = g.zper;
+    const int z0 = blockIdx.y * zper, z1 = min(zb, z0 + zper);
     const int tyi = it.x / g.NT, txi = it.x - tyi * g.NT;
     const int P = g.P;
     const int cnt = min(it.z, kTab);
@@ -452,7 +453,8 @@ void launch_gather_tc(float2 *rows, int zb, const GeoDev &gd, const UsGeo &g, co
                       int accumulate, cudaStream_t s) {
     if (gd.n_fwd_tc_items == 0) return;
     if (g.T != kT) throw Error(1, "tile size must be 16");
-    dim3 gs(gd.n_fwd_tc_items, (zb + kZPer - 1) / kZPer);
+    if (g.zper < 1 || g.zper > kZPer) throw Error(1, "gather slices per block must be in [1, 64]");
+    dim3 gs(gd.n_fwd_tc_items, (zb + g.zper - 1) / g.zper);
     k_gather_tc<<<gs, kThr, sizeof(TcSmem), s>>>(rows, gd.fwd_pts, gd.fwd_tc_items, gd.sincos, gd.kmat, gd.shiftfwd,
                                                  tmap, g, zb, jbase, accumulate, gd.err);
     LAUNCH_CHECK("k_gather_tc");

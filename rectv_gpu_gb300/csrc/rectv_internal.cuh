@@ -62,6 +62,11 @@ struct UsGeo {
     float cw;           // (pi/mu)/n : gather weight scale and 1/n of gather
     int T;              // tile core side
     int NT;             // tiles per side P/T
+    // launch shapes chosen per problem (tunable): slices per block of the
+    // tensor-core gather (1..64), and blocks of the persistent tensor-core
+    // scatter (0: one per SM)
+    int zper;
+    int sc_grid;
 };
 
 // Weights of one polar sample restricted to one 16x16 tile of the adjoint

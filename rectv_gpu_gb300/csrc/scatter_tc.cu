@@ -595,7 +595,7 @@ void launch_scatter_tc(const float2 *rowsc, float2 *spec, int zb, const GeoDev &
         CUDA_CHECK(cudaGetDevice(&dev));
         CUDA_CHECK(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
     }
-    const int grid = (int)std::min<long long>(nunits, nsm);
+    const int grid = (int)std::min<long long>(nunits, g.sc_grid > 0 ? g.sc_grid : nsm);
     if (!gd.adj_tabs || !gd.adj_info) throw Error(1, "adjoint table segmentation missing");
     k_scatter_tc<<<grid, kThr, kScSmemBytes, s>>>(rowsc, spec, gd.adj_recs, gd.adj_items, gd.adj_tabs,
                                                   gd.adj_tab_base, gd.adj_info, gd.kmat, gd.shiftadj, g, zb, npairs,

@@ -154,3 +154,24 @@ class rectv:
     def op_divergent(self, fn_ptr, h2_ptr, lambda1, tau):
         _lib.check(_lib.load().rectv_op_divergent(self._h, _addr(fn_ptr), _addr(h2_ptr), float(lambda1),
                                                   float(tau)))
+
+    def autotune(self, force=False):
+        """Pick the launch shapes of the tensor-core USFFT kernels for this
+        problem by timing them (after setup_device); returns (gather slices
+        per block, scatter blocks or 0 for one per SM)."""
+        z = ctypes.c_int()
+        sg = ctypes.c_int()
+        _lib.check(_lib.load().rectv_autotune(self._h, int(bool(force)), ctypes.byref(z), ctypes.byref(sg)))
+        return z.value, sg.value
+
+    def device_bytes(self):
+        b = ctypes.c_double()
+        _lib.check(_lib.load().rectv_get_device_bytes(self._h, ctypes.byref(b)))
+        return b.value
+
+
+def estimate_bytes(n, ntheta, m, nz, nzp):
+    """Estimated device memory of a rectv object with these dimensions."""
+    b = ctypes.c_double()
+    _lib.check(_lib.load().rectv_estimate_bytes(int(n), int(ntheta), int(m), int(nz), int(nzp), ctypes.byref(b)))
+    return b.value
