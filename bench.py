@@ -31,6 +31,9 @@ import numpy as np
 
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
+# hardware work queues for the concurrent streams of the multi-problem engine
+# (read at CUDA initialisation; a per-process setting)
+os.environ.setdefault("CUDA_DEVICE_MAX_CONNECTIONS", "32")
 
 WORKLOAD = dict(n=1024, nz=64, nzp=16, ntheta=2880, nrot=8, m=16, titer=4, lambda0=1e-3, lambda1=4.0)
 SMALL = dict(n=256, nz=16, nzp=8, ntheta=720, nrot=8, m=16, titer=4, lambda0=1e-3, lambda1=4.0)
@@ -287,6 +290,270 @@ def fp64_accuracy(torch, w, g_h, theta, phi, iters, nsub=2):
             "seconds": time.perf_counter() - t0}
 
 
+# ---------------------------------------------------------------------------
+# batched form and serving loop (many problems of uneven size on one GPU)
+# ---------------------------------------------------------------------------
+MIX = dict(n=(256, 512, 1024), nz=(4, 64), ntheta=(720, 1440, 2880), m=(8, 16), nrot=8, titer=4, lambda0=1e-3,
+           lambda1=4.0)
+
+
+def draw_jobs(seed, count, iters):
+    """Problems of the batched / serving mix: N from {256, 512, 1024}, Nz
+    uniform in [4, 64] (one chunk: Nzp = Nz), Ntheta from {720, 1440, 2880},
+    M from {8, 16}; `iters` = (lo, hi) outer iterations, uniform."""
+    rng = np.random.default_rng(seed)
+    jobs = []
+    for i in range(count):
+        n = int(rng.choice(MIX["n"]))
+        nz = int(rng.integers(MIX["nz"][0], MIX["nz"][1] + 1))
+        ntheta = int(rng.choice(MIX["ntheta"]))
+        m = int(rng.choice(MIX["m"]))
+        niter = int(rng.integers(iters[0], iters[1] + 1))
+        jobs.append(dict(n=n, nz=nz, nzp=nz, ntheta=ntheta, m=m, nrot=MIX["nrot"], niter=niter,
+                         titer=MIX["titer"], seed=seed * 1000 + i))
+    return jobs
+
+
+def make_job_data(torch, jobs, device):
+    """Per job: its own seeded phantom, forward-projected with this library's
+    operator plus 1% Gaussian noise, in page-locked host memory; and a
+    page-locked output array."""
+    from rectv_gpu_gb300 import rectv, takephi
+    from rectv_gpu_gb300.phantom import scan_angles
+    groups = {}
+    for j in jobs:
+        groups.setdefault((j["n"], j["ntheta"], j["m"]), []).append(j)
+    for (n, ntheta, m), js in groups.items():
+        nzmax = max(j["nz"] for j in js)
+        theta = scan_angles(ntheta, MIX["nrot"])
+        phi = takephi(ntheta, m)
+        obj = rectv(n, ntheta, m, nzmax, nzmax, 1)
+        d_th = torch.from_numpy(theta).to(device)
+        d_ph = torch.from_numpy(phi).to(device)
+        torch.cuda.synchronize()
+        obj.op_set_geometry(d_th.data_ptr(), d_ph.data_ptr(), n / 2)
+        for j in js:
+            w = dict(n=n, nz=j["nz"], m=m, ntheta=ntheta)
+            u = phantom_device(torch, w, seed=j["seed"], device=device)
+            dg = torch.empty((j["nz"], ntheta, n), dtype=torch.float32, device=device)
+            torch.cuda.synchronize()
+            obj.op_radonapr(dg.data_ptr(), u.data_ptr(), j["nz"], 1.0)
+            gen = torch.Generator(device=device).manual_seed(j["seed"])
+            dg += 0.01 * float(dg.abs().max()) * torch.randn(dg.shape, generator=gen, device=device)
+            gh = torch.empty(dg.shape, dtype=torch.float32, pin_memory=True)
+            gh.copy_(dg)
+            j["g"] = gh
+            j["out"] = torch.empty((j["nz"], m, n, n), dtype=torch.float32, pin_memory=True)
+            j["theta"], j["phi"] = theta, phi
+            del u, dg
+        obj.free()
+        del obj
+        torch.cuda.synchronize()
+    torch.cuda.empty_cache()  # the engine's budget is the free device memory
+    return jobs
+
+
+def run_engine(jobs, arrivals, max_resident=0, autotune=False, largest_first=False, keep=None):
+    """Runs the jobs through the engine; returns per-job info and stats."""
+    from rectv_gpu_gb300.engine import Engine
+    with Engine(max_resident=max_resident, autotune=autotune, largest_first=largest_first) as eng:
+        ids = []
+        for j, a in zip(jobs, arrivals):
+            ids.append(eng.submit(j["g"].numpy(), j["theta"], j["phi"], nzp=j["nzp"], niter=j["niter"],
+                                  titer=j["titer"], lambda0=MIX["lambda0"], lambda1=MIX["lambda1"], arrival=a,
+                                  out=j["out"].numpy(), copy_input=False))
+        eng.run()
+        infos = [eng.info(i) for i in ids]
+        st = eng.stats()
+        if keep is not None:
+            keep.extend(j["out"].numpy().copy() for j in jobs)
+    bad = [x for x in infos if x["status"] != "done"]
+    if bad:
+        raise RuntimeError("engine jobs failed: %s" % bad[0]["error"])
+    return infos, st
+
+
+def job_work(j):
+    return float(j["n"]) ** 2 * j["m"] * j["nz"] * j["niter"]
+
+
+def pretune(torch, jobs, device):
+    """Autotunes the launch shapes of every distinct problem shape once, in
+    isolation (the engine then applies the cached shapes at admission)."""
+    from rectv_gpu_gb300 import rectv
+    seen = {}
+    t0 = time.perf_counter()
+    for j in jobs:
+        key = (j["n"], j["ntheta"], j["m"], j["nz"], j["nzp"])
+        if key in seen:
+            continue
+        obj = rectv(j["n"], j["ntheta"], j["m"], j["nz"], j["nzp"], 1)
+        obj.set_verbose(False)
+        dg = j["g"].to(device)
+        d_th = torch.from_numpy(j["theta"]).to(device)
+        d_ph = torch.from_numpy(j["phi"]).to(device)
+        torch.cuda.synchronize()
+        obj.setup_device(dg.data_ptr(), d_th.data_ptr(), d_ph.data_ptr(), j["n"] / 2,
+                         MIX["lambda0"] * MIX["lambda1"], MIX["lambda1"], j["titer"])
+        seen[key] = obj.autotune()
+        obj.free()
+        del obj, dg
+    torch.cuda.synchronize()
+    return {"%dx%dx%dx%d" % k[:4]: v for k, v in seen.items()}, time.perf_counter() - t0
+
+
+def batched_form(torch, device, count=32, iters=8, seed=4):
+    """Config 4: `count` slice chunks of the mix, all arriving at once; the
+    engine (autotuned launch shapes, largest work first) against the same
+    jobs one at a time."""
+    jobs = make_job_data(torch, draw_jobs(seed, count, (iters, iters)), device)
+    tuned, tune_s = pretune(torch, jobs, device)
+    work = sum(job_work(j) for j in jobs)
+    run_engine(jobs[:2], [0.0, 0.0], autotune=True)  # warm-up of the engine path
+    mix_out, solo_out = [], []
+    infos, st = run_engine(jobs, [0.0] * len(jobs), autotune=True, largest_first=True, keep=mix_out)
+    infos1, st1 = run_engine(jobs, [0.0] * len(jobs), max_resident=1, autotune=True, largest_first=True,
+                             keep=solo_out)
+    same = all(np.array_equal(a, b) for a, b in zip(mix_out, solo_out))
+    return {
+        "workload": "%d slice chunks: N from {256,512,1024}, Nz uniform in [4,64] (Nzp=Nz), Ntheta from "
+                    "{720,1440,2880}, M from {8,16}, Nrot=8, titer=4, %d outer iterations each, seeded phantoms "
+                    "(seed %d)" % (count, iters, seed),
+        "voxel_updates": work,
+        "voxel_updates_per_s": work / st["makespan"], "makespan_s": st["makespan"],
+        "one_at_a_time_voxel_updates_per_s": work / st1["makespan"], "one_at_a_time_makespan_s": st1["makespan"],
+        "speedup_vs_one_at_a_time": st1["makespan"] / st["makespan"],
+        "peak_running": st["peak_running"], "peak_bytes": st["peak_bytes"], "budget_bytes": st["budget"],
+        "results_equal_one_at_a_time": same,
+        "autotune": {"shapes": tuned, "seconds": tune_s,
+                     "note": "(gather slices per block, scatter persistent blocks; 0 = one per SM) per "
+                             "NxNthetaxMxNz, timed in isolation before the runs"},
+        "shapes": [[j["n"], j["nz"], j["ntheta"], j["m"]] for j in jobs],
+    }, jobs
+
+
+def serving_form(torch, device, throughput, count, iters, seed=5, load=0.8):
+    """Config 5: a Poisson stream of `count` requests of the mix with `iters`
+    outer iterations each, at `load` times the rate the batched throughput
+    sustains; continuous batching (admission by the HBM budget, resident
+    state, concurrent jobs) against one request at a time (same arrivals)."""
+    jobs = make_job_data(torch, draw_jobs(seed, count, iters), device)
+    mean_work = sum(job_work(j) for j in jobs) / count
+    rate = load * throughput / mean_work
+    rng = np.random.default_rng(seed + 77)
+    arrivals = list(np.cumsum(rng.exponential(1.0 / rate, size=count)))
+    work = sum(job_work(j) for j in jobs)
+    out = {"workload": "%d requests of the batched mix with %d-%d outer iterations each (titer=4), Poisson "
+                       "arrivals at %.3f requests/s (%.0f%% of the batched throughput)"
+                       % (count, iters[0], iters[1], rate, 100 * load),
+           "rate_per_s": rate}
+    for name, mr in (("continuous_batching", 0), ("one_at_a_time", 1)):
+        infos, st = run_engine(jobs, arrivals, max_resident=mr, autotune=True)
+        lat = np.array([x["latency"] for x in infos])
+        out[name] = {"p50_latency_s": float(np.percentile(lat, 50)), "p99_latency_s": float(np.percentile(lat, 99)),
+                     "mean_latency_s": float(lat.mean()), "makespan_s": st["makespan"],
+                     "requests_per_s": count / st["makespan"], "voxel_updates_per_s": work / st["makespan"],
+                     "peak_running": st["peak_running"]}
+    return out
+
+
+CONFIG2 = dict(n=512, nz=32, nzp=8, ntheta=1440, nrot=8, m=16, titer=4, lambda0=1e-3, lambda1=4.0)
+
+
+def _ref_seconds_per_iter(g, theta, phi, w, iters):
+    """Seconds per outer iteration of the reference's CUDA build on g:
+    (time of run(1 + iters) - time of run(1)) / iters, in a child process."""
+    from oracle import ref_run
+    n = g.shape[2]
+    _, info = ref_run.run(g, theta, phi, n / 2, w["lambda0"] * w["lambda1"], w["lambda1"], 1, w["titer"], w["nzp"],
+                          time_niters=[1, 1 + iters], timeout=3000)
+    return (info["times"][1] - info["times"][0]) / iters
+
+
+def plain_fp32(torch, device, w, value, iters=2, steps=10):
+    """The reference's own CUDA build -- the plain FP32 form, src/cuda/*.cu
+    unchanged, compiled for sm_103a by oracle/ref_build.py -- timed through
+    rectv::run in a child process, beside this library:
+
+    * config 2 (N=512, Nz=32, Nzp=8, Ntheta=1440, M=16): both on the same
+      data, both measured;
+    * the benchmark workload: the reference cannot allocate it -- the size of
+      psi and mu, (n+1)^2 (m+1)(nzp+1) nz/nzp float4 (rectv.cu:15-16), is
+      computed in 32-bit int and overflows for n=1024, m=16, nz=64 (19.4e9),
+      so the allocation fails and run() faults on the host.  Its time per
+      outer iteration is extrapolated from single-chunk runs of the same
+      geometry (Nz = Nzp = 2, 4, 7, a least-squares line a + b Nz per chunk)
+      to 4 chunks of 16 slices."""
+    from oracle import ref_build
+    from rectv_gpu_gb300 import rectv, takephi
+    from rectv_gpu_gb300.phantom import scan_angles
+    if ref_build.build() is None:
+        return {"unavailable": "the reference's CUDA sources are not on this machine"}
+    out = {"what": "reference CUDA build (src/cuda/*.cu unchanged, nvcc sm_103a) through rectv::run: includes its "
+                   "host-side norm loop and managed-memory prefetches"}
+    t0 = time.perf_counter()
+    # ---- config 2, measured on both sides ----
+    c2 = CONFIG2
+    theta2 = scan_angles(c2["ntheta"], c2["nrot"])
+    phi2 = takephi(c2["ntheta"], c2["m"])
+    obj = rectv(c2["n"], c2["ntheta"], c2["m"], c2["nz"], c2["nzp"], 1)
+    obj.set_verbose(False)
+    d_th = torch.from_numpy(theta2).to(device)
+    d_ph = torch.from_numpy(phi2).to(device)
+    u = phantom_device(torch, c2, seed=0, device=device)
+    dg = torch.empty((c2["nz"], c2["ntheta"], c2["n"]), dtype=torch.float32, device=device)
+    torch.cuda.synchronize()
+    obj.op_set_geometry(d_th.data_ptr(), d_ph.data_ptr(), c2["n"] / 2)
+    obj.op_radonapr(dg.data_ptr(), u.data_ptr(), c2["nz"], 1.0)
+    gen = torch.Generator(device=device).manual_seed(7)
+    dg += 0.01 * float(dg.abs().max()) * torch.randn(dg.shape, generator=gen, device=device)
+    del u
+    obj.setup_device(dg.data_ptr(), d_th.data_ptr(), d_ph.data_ptr(), c2["n"] / 2, c2["lambda0"] * c2["lambda1"],
+                     c2["lambda1"], c2["titer"])
+    obj.autotune()
+    obj.iterate(3)
+    stream = torch.cuda.ExternalStream(obj.stream, device=device)
+    a = torch.cuda.Event(enable_timing=True)
+    b = torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    a.record(stream)
+    obj.iterate(steps)
+    b.record(stream)
+    torch.cuda.synchronize()
+    ours2 = steps / (a.elapsed_time(b) * 1e-3)
+    g2 = dg.cpu().numpy()
+    obj.free()
+    del obj, dg
+    torch.cuda.empty_cache()
+    ref2 = 1.0 / _ref_seconds_per_iter(g2, theta2, phi2, c2, iters)
+    out["config2"] = {"workload": workload_name(c2), "reference_iter_per_s": ref2, "ours_iter_per_s": ours2,
+                      "speedup": ours2 / ref2}
+    # ---- the benchmark workload: single-chunk runs, extrapolated ----
+    theta = scan_angles(w["ntheta"], w["nrot"])
+    phi = takephi(w["ntheta"], w["m"])
+    rng = np.random.default_rng(11)
+    pts = []
+    for nzs in (2, 4, 7):
+        g = (0.01 * rng.standard_normal((nzs, w["ntheta"], w["n"]))).astype(np.float32)
+        ws = dict(w, nz=nzs, nzp=nzs)
+        pts.append((nzs, _ref_seconds_per_iter(g, theta, phi, ws, iters)))
+    x = np.array([p[0] for p in pts], dtype=np.float64)
+    y = np.array([p[1] for p in pts])
+    bcoef, acoef = np.polyfit(x, y, 1)
+    chunks = w["nz"] // w["nzp"]
+    per = chunks * (acoef + bcoef * w["nzp"])
+    out["workload"] = {"workload": workload_name(w), "reference_iter_per_s": 1.0 / per,
+                       "reference_seconds_per_iteration": per, "kind": "extrapolated",
+                       "single_chunk_runs": [{"nz": int(p[0]), "seconds_per_iteration": p[1]} for p in pts],
+                       "model": "per chunk a + b*Nzp, a=%.3f s, b=%.3f s/slice, x%d chunks of %d slices"
+                                % (acoef, bcoef, chunks, w["nzp"]),
+                       "speedup": value * per}
+    out["value"] = 1.0 / per
+    out["unit"] = "iter/s"
+    out["seconds"] = time.perf_counter() - t0
+    return out
+
+
 def run_reference_arm(args, rank):
     """--impl reference: the reference's algorithm (FP64 oracle restatement; the
     reference has no CPU path and its CUDA build cannot travel) on host cores."""
@@ -360,6 +627,9 @@ def run_ours(args, rank, world, local_rank):
 
     # ---- device-resident timed region ----
     obj.setup_device(d_g.data_ptr(), d_theta.data_ptr(), d_phi.data_ptr(), center, lam0, lam1, titer)
+    t_tune = time.perf_counter()
+    tuned = obj.autotune()
+    t_tune = time.perf_counter() - t_tune
     obj.iterate(args.warmup)
     torch.cuda.synchronize()
     if dist:
@@ -453,6 +723,7 @@ def run_ours(args, rank, world, local_rank):
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
+        cpu_sample(w)  # warm: FFT plans, thread pool
         v, s, sample, workers = cpu_sample(w)
         cpu = {"value": v, "unit": "iter/s", "cores": workers, "kind": "port", "sample": sample}
 
@@ -477,9 +748,38 @@ def run_ours(args, rank, world, local_rank):
         "cufft_execs": ffts[0].value * args.steps,
         "rho_final": float(hist["rho"][-1]) if len(hist["rho"]) else None,
         "rel_err_vs_fp64": acc,
+        "autotune": {"gather_slices_per_block": tuned[0], "scatter_blocks": tuned[1] or "one per SM",
+                     "seconds": t_tune},
         "result_finite": finite,
     }
     obj.free()
+    del obj
+    torch.cuda.synchronize()
+    torch.cuda.empty_cache()
+    if rank == 0 and world == 1:
+        # first call: a fresh object (allocation, angle plan, adjoint records,
+        # graph capture) and rectv_run, as a user's first reconstruction runs
+        t0 = time.perf_counter()
+        fresh = rectv(n, ntheta, m, nz, nzp, 1)
+        fresh.set_verbose(False)
+        fresh.run(f_h.data_ptr(), g_h.data_ptr(), th_h.data_ptr(), ph_h.data_ptr(), center, lam0, lam1,
+                  args.steps, titer)
+        t1 = time.perf_counter()
+        fresh.free()
+        del fresh
+        line["e2e"]["first_call"] = {"value": args.steps / (t1 - t0), "unit": "iter/s", "seconds": t1 - t0,
+                                     "what": "rectv(...) creation + rectv_run of the same steps"}
+    del g_h, f_h
+    torch.cuda.empty_cache()
+    if rank == 0 and world == 1 and args.plain_iters > 0:
+        line["plain_fp32"] = plain_fp32(torch, dev, w, value, args.plain_iters)
+        if "value" in line["plain_fp32"]:
+            line["plain_fp32"]["speedup_e2e"] = line["e2e"]["value"] / line["plain_fp32"]["value"]
+    if rank == 0 and world == 1 and args.batched > 0:
+        line["batched"], _ = batched_form(torch, dev, count=args.batched, iters=args.batched_iters)
+        if args.serve > 0:
+            line["serving"] = serving_form(torch, dev, line["batched"]["voxel_updates_per_s"], args.serve,
+                                           tuple(args.serve_iters))
     if rank == 0:
         print(json.dumps(line))
     if dist:
@@ -501,6 +801,13 @@ def main():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--small", action="store_true", help="N=256 workload (quick check)")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
+    ap.add_argument("--plain-iters", type=int, default=2,
+                    help="outer iterations of the reference CUDA build timed on the same data (0: skip)")
+    ap.add_argument("--batched", type=int, default=32, help="slice chunks of the batched form (0: skip)")
+    ap.add_argument("--batched-iters", type=int, default=8, help="outer iterations per batched chunk")
+    ap.add_argument("--serve", type=int, default=32, help="requests of the serving run (0: skip)")
+    ap.add_argument("--serve-iters", type=int, nargs=2, default=[8, 16],
+                    help="range of outer iterations per request (the full serving config: 200 requests, 32 128)")
     ap.add_argument("--acc-iters", type=int, default=64,
                     help="outer iterations of the FP64 accuracy check on a 2-slice subset (0: skip)")
     ap.add_argument("--nz", type=int, default=None, help="slices (default: the workload's); for small ncu cases")

@@ -52,10 +52,16 @@ class Engine:
         self._keep = {}
 
     def submit(self, g, theta, phi, nzp, niter, titer, center=None, lambda0=1e-3, lambda1=1.0, arrival=0.0,
-               scale_lambda0=True):
+               scale_lambda0=True, out=None, copy_input=None):
         """Queue one reconstruction; g [nz, ntheta, n] float32, theta [ntheta],
         phi [m, 2*ntheta].  lambda0 is multiplied by lambda1 as Solver.recon
-        does (solver.py:76) unless scale_lambda0=False.  Returns the job id."""
+        does (solver.py:76) unless scale_lambda0=False.  `out` (float32
+        [nz, m, n, n], C-contiguous) receives the result, else a new array
+        does; g is copied into page-locked memory unless copy_input=False (the
+        caller's array is then used as is and must stay alive and unchanged
+        until run() returns).  Returns the job id."""
+        if copy_input is None:
+            copy_input = self._pin
         g = np.ascontiguousarray(g, dtype=np.float32)
         theta = np.ascontiguousarray(theta, dtype=np.float32)
         phi = np.ascontiguousarray(phi, dtype=np.float32)
@@ -67,13 +73,15 @@ class Engine:
             center = n / 2
         if scale_lambda0:
             lambda0 = lambda0 * lambda1
-        if self._pin:
+        gp, gt = g, None
+        if copy_input:
             gp, gt = _pinned(g.shape)
             gp[...] = g
-            out, ot = _pinned((nz, m, n, n))
-        else:
-            gp, gt = g, None
-            out, ot = np.empty((nz, m, n, n), dtype=np.float32), None
+        ot = None
+        if out is None:
+            out, ot = _pinned((nz, m, n, n)) if self._pin else (np.empty((nz, m, n, n), dtype=np.float32), None)
+        elif out.shape != (nz, m, n, n) or out.dtype != np.float32 or not out.flags.c_contiguous:
+            raise ValueError("out must be a C-contiguous float32 array [nz, m, n, n]")
         jid = ctypes.c_int()
         _lib.check(_lib.load().rectv_engine_submit(
             self._h, n, ntheta, m, nz, int(nzp), gp.ctypes.data, theta.ctypes.data, phi.ctypes.data, float(center),

@@ -161,3 +161,50 @@ def test_admm_reduces_data_misfit():
     r1 = np.linalg.norm(ops.radonapr(f) - g)
     assert r1 < 0.5 * r0
     assert all(h["rho"] > 0 for h in hist)
+
+
+# ---------------------------------------------------------------------------
+# Pins against the reference's own CUDA build: fixtures made by
+# tests/golden/make_ref_golden.py, which runs the reference's src/cuda/*.cu
+# (compiled unchanged for sm_103a by oracle/ref_build.py) on a GB300.
+# ---------------------------------------------------------------------------
+REF_PIN = 1e-5  # the reference computes in FP32 with __sinf/__cosf sample positions
+
+
+def _golden(name):
+    import os
+    return os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", name)
+
+
+def test_oracle_matches_reference_build_config1():
+    """Config 1 (32 ADMM iterations): the oracle's FP64 reconstruction
+    (committed) against the reference build's."""
+    ref = np.load(_golden("ref_c1_recon.npz"))
+    f64 = np.load(_golden("c1_recon.npz"))
+    err = np.linalg.norm(f64["f"].astype(np.float64) - ref["f"]) / np.linalg.norm(f64["f"].astype(np.float64))
+    assert err < REF_PIN, err
+    np.testing.assert_allclose(ref["rdiff"], f64["rdiff"], rtol=1e-4)
+
+
+def test_oracle_matches_reference_build_16_time_samples():
+    import sys
+    sys.path.insert(0, os.path.dirname(_golden("x")))
+    import make_ref_golden
+    c = make_ref_golden.M16
+    theta, phi, g = make_ref_golden.m16_inputs()
+    f, hist = orc.run(g, theta, phi, c["n"] / 2, c["lambda0"] * c["lambda1"], c["lambda1"], c["niter"], c["titer"],
+                      c["nzp"], return_history=True)
+    ref = np.load(_golden("ref_m16_recon.npz"))
+    err = np.linalg.norm(f - ref["f"]) / np.linalg.norm(f)
+    assert err < REF_PIN, err
+    np.testing.assert_allclose(ref["rdiff"], [x["rdiff"] for x in hist], rtol=1e-4)
+
+
+def test_oracle_check_adjoints_matches_reference_build():
+    """The reference test's own configuration (n=504, ntheta=2400, m=16)."""
+    import json
+    with open(_golden("ref_refconfig_adjoint.json")) as fh:
+        ref = np.array(json.load(fh)["res"])
+    with open(_golden("refconfig_adjoint.json")) as fh:
+        f64 = np.array(json.load(fh)["res"])
+    np.testing.assert_allclose(f64, ref, rtol=REF_PIN)
