@@ -231,6 +231,7 @@ struct Engine {
     // that make the job fail.
     bool admit(Job &j) {
         std::unique_ptr<Handle> h;
+        bool fresh = false;
         for (size_t i = 0; i < idle.size(); ++i)
             if (same_dims(*idle[i].second, j)) {
                 h = std::move(idle[i].second);
@@ -252,11 +253,17 @@ struct Engine {
                 if (e.code == RECTV_ERR_NOMEM && running > 0) return false;  // retry after a completion
                 throw;
             }
+            fresh = true;
         }
         h->verbose = false;
         const size_t gbytes = sizeof(float) * (size_t)j.nz * j.ntheta * j.n;
         CUDA_CHECK(cudaMemcpyAsync(h->gdata, j.g, gbytes, cudaMemcpyHostToDevice, h->stream));
         h->setup(j.theta, j.phi, j.center, j.lambda0, j.lambda1, j.titer);
+        if (fresh && running > 0 && used + (double)h->device_bytes() > budget) {
+            // the estimate was short: remember the real size and wait for memory
+            j.est_bytes = std::max(j.est_bytes, (double)h->device_bytes());
+            return false;
+        }
         if (tune) j.tune = autotune(*h, false);
         h->enqueue_iterations(j.niter);
         const size_t nf = (size_t)h->nzc * h->slab;

@@ -677,6 +677,8 @@ struct Handle {
             launch_crop_accum_real(reinterpret_cast<const float *>(spec), u, zb, tau, gd.deapod, ug, stream);
             return;
         }
+        if (lay.img_spec < (long long)ug.P * ug.P)
+            throw Error(RECTV_ERR_STATE, "rectv: spectra buffer sized for half planes, FP32 scatter needs full planes");
         launch_zero_split(spec, zb, gd, ug, stream);
         launch_scatter_adj(rowsc, spec, zb, gd, ug, stream);
         for (int i = 0; i < nimg; i += img_per_fft) {

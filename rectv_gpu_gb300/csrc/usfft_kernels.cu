@@ -363,7 +363,9 @@ void launch_gather_fwd(const float2 *spec, float2 *rows, int zb, const GeoDev &g
     const int mp = mp_for(g.m);
     for (int jb = 0; jb < g.m; jb += 16) {
         const int acc = jb > 0;
-        if (mp == 16) launch_gather_tc(rows, zb, gd, g, *tmap, jb, acc, s);
+        // the plan gives items with several samples per ray to the tensor-core
+        // gather from 8 time samples up (any group size: missing samples are zero)
+        if (gd.n_fwd_tc_items > 0) launch_gather_tc(rows, zb, gd, g, *tmap, jb, acc, s);
         if (gd.n_fwd_items == 0) continue;
         switch (mp) {
             case 1: gather_fwd_t<1, 16>(spec, rows, zb, gd, g, jb, acc, gd.err, s); break;
@@ -642,7 +644,9 @@ void launch_scatter_adj(const float2 *rowsc, float2 *spec, int zb, const GeoDev 
     if (g.T != 16) throw Error(1, "tile size must be 16");
     const int mp = mp_for(g.m);
     for (int jb = 0; jb < g.m; jb += 16) {
-        if (mp == 16 && gd.tc_scatter) {
+        // the tensor-core scatter fills the Hermitian half planes the spectra
+        // buffer is sized for (from 8 time samples up)
+        if (gd.tc_scatter) {
             launch_scatter_tc(rowsc, spec, zb, gd, g, jb, s);
             continue;
         }
