@@ -353,10 +353,11 @@ def make_job_data(torch, jobs, device):
     return jobs
 
 
-def run_engine(jobs, arrivals, max_resident=0, autotune=False, largest_first=False, keep=None):
+def run_engine(jobs, arrivals, max_resident=0, autotune=False, largest_first=False, age_priority=True, keep=None):
     """Runs the jobs through the engine; returns per-job info and stats."""
     from rectv_gpu_gb300.engine import Engine
-    with Engine(max_resident=max_resident, autotune=autotune, largest_first=largest_first) as eng:
+    with Engine(max_resident=max_resident, autotune=autotune, largest_first=largest_first,
+                age_priority=age_priority) as eng:
         ids = []
         for j, a in zip(jobs, arrivals):
             ids.append(eng.submit(j["g"].numpy(), j["theta"], j["phi"], nzp=j["nzp"], niter=j["niter"],
@@ -447,8 +448,9 @@ def serving_form(torch, device, throughput, count, iters, seed=5, load=0.8):
                        "arrivals at %.3f requests/s (%.0f%% of the batched throughput)"
                        % (count, iters[0], iters[1], rate, 100 * load),
            "rate_per_s": rate}
-    for name, mr in (("continuous_batching", 0), ("one_at_a_time", 1)):
-        infos, st = run_engine(jobs, arrivals, max_resident=mr, autotune=True)
+    for name, mr, prio in (("continuous_batching", 0, True), ("continuous_batching_equal_priority", 0, False),
+                           ("one_at_a_time", 1, False)):
+        infos, st = run_engine(jobs, arrivals, max_resident=mr, autotune=True, age_priority=prio)
         lat = np.array([x["latency"] for x in infos])
         out[name] = {"p50_latency_s": float(np.percentile(lat, 50)), "p99_latency_s": float(np.percentile(lat, 99)),
                      "mean_latency_s": float(lat.mean()), "makespan_s": st["makespan"],

@@ -196,7 +196,10 @@ typedef struct rectv_engine rectv_engine;
 enum {
     RECTV_ENGINE_NO_REUSE = 1,      /* free each job's handle when it finishes */
     RECTV_ENGINE_AUTOTUNE = 2,      /* rectv_autotune each job's launch shapes (cached) */
-    RECTV_ENGINE_LARGEST_FIRST = 4  /* among equal arrival times, admit the most work first */
+    RECTV_ENGINE_LARGEST_FIRST = 4, /* among equal arrival times, admit the most work first */
+    RECTV_ENGINE_AGE_PRIORITY = 8   /* each job's stream gets a lower priority than every job running
+                                       when it was admitted: the oldest runs first, newer jobs fill the
+                                       SMs it leaves idle */
 };
 
 /* hbm_budget_bytes <= 0: the free device memory minus 4 GiB; max_resident <= 0:

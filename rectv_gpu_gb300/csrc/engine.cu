@@ -154,6 +154,9 @@ struct Job {
     std::string error;
     std::unique_ptr<Handle> h;
     cudaEvent_t ev = nullptr;
+    cudaStream_t stream = nullptr;  // the job's stream (priority by age) while it runs
+    int priority = 0;
+    double acct = 0;                // bytes counted against the budget while it runs
     double rho_final = 0, rdiff_final = 0;
     Tune tune;
 };
@@ -166,6 +169,8 @@ struct Engine {
     bool reuse;
     bool tune;
     bool largest_first = false;
+    bool age_priority = false;
+    int prio_least = 0, prio_greatest = 0;  // stream priority range (numerically lower = higher)
     int device = 0;
     std::vector<std::unique_ptr<Job>> jobs;
     std::vector<std::pair<double, std::unique_ptr<Handle>>> idle;  // (time returned, handle)
@@ -187,6 +192,18 @@ struct Engine {
         reuse = !(flags & RECTV_ENGINE_NO_REUSE);
         tune = (flags & RECTV_ENGINE_AUTOTUNE) != 0;
         largest_first = (flags & RECTV_ENGINE_LARGEST_FIRST) != 0;
+        age_priority = (flags & RECTV_ENGINE_AGE_PRIORITY) != 0;
+        CUDA_CHECK(cudaDeviceGetStreamPriorityRange(&prio_least, &prio_greatest));
+    }
+
+    // Stream priority of a newly admitted job: with age priority, below every
+    // running job (the oldest runs first, newer jobs fill the SMs it leaves
+    // idle), down to the least priority; else the default.
+    int next_priority(const std::vector<Job *> &active) const {
+        if (!age_priority) return prio_least;
+        int p = prio_greatest - 1;
+        for (const Job *a : active) p = std::max(p, a->priority);
+        return std::min(prio_least, p + 1);
     }
 
     ~Engine() {
@@ -229,7 +246,7 @@ struct Engine {
 
     // Admits job j if it fits; false when it has to wait.  Throws on errors
     // that make the job fail.
-    bool admit(Job &j) {
+    bool admit(Job &j, const std::vector<Job *> &active) {
         std::unique_ptr<Handle> h;
         bool fresh = false;
         for (size_t i = 0; i < idle.size(); ++i)
@@ -256,6 +273,23 @@ struct Engine {
             fresh = true;
         }
         h->verbose = false;
+        // the job's own stream; the handle's earlier work has finished (fresh,
+        // or idle after its previous job's completion event)
+        const int prio = next_priority(active);
+        cudaStream_t st = nullptr;
+        CUDA_CHECK(cudaStreamCreateWithPriority(&st, cudaStreamNonBlocking, prio));
+        struct Unbind {  // on any early exit: back to the handle's stream, drop st
+            Handle *h;
+            cudaStream_t st;
+            ~Unbind() {
+                if (h) {
+                    cudaStreamSynchronize(st);
+                    h->bind_stream(nullptr);
+                }
+                if (st) cudaStreamDestroy(st);
+            }
+        } guard{h.get(), st};
+        h->bind_stream(st);
         const size_t gbytes = sizeof(float) * (size_t)j.nz * j.ntheta * j.n;
         CUDA_CHECK(cudaMemcpyAsync(h->gdata, j.g, gbytes, cudaMemcpyHostToDevice, h->stream));
         h->setup(j.theta, j.phi, j.center, j.lambda0, j.lambda1, j.titer);
@@ -270,8 +304,13 @@ struct Engine {
         CUDA_CHECK(cudaMemcpyAsync(j.fres, h->U[h->cur], sizeof(float) * nf, cudaMemcpyDeviceToHost, h->stream));
         if (!j.ev) CUDA_CHECK(cudaEventCreateWithFlags(&j.ev, cudaEventDisableTiming));
         CUDA_CHECK(cudaEventRecord(j.ev, h->stream));
+        guard.h = nullptr;  // the job keeps st until it finishes
+        guard.st = nullptr;
+        j.stream = st;
+        j.priority = prio;
         j.bytes = (double)h->device_bytes();
-        used += std::max(j.bytes, j.est_bytes);
+        j.acct = j.bytes;
+        used += j.acct;
         peak = std::max(peak, used);
         j.h = std::move(h);
         j.state = kRunning;
@@ -281,16 +320,27 @@ struct Engine {
         return true;
     }
 
+    void release_stream(Job &j) {
+        if (!j.stream) return;
+        if (j.h) {
+            cudaStreamSynchronize(j.stream);
+            j.h->bind_stream(nullptr);
+        }
+        cudaStreamDestroy(j.stream);
+        j.stream = nullptr;
+    }
+
     void finish(Job &j) {
         Handle &h = *j.h;
         h.collect_history();
+        release_stream(j);
         const size_t nf = (size_t)h.nzc * h.slab, total = (size_t)j.nz * h.slab;
         if (total > nf) std::memset(j.fres + nf, 0, sizeof(float) * (total - nf));
         if (!h.h_rho.empty()) {
             j.rho_final = h.h_rho.back();
             j.rdiff_final = h.h_rdiff.back();
         }
-        used -= std::max(j.bytes, j.est_bytes);
+        used -= j.acct;
         j.done = now();
         j.state = kDone;
         --running;
@@ -304,9 +354,10 @@ struct Engine {
 
     void fail(Job &j, const std::string &msg) {
         if (j.state == kRunning) {
-            used -= std::max(j.bytes, j.est_bytes);
+            used -= j.acct;
             --running;
         }
+        release_stream(j);
         j.h.reset();
         j.state = kFailed;
         j.error = msg;
@@ -350,7 +401,7 @@ struct Engine {
                 Job &j = *order[next];
                 bool ok = false;
                 try {
-                    ok = admit(j);
+                    ok = admit(j, active);
                 } catch (const std::exception &e) {
                     fail(j, e.what());
                     ++next;

@@ -149,7 +149,8 @@ struct Handle {
     bool freed = false;
     bool verbose = true;
     bool use_graphs = true;
-    cudaStream_t stream = nullptr;
+    cudaStream_t stream = nullptr;      // where work is queued (bind_stream)
+    cudaStream_t own_stream = nullptr;  // created with the handle, owns its allocations
     std::vector<void *> owned;
 
     Layout lay;
@@ -248,6 +249,7 @@ struct Handle {
 
     void init() {
         CUDA_CHECK(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
+        own_stream = stream;
         usfft_prepare();
         gather_tc_prepare();
         scatter_tc_prepare();
@@ -440,8 +442,20 @@ struct Handle {
         gd.err = err;
     }
 
+    // Queue this handle's work on s (a stream of the same device) from now on;
+    // nullptr returns to the handle's own stream.  The caller orders s after
+    // the handle's earlier work (the engine binds only idle handles).
+    void bind_stream(cudaStream_t s) {
+        stream = s ? s : own_stream;
+        if (plans_made)
+            for (cufftHandle h : {p_r2c2d, p_c2c2d, p_rows_c2c, p_rows_r2c, p_c2r2d})
+                CUFFT_CHECK(cufftSetStream(h, stream));
+    }
+
     void release() {
         if (stream) cudaStreamSynchronize(stream);
+        if (own_stream && own_stream != stream) cudaStreamSynchronize(own_stream);
+        stream = own_stream;
         drop_graphs();
         free_geo();
         if (plans_made) {
@@ -457,8 +471,8 @@ struct Handle {
         if (stats_host) cudaFreeHost(stats_host);
         stats_host = nullptr;
         stats_host_cap = 0;
-        if (stream) cudaStreamDestroy(stream);
-        stream = nullptr;
+        if (own_stream) cudaStreamDestroy(own_stream);
+        stream = own_stream = nullptr;
         freed = true;
         session = false;
     }

@@ -26,6 +26,7 @@ from . import _lib
 NO_REUSE = 1
 AUTOTUNE = 2
 LARGEST_FIRST = 4
+AGE_PRIORITY = 8
 STATUS = {0: "waiting", 1: "running", 2: "done", 3: "failed"}
 
 
@@ -42,9 +43,14 @@ def _pinned(shape, dtype=np.float32):
 
 class Engine:
     def __init__(self, budget_bytes=0.0, max_resident=0, reuse=True, autotune=False, largest_first=False,
-                 pin=True):
+                 age_priority=True, pin=True):
+        """budget_bytes <= 0: the free device memory minus 4 GiB; max_resident
+        <= 0: no limit on running jobs; age_priority: each job's stream has a
+        lower priority than the jobs running when it was admitted (the oldest
+        runs first, newer jobs fill the SMs it leaves idle)."""
         lib = _lib.load()
-        flags = (0 if reuse else NO_REUSE) | (AUTOTUNE if autotune else 0) | (LARGEST_FIRST if largest_first else 0)
+        flags = ((0 if reuse else NO_REUSE) | (AUTOTUNE if autotune else 0) | (LARGEST_FIRST if largest_first else 0)
+                 | (AGE_PRIORITY if age_priority else 0))
         h = ctypes.c_void_p()
         _lib.check(lib.rectv_engine_create(float(budget_bytes), int(max_resident), flags, ctypes.byref(h)))
         self._h = h
