@@ -64,3 +64,27 @@ def test_solver_signature_matches_reference():
 def test_library_is_sm103a_only(lib_built):
     from rectv_gpu_gb300 import build
     assert build.ARCH == ["-gencode", "arch=compute_103a,code=sm_103a"]
+
+
+def test_estimate_bytes_is_host_arithmetic(lib_built):
+    """rectv_estimate_bytes needs no GPU: the sizes the engine admits jobs by
+    (config 3: about 94.5 GB, measured on the GPU: 94.4 GB)."""
+    from rectv_gpu_gb300 import _lib
+    from rectv_gpu_gb300.rectv import estimate_bytes
+    c3 = estimate_bytes(1024, 2880, 16, 64, 16)
+    assert 90e9 < c3 < 100e9
+    assert estimate_bytes(512, 1440, 16, 32, 8) < estimate_bytes(512, 1440, 16, 64, 8)
+    # fewer than 8 time samples take the FP32 scatter with full periodic planes
+    assert estimate_bytes(256, 720, 4, 8, 8) > 0
+    with pytest.raises(_lib.RectvError):
+        estimate_bytes(64, 128, 8, 4, 8)  # nzp > nz
+
+
+def test_engine_without_gpu_reports_an_error(lib_built):
+    torch = pytest.importorskip("torch")
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    from rectv_gpu_gb300 import _lib
+    from rectv_gpu_gb300.engine import Engine
+    with pytest.raises(_lib.RectvError):
+        Engine(budget_bytes=1e9)

@@ -41,3 +41,53 @@ def test_oracle_ingest_matches_reference_formula():
     got = orc.preprocess(data, dark, flat)
     assert got.shape == (nz, ntheta, n)
     assert np.allclose(got, ref, rtol=1e-14, atol=0)
+
+
+def test_tiff_ifd_follows_the_baseline_spec(tmp_path):
+    """Checks the file against the TIFF 6.0 baseline rules, independently of
+    read_tiff: IFD entries sorted by tag, the required tags of a grayscale
+    image present, one strip covering the whole image, IEEE float samples."""
+    import struct
+    p = str(tmp_path / "b.tiff")
+    img = np.arange(35, dtype=np.float32).reshape(5, 7)
+    tiff.write_tiff(p, img)
+    buf = open(p, "rb").read()
+    (ifd,) = struct.unpack_from("<I", buf, 4)
+    (n,) = struct.unpack_from("<H", buf, ifd)
+    tags = {}
+    order = []
+    for i in range(n):
+        tag, typ, cnt = struct.unpack_from("<HHI", buf, ifd + 2 + 12 * i)
+        val = struct.unpack_from("<H" if typ == 3 else "<I", buf, ifd + 10 + 12 * i)[0]
+        tags[tag] = val
+        order.append(tag)
+    assert order == sorted(order)
+    for required in (256, 257, 258, 259, 262, 273, 277, 278, 279):
+        assert required in tags
+    assert (tags[256], tags[257], tags[258], tags[259], tags[277], tags[339]) == (7, 5, 32, 1, 1, 3)
+    assert tags[278] == 5 and tags[279] == 35 * 4
+    assert np.array_equal(np.frombuffer(buf, "<f4", 35, tags[273]).reshape(5, 7), img)
+    assert struct.unpack_from("<I", buf, ifd + 2 + 12 * n)[0] == 0  # single image
+
+
+def test_standard_readers_read_the_stack(tmp_path):
+    """tifffile or PIL, where installed, read the files back (neither is on
+    the build image)."""
+    vol = np.random.default_rng(2).standard_normal((2, 9, 11)).astype(np.float32)
+    names = tiff.write_tiff_stack(vol, str(tmp_path / "rec_t"))
+    readers = []
+    try:
+        import tifffile
+        readers.append(lambda f: tifffile.imread(f))
+    except ImportError:
+        pass
+    try:
+        from PIL import Image
+        readers.append(lambda f: np.asarray(Image.open(f), dtype=np.float32))
+    except ImportError:
+        pass
+    if not readers:
+        import pytest
+        pytest.skip("no standard TIFF reader installed (tifffile, PIL)")
+    for rd in readers:
+        assert np.array_equal(np.stack([rd(n) for n in names]), vol)
