@@ -699,17 +699,27 @@ def run_ours(args, rank, world, local_rank):
         "k_scatter_tc": "block barriers and the per-cell ray sums on the CUDA cores (shared-memory loads), "
                         "the tcgen05 time-sample GEMM (3xTF32) at ~14% of the tensor pipe; DRAM traffic 4.0x "
                         "the algorithmic bytes (float2 atomics read and write every Hermitian half-plane cell "
-                        "twice) at 13% of the DRAM peak, so not DRAM-bound",
+                        "twice), about 1.7 TB/s (25% of the DRAM peak) at full size, so not DRAM-bound",
         "k_gather_tc": "shared-memory bandwidth of the per-sample 81-tap sums and of the TMEM -> shared "
                        "read-out of G, block barriers; TMA-staged footprints, DRAM traffic 3.0x the spectra "
                        "(overlapping footprints) at 8% of the DRAM peak",
         "k_graddiv": "HBM bandwidth", "k_shrink": "HBM bandwidth",
         KERNEL_NAMES[4]: "HBM bandwidth", KERNEL_NAMES[5]: "HBM bandwidth"}[KERNEL_NAMES[dom]]
+    fma = ctypes.c_double()
+    fma2 = ctypes.c_double()
+    _lib.check(lib.rectv_measure_fp32_peak(ctypes.byref(fma), ctypes.byref(fma2)))
+    fp32_rate = flops.value / (ktimes[dom] * 1e-3) / 1e12
     roofline = {"bound": "hbm", "limiter": limiter, "kernel": KERNEL_NAMES[dom], "achieved": achieved,
                 "peak": peak,
                 "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / peak,
                 "traffic": ncu_traffic(KERNEL_NAMES[dom], workload_name(w)),
-                "algorithmic_bytes": bytes_.value, "fp32_tflops": flops.value / (ktimes[dom] * 1e-3) / 1e12,
+                "algorithmic_bytes": bytes_.value, "fp32_tflops": fp32_rate,
+                "compute": {"fp32_equivalent_tflops": fp32_rate, "fp32_peak_tflops": fma2.value,
+                            "fp32_peak_scalar_tflops": fma.value, "frac": fp32_rate / fma2.value,
+                            "note": "flops of the direct formulation (81 taps x M time samples per polar sample, "
+                                    "complex); the kernel does fewer on the CUDA cores (time samples mixed on the "
+                                    "tensor cores). Peaks measured in this run (rectv_measure_fp32_peak): packed "
+                                    "fma.rn.f32x2 and scalar fma.rn chains on every SM"},
                 "ms_per_launch": ktimes[dom],
                 "per_iteration_ms": {KERNEL_NAMES[k]: share[k] for k in share}}
 

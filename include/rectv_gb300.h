@@ -157,6 +157,11 @@ int rectv_get_launch_counts(rectv_handle *h, int *kernels, int *fft_execs, int *
  * CUDA context stays usable. */
 int rectv_selftest_wait(rectv_handle *h, long long limit_cycles, int nwait);
 
+/* FP32 FMA peak of the current device (the compute roofline of the CUDA-core
+ * parts of the USFFT kernels), measured with scalar fma.rn and packed
+ * fma.rn.f32x2 chains on every SM, in TFLOP/s. */
+int rectv_measure_fp32_peak(double *tflops_fma, double *tflops_fma2);
+
 /* Launch-shape autotuner (no reference counterpart; the reference launches
  * every kernel with fixed 32x32 blocks, rectv.cu:32-33, radonusfft.cu:47-48).
  * On a handle with a set-up session, times the candidate launch shapes of the

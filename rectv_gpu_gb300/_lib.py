@@ -44,6 +44,7 @@ SIGNATURES = {
     "rectv_get_launch_counts": (_I, [_P, _IP, _IP, _IP]),
     "rectv_selftest_wait": (_I, [_P, ctypes.c_longlong, _I]),
     "rectv_autotune": (_I, [_P, _I, _IP, _IP]),
+    "rectv_measure_fp32_peak": (_I, [_P, _P]),
     "rectv_get_device_bytes": (_I, [_P, _P]),
     "rectv_estimate_bytes": (_I, [_I, _I, _I, _I, _I, _P]),
     "rectv_engine_create": (_I, [_D, _I, _I, ctypes.POINTER(_P)]),

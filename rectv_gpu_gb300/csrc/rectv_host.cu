@@ -327,6 +327,79 @@ int rectv_kernel_cost(rectv_handle *h, int which, double *bytes, double *flops) 
 }  // extern "C"
 
 namespace rectv {
+// FP32 FMA throughput: 8 independent chains per thread of scalar fma.rn
+// (packed = 0) or packed fma.rn.f32x2 (packed = 1), enough blocks to fill
+// every SM; the result is written so that the chains are not removed.
+__global__ void k_fma_peak(float *out, int iters, int packed) {
+    float2 a[8];
+#pragma unroll
+    for (int i = 0; i < 8; ++i) a[i] = make_float2(threadIdx.x * 1e-7f + i, blockIdx.x * 1e-7f - i);
+    const float2 b = make_float2(0.999999f, 0.999998f), c = make_float2(1e-7f, 2e-7f);
+    if (packed) {
+        for (int k = 0; k < iters; ++k)
+#pragma unroll
+            for (int i = 0; i < 8; ++i) {
+                unsigned long long d;
+                asm volatile("fma.rn.f32x2 %0, %1, %2, %3;"
+                             : "=l"(d)
+                             : "l"(*reinterpret_cast<const unsigned long long *>(&a[i])),
+                               "l"(*reinterpret_cast<const unsigned long long *>(&b)),
+                               "l"(*reinterpret_cast<const unsigned long long *>(&c)));
+                a[i] = *reinterpret_cast<const float2 *>(&d);
+            }
+    } else {
+        for (int k = 0; k < iters; ++k)
+#pragma unroll
+            for (int i = 0; i < 8; ++i) {
+                a[i].x = fmaf(a[i].x, b.x, c.x);
+                a[i].y = fmaf(a[i].y, b.y, c.y);
+            }
+    }
+    float s = 0.f;
+#pragma unroll
+    for (int i = 0; i < 8; ++i) s += a[i].x + a[i].y;
+    out[blockIdx.x * blockDim.x + threadIdx.x] = s;
+}
+}  // namespace rectv
+
+extern "C" int rectv_measure_fp32_peak(double *tflops_fma, double *tflops_fma2) {
+    return rectv::guarded([&] {
+        if (!tflops_fma || !tflops_fma2) throw rectv::Error(RECTV_ERR_ARG, "rectv_measure_fp32_peak: null output");
+        int dev = 0, nsm = 0;
+        CUDA_CHECK(cudaGetDevice(&dev));
+        CUDA_CHECK(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+        const int threads = 256, blocks = nsm * 8, iters = 4096;
+        float *out = nullptr;
+        cudaStream_t s = nullptr;
+        cudaEvent_t a = nullptr, b = nullptr;
+        CUDA_CHECK(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
+        CUDA_CHECK(cudaMallocAsync(&out, sizeof(float) * threads * blocks, s));
+        CUDA_CHECK(cudaEventCreate(&a));
+        CUDA_CHECK(cudaEventCreate(&b));
+        for (int packed = 0; packed < 2; ++packed) {
+            float best = 1e30f;
+            for (int rep = 0; rep < 4; ++rep) {  // the first launch warms up; best of the rest
+                CUDA_CHECK(cudaEventRecord(a, s));
+                rectv::k_fma_peak<<<blocks, threads, 0, s>>>(out, iters, packed);
+                LAUNCH_CHECK("k_fma_peak");
+                CUDA_CHECK(cudaEventRecord(b, s));
+                CUDA_CHECK(cudaEventSynchronize(b));
+                float ms = 0.f;
+                CUDA_CHECK(cudaEventElapsedTime(&ms, a, b));
+                if (rep > 0) best = std::min(best, ms);
+            }
+            const double flops = 2.0 * 16 * (double)iters * threads * blocks;  // 16 FMAs per thread and iteration
+            (packed ? *tflops_fma2 : *tflops_fma) = flops / (best * 1e-3) / 1e12;
+        }
+        CUDA_CHECK(cudaFreeAsync(out, s));
+        CUDA_CHECK(cudaStreamSynchronize(s));
+        cudaEventDestroy(a);
+        cudaEventDestroy(b);
+        cudaStreamDestroy(s);
+    });
+}
+
+namespace rectv {
 // One block waits on an mbarrier that nothing arrives on: first for `limit`
 // cycles, then nwait - 1 more times as the kernels' later waits do after an
 // expiry (healthy = false), and records the expiry in the handle's device

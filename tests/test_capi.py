@@ -13,7 +13,7 @@ ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 def header_symbols():
     txt = open(os.path.join(ROOT, "include", "rectv_gb300.h")).read()
     txt = re.sub(r"/\*.*?\*/", "", txt, flags=re.S)
-    return sorted(set(re.findall(r"\b(rectv_[a-z_]+)\s*\(", txt)))
+    return sorted(set(re.findall(r"\b(rectv_[a-z0-9_]+)\s*\(", txt)))
 
 
 def test_header_declares_reference_replacements():
