@@ -148,6 +148,18 @@ int rectv_kernel_cost(rectv_handle *h, int which, double *bytes, double *flops);
  * executions; and the batch size in slices. */
 int rectv_get_launch_counts(rectv_handle *h, int *kernels, int *fft_execs, int *batch_slices);
 
+/* USFFT path of the handle's current geometry (no reference counterpart: the
+ * reference interpolates every ray, kernels_radonusfft.cuh:81-144).  *ndir =
+ * number of ray directions (theta modulo pi) when the rays of a direction
+ * share their sample positions (scans over several half-turns: the
+ * interpolation runs once per position, dir_kernels.cu), 0 when every ray is
+ * interpolated (tensor-core or FP32 kernels); *nrays = ntheta.  Selected at
+ * geometry set-up: directions are used when the rays average at least 2.5
+ * per direction (RECTV_DIRS=0 never, RECTV_DIRS=1 whenever possible) and
+ * rays are grouped when their samples agree within RECTV_DIR_TOL grid cells
+ * (default 2e-3). */
+int rectv_get_directions(rectv_handle *h, int *ndir, int *nrays);
+
 /* Self-test of the bounded waits of the tensor-core and TMA kernels: queues
  * on the handle's stream one block that waits on an mbarrier nothing arrives
  * on, first for limit_cycles SM cycles, then nwait - 1 more times with the

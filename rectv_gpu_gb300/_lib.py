@@ -42,6 +42,7 @@ SIGNATURES = {
     "rectv_launch_kernel": (_I, [_P, _I, _I]),
     "rectv_kernel_cost": (_I, [_P, _I, _P, _P]),
     "rectv_get_launch_counts": (_I, [_P, _IP, _IP, _IP]),
+    "rectv_get_directions": (_I, [_P, _IP, _IP]),
     "rectv_selftest_wait": (_I, [_P, ctypes.c_longlong, _I]),
     "rectv_autotune": (_I, [_P, _I, _IP, _IP]),
     "rectv_measure_fp32_peak": (_I, [_P, _P]),

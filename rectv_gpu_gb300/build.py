@@ -22,7 +22,7 @@ LIB_NAME = "librectv_gb300.so"
 LIB_PATH = os.path.join(HERE, LIB_NAME)
 BUILD_DIR = os.path.join(HERE, "_build")
 
-SOURCES = ["plan.cpp", "usfft_kernels.cu", "gather_tc.cu", "scatter_tc.cu", "fft_kernels.cu", "tv_kernels.cu", "io_kernels.cu", "rectv_host.cu", "engine.cu"]
+SOURCES = ["plan.cpp", "usfft_kernels.cu", "gather_tc.cu", "scatter_tc.cu", "dir_kernels.cu", "fft_kernels.cu", "tv_kernels.cu", "io_kernels.cu", "rectv_host.cu", "engine.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

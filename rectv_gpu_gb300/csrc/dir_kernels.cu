@@ -1,0 +1,474 @@
+// USFFT gather and scatter for scans that revisit their directions.
+//
+// A scan over several half-turns sees every direction (theta modulo pi) more
+// than once: rays theta, theta + pi, theta + 2 pi, ... sample the same points
+// of the frequency plane (sample k of ray theta + pi is sample n - k of ray
+// theta), and only their time weights K'(theta, j) differ.  The Gaussian
+// interpolation (gather, kernels_radonusfft.cuh:81-144: 81 taps per sample)
+// is linear and does not depend on a ray's time, so it is done once per
+// position p = (direction d, 1 <= q < n) and time sample j, and the rays of
+// the position are formed from it (the basis sums of operators.cu:143-152
+// and 171-176 as the mixing K'):
+//
+//   forward:  S_j(p) = sum_taps w(p, c) F_j(c)
+//             row(theta, k) = f(k) sum_j K'(theta, j) S_j(p)        (every ray theta of p)
+//   adjoint:  E_j(p) = sum_{rays theta of p} conj K'(theta, j) f'(k) e(theta, k)
+//             F_j(c) += sum_p w(p, c) E_j(p)
+//
+// with k = q for the rays of the representative's orientation and k = n - q
+// for the opposite ones, f(k) = (-1)^(k+1) shiftfwd(k) (pi/mu)/n and f'(k) the
+// same with shiftadj.  At 2880 angles over 8 half-turns there are 360
+// directions: one eighth of the taps of the per-ray kernels, and the [ntheta x
+// M] basis contraction becomes an 8-ray x 16-time-sample mix per position
+// (FP32 on the CUDA cores: 16 complex products per ray sample, against 1296
+// for the taps of the per-ray formulation).
+//
+// Both kernels take 16 time samples [jbase, jbase + 16) per launch.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+
+#include "rectv_internal.cuh"
+#include "usfft_common.cuh"
+
+namespace rectv {
+
+namespace {
+
+constexpr int kT = 16;
+constexpr int kFW = kT + 2 * kR;   // footprint side (24)
+constexpr int kCells = kFW * kFW;  // 576
+constexpr int kChunks = 8;         // 16-byte chunks of a cell: time samples (2i, 2i+1), complex
+
+// ---- forward ----
+constexpr int kFThr = 256;
+constexpr int kFCap = 128;  // positions per forward item
+constexpr int kFill = 2 * kFW * (kFW / 4) * 32;  // 8-byte copies of one footprint (9216)
+
+struct FwdSmem {
+    float4 fp[kCells * kChunks];  // footprint of 16 time samples, cell-major; chunk i of cell c at
+                                  // slot (i + 2 (c & 3)) & 7
+    float wx[kFCap][kTaps];       // (-1)^b w_b of the 9 x taps
+    float wy[kFCap][kTaps];       // (-1)^a w_a of the 9 y taps times the stencil origin's fftshift sign
+    int org[kFCap];               // footprint cell of the stencil origin
+    int pid[kFCap];               // d*n + q, -1: none
+};
+
+// ---- adjoint ----
+constexpr int kAHalf = kT * kT;        // threads per slice: one per cell
+constexpr int kAThr = 2 * kAHalf;      // a slice pair per block
+constexpr int kATab = 256;             // entries per table (host table builder)
+constexpr int kAMaxSeg = 16;           // directions per table (host table builder)
+constexpr int kAInfo = adj_info_words(kAMaxSeg);
+
+struct AdjSmem {
+    AdjRec rec[2][kATab];          // geometry records of this table and the next
+    uint32_t info[2][kAInfo];      // their direction segmentation
+    float4 e[2][kATab][kChunks];   // E_j of the table's entries, both slices of the pair
+};
+
+__device__ __forceinline__ uint32_t saddr(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void cp_async8(void *dst, const void *src) {
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(saddr(dst)), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async16(void *dst, const void *src) {
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(saddr(dst)), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_wait() {
+    asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory");
+}
+
+// conj(a) b
+__device__ __forceinline__ float2 cmulc(float2 a, float2 b) {
+    return make_float2(a.x * b.x + a.y * b.y, a.x * b.y - a.y * b.x);
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// Forward: one block (256 threads) per (work item, slices); an item is at
+// most 128 positions whose stencils start in one 16x16 tile of the
+// oversampled grid.  Per slice the tile's 24x24-cell footprint of 16 time
+// samples is copied (8-byte cp.async, cell-major) from the halo-padded
+// spectra (tiles right of the Nyquist column read the mirrored cells and
+// conjugate), then eight lanes per position (two time samples each) sum the
+// 81 taps, and mix the position's rays: each lane forms its two time
+// samples' share of all eight rays of a round, the eight lanes add their
+// shares by recursive halving (14 shuffles) and lane i keeps ray i.
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(kFThr, 2)
+    k_gather_dir(float2 *__restrict__ rows, const float2 *__restrict__ spec, const uint32_t *__restrict__ pos,
+                 const int4 *__restrict__ items, const float2 *__restrict__ dsincos,
+                 const int *__restrict__ ray_start, const uint32_t *__restrict__ rays,
+                 const float2 *__restrict__ kmat, const float2 *__restrict__ shiftf, UsGeo g, int zb, int jbase,
+                 int accumulate, int *__restrict__ err) {
+    extern __shared__ __align__(16) unsigned char dir_fwd_smem[];
+    FwdSmem &sm = *reinterpret_cast<FwdSmem *>(dir_fwd_smem);
+    const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+    const int4 it = items[blockIdx.x];
+    const int z0 = blockIdx.y * g.zper, z1 = min(zb, z0 + g.zper);
+    const int tyi = it.x / g.NT, txi = it.x - tyi * g.NT;
+    const int cnt = min(it.z, kFCap);
+    const bool mirrored = txi * kT > g.n + 2;
+    const int KY0 = tyi * kT - kR, KX0 = txi * kT - kR;  // footprint cell (0, 0) in the periodic spectrum
+
+    // ---- the item's positions (the same for every slice) ----
+    for (int e = tid; e < kFCap; e += kFThr) {
+        int id = -1, org = 0;
+        float wx[kTaps], wy[kTaps];
+#pragma unroll
+        for (int b = 0; b < kTaps; ++b) wx[b] = wy[b] = 0.f;
+        if (e < cnt) {
+            const uint32_t u = __ldg(pos + it.y + e);
+            const int d = u / (uint32_t)g.n, q = u - d * g.n;
+            float x0, y0;
+            int fx, fy;
+            sample_pos(q, __ldg(dsincos + d), g, x0, y0, fx, fy);
+            const int lx0 = g.n + fx - txi * kT, ly0 = g.n + fy - tyi * kT;
+            if (lx0 < 0 || lx0 >= kT || ly0 < 0 || ly0 >= kT) {  // host/device bin disagreement
+                atomicAdd(err, 1);
+            } else {
+                id = (int)u;
+                org = ly0 * kFW + lx0;
+                const float sgn = ((lx0 + ly0) & 1) ? -1.f : 1.f;
+#pragma unroll
+                for (int b = 0; b < kTaps; ++b) {
+                    const float a = tap_weight(fx, b, x0, g), c = tap_weight(fy, b, y0, g);
+                    wx[b] = (b & 1) ? -a : a;
+                    wy[b] = ((b & 1) ? -c : c) * sgn;
+                }
+            }
+        }
+        sm.pid[e] = id;
+        sm.org[e] = org;
+#pragma unroll
+        for (int b = 0; b < kTaps; ++b) {
+            sm.wx[e][b] = wx[b];
+            sm.wy[e][b] = wy[b];
+        }
+    }
+
+    const int ngroups = (cnt + 3) / 4;  // four positions per warp
+    const int pi = lane >> 3, ci = lane & 7;
+    const int j0 = jbase + 2 * ci;      // this lane's time samples j0, j0 + 1
+    for (int z = z0; z < z1; ++z) {
+        // ---- footprint of slice z: copy t -> (jh, row, colq, jj, cl), lanes = 4 cells x 8 time samples ----
+        const float2 *simg = spec + ((long long)z * g.m + jbase) * g.img_fwd;
+        for (int t = tid; t < kFill; t += kFThr) {
+            const int cl = t & 3, jj = (t >> 2) & 7;
+            int r = t >> 5;
+            const int colq = r % (kFW / 4);
+            r /= kFW / 4;
+            const int row = r % kFW, jh = r / kFW;
+            const int j = 8 * jh + jj, col = 4 * colq + cl;
+            const int cell = row * kFW + col;
+            float2 *dst = reinterpret_cast<float2 *>(&sm.fp[cell * kChunks]) + ((j + 4 * (cell & 3)) & 15);
+            if (jbase + j < g.m) {
+                const int KY = KY0 + row, KX = KX0 + col;
+                const int Y = (mirrored ? g.P - KY : KY) + kHalo, X = (mirrored ? g.P - KX : KX) + kHalo;
+                cp_async8(dst, simg + (long long)j * g.img_fwd + (long long)Y * g.qp + X);
+            } else {
+                *dst = make_float2(0.f, 0.f);
+            }
+        }
+        cp_commit();
+        cp_wait<0>();
+        __syncthreads();
+
+        for (int gi = wid; gi < ngroups; gi += kFThr / 32) {
+            const int e = 4 * gi + pi;
+            const int id = sm.pid[e];
+            const int org = sm.org[e];
+            const int lx0 = org % kFW;
+            const float4 *fb = sm.fp + org * kChunks;
+            int so[4];
+#pragma unroll
+            for (int bq = 0; bq < 4; ++bq) so[bq] = (ci + 2 * ((lx0 + bq) & 3)) & 7;
+            float wx[kTaps];
+#pragma unroll
+            for (int b = 0; b < kTaps; ++b) wx[b] = sm.wx[e][b];
+            // ---- S_j of this lane's two time samples: 81 taps ----
+            float2 s0 = make_float2(0.f, 0.f), s1 = make_float2(0.f, 0.f);
+#pragma unroll
+            for (int a = 0; a < kTaps; ++a) {
+                float2 r0 = make_float2(0.f, 0.f), r1 = make_float2(0.f, 0.f);
+#pragma unroll
+                for (int b = 0; b < kTaps; ++b) {
+                    const float4 f = fb[(a * kFW + b) * kChunks + so[b & 3]];
+                    r0 = ffma2(make_float2(wx[b], wx[b]), make_float2(f.x, f.y), r0);
+                    r1 = ffma2(make_float2(wx[b], wx[b]), make_float2(f.z, f.w), r1);
+                }
+                const float w = sm.wy[e][a];
+                s0 = ffma2(make_float2(w, w), r0, s0);
+                s1 = ffma2(make_float2(w, w), r1, s1);
+            }
+            if (mirrored) {  // the footprint held the conjugate-mirrored cells
+                s0.y = -s0.y;
+                s1.y = -s1.y;
+            }
+            // ---- rays of the position, eight per round ----
+            int q = 0, rs = 0, nr = 0;
+            if (id >= 0) {
+                const int d = id / g.n;
+                q = id - d * g.n;
+                rs = __ldg(ray_start + d);
+                nr = __ldg(ray_start + d + 1) - rs;
+            }
+            const int rounds = __reduce_max_sync(0xffffffffu, (nr + 7) >> 3);
+            for (int rd = 0; rd < rounds; ++rd) {
+                float v[16];
+#pragma unroll
+                for (int rr = 0; rr < 8; ++rr) {
+                    float2 k0 = make_float2(0.f, 0.f), k1 = make_float2(0.f, 0.f);
+                    if (8 * rd + rr < nr) {
+                        const long long th = __ldg(rays + rs + 8 * rd + rr) & 0x7fffffffu;
+                        if (j0 < g.m) k0 = __ldg(kmat + th * g.m + j0);
+                        if (j0 + 1 < g.m) k1 = __ldg(kmat + th * g.m + j0 + 1);
+                    }
+                    v[2 * rr] = k0.x * s0.x - k0.y * s0.y + k1.x * s1.x - k1.y * s1.y;
+                    v[2 * rr + 1] = k0.x * s0.y + k0.y * s0.x + k1.x * s1.y + k1.y * s1.x;
+                }
+                // sum over the eight lanes of the position by recursive halving;
+                // lane ci ends with ray 8 rd + ci
+                float w8[8], w4[4], w2[2];
+                const bool b4 = ci & 4, b2 = ci & 2, b1 = ci & 1;
+#pragma unroll
+                for (int t = 0; t < 8; ++t) {
+                    const float send = b4 ? v[t] : v[8 + t];
+                    const float keep = b4 ? v[8 + t] : v[t];
+                    w8[t] = keep + __shfl_xor_sync(0xffffffffu, send, 4);
+                }
+#pragma unroll
+                for (int t = 0; t < 4; ++t) {
+                    const float send = b2 ? w8[t] : w8[4 + t];
+                    const float keep = b2 ? w8[4 + t] : w8[t];
+                    w4[t] = keep + __shfl_xor_sync(0xffffffffu, send, 2);
+                }
+#pragma unroll
+                for (int t = 0; t < 2; ++t) {
+                    const float send = b1 ? w4[t] : w4[2 + t];
+                    const float keep = b1 ? w4[2 + t] : w4[t];
+                    w2[t] = keep + __shfl_xor_sync(0xffffffffu, send, 1);
+                }
+                const int ri = 8 * rd + ci;
+                if (ri < nr) {
+                    const uint32_t rv = __ldg(rays + rs + ri);
+                    const long long th = rv & 0x7fffffffu;
+                    const int k = (rv >> 31) ? g.n - q : q;
+                    const float2 sh = __ldg(shiftf + k);
+                    const float cf = (k & 1) ? g.cw : -g.cw;  // (-1)^(k+1) (pi/mu)/n
+                    float2 o = cmul(make_float2(w2[0], w2[1]), make_float2(sh.x * cf, sh.y * cf));
+                    float2 *dst = rows + ((long long)z * g.ntheta + th) * g.n + k;
+                    if (accumulate) {
+                        const float2 p = *dst;
+                        o.x += p.x;
+                        o.y += p.y;
+                    }
+                    *dst = o;
+                }
+            }
+        }
+        __syncthreads();  // the footprint buffer is refilled for the next slice
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Adjoint: persistent blocks of 512 threads, one per SM, take (tile, slice
+// pair) units round-robin (pairs fastest, so that blocks in flight share
+// their tiles' records in L2); each block half works on one slice, one thread
+// per cell of the 16x16 tile.  A tile's entries (positions whose stencil
+// touches it, direction-major) come in tables of at most 256 entries and 16
+// directions, with the geometry records of the per-ray scatter (x and y
+// weight rows over the tile, k_adj_records on the directions) and the rows of
+// each direction that cover each warp's two tile rows (k_adj_tabinfo); the
+// next table's records are copied (cp.async) while the current one is
+// processed.  Per table: E_j of every entry and slice (eight lanes per entry,
+// two time samples each, summed over the direction's rays in ray order), then
+// every cell adds w(p, c) E_j(p) of the entries covering its rows into its 16
+// time samples (FP32, entry order: reproducible).  The unit's sums go into
+// the Hermitian half planes of the C2R inverse as in k_scatter_tc.
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(kAThr, 1)
+    k_scatter_dir(const float2 *__restrict__ rowsc, float2 *__restrict__ spec, const AdjRec *__restrict__ recs,
+                  const int4 *__restrict__ items, const int4 *__restrict__ tabs, const int *__restrict__ tab_base,
+                  const uint32_t *__restrict__ info, const int *__restrict__ ray_start,
+                  const uint32_t *__restrict__ rays, const float2 *__restrict__ kmat,
+                  const float2 *__restrict__ shifta, UsGeo g, int zb, int npairs, int nunits, int jbase) {
+    extern __shared__ __align__(16) unsigned char dir_adj_smem[];
+    AdjSmem &sm = *reinterpret_cast<AdjSmem *>(dir_adj_smem);
+    const int P = g.P, hn = g.n / 2 + 1;
+    const int tid = threadIdx.x, wid = tid >> 5;
+    const int h = tid / kAHalf;          // slice 2 pair + h
+    const int ct = tid % kAHalf;         // cell (cx, cy)
+    const int hw = wid % (kAHalf / 32);  // warp of the half: tile rows 2 hw, 2 hw + 1
+    const int cx = ct % kT, cy = ct / kT;
+    const int ci = ct & 7;               // E phase: time samples jbase + 2 ci, + 1
+    const int j0 = jbase + 2 * ci;
+
+    // copy cursor: the next table (unit, table of the unit) in consumption order
+    int fu = blockIdx.x, ft = 0;
+    auto fetch = [&](int slot) {
+        if (fu < nunits) {
+            const int item = fu / npairs;
+            const int tb0 = __ldg(tab_base + item), tb1 = __ldg(tab_base + item + 1);
+            const int4 tb = __ldg(tabs + tb0 + ft);  // (first entry, count, word offset, words)
+            const int cnt = min(tb.y, kATab), nw = min(tb.w, kAInfo);
+            const char *rs = reinterpret_cast<const char *>(recs + tb.x);
+            char *rd = reinterpret_cast<char *>(sm.rec[slot]);
+            constexpr int kRecChunks = (int)(sizeof(AdjRec) / 16);
+            for (int c = tid; c < cnt * kRecChunks; c += kAThr) cp_async16(rd + 16 * c, rs + 16 * c);
+            const char *is = reinterpret_cast<const char *>(info + tb.z);
+            char *id = reinterpret_cast<char *>(sm.info[slot]);
+            for (int c = tid; c < nw / 4; c += kAThr) cp_async16(id + 16 * c, is + 16 * c);
+            if (++ft >= tb1 - tb0) {
+                ft = 0;
+                fu += gridDim.x;
+            }
+        }
+        cp_commit();
+    };
+    fetch(0);
+    int seq = 0;  // tables consumed: buffer seq & 1
+
+    for (int u = blockIdx.x; u < nunits; u += gridDim.x) {
+        const int item = u / npairs;
+        const int z = 2 * (u % npairs) + h;
+        const bool zok = z < zb;  // the last pair of an odd batch has one slice
+        const int4 it = __ldg(items + item);
+        const int tyi = it.x / g.NT, txi = it.x - tyi * g.NT;
+        float acc[32];  // F of this cell: 16 time samples x (re, im)
+#pragma unroll
+        for (int i = 0; i < 32; ++i) acc[i] = 0.f;
+        const int tb0 = __ldg(tab_base + item), tb1 = __ldg(tab_base + item + 1);
+        for (int ti = tb0; ti < tb1; ++ti) {
+            const int buf = seq & 1;
+            fetch(buf ^ 1);  // the next table: that buffer was released by the last barrier
+            cp_wait<1>();    // this table's copies (issued one table earlier)
+            __syncthreads();
+            const int cnt = min(__ldg(tabs + ti).y, kATab);
+            const AdjRec *rec = sm.rec[buf];
+            const uint32_t *inf = sm.info[buf];
+            const int nseg = min(min((int)inf[0], cnt), kAMaxSeg);
+
+            // ---- E_j of the table's entries for this half's slice ----
+            for (int e = ct >> 3; e < cnt; e += kAHalf / 8) {
+                const int d = (int)((unsigned)rec[e].thm >> 16), q = rec[e].k;
+                const int rs = __ldg(ray_start + d), re = __ldg(ray_start + d + 1);
+                float2 e0 = make_float2(0.f, 0.f), e1 = make_float2(0.f, 0.f);
+                for (int r = rs; r < re; ++r) {
+                    const uint32_t rv = __ldg(rays + r);
+                    const long long th = rv & 0x7fffffffu;
+                    const int k = (rv >> 31) ? g.n - q : q;
+                    float2 R = make_float2(0.f, 0.f);
+                    if (zok) R = __ldg(rowsc + ((long long)z * g.ntheta + th) * hn + (k <= g.n / 2 ? k : g.n - k));
+                    if (k > g.n / 2) R.y = -R.y;  // the other half of the real row's spectrum
+                    const float2 sh = __ldg(shifta + k);
+                    const float cf = (k & 1) ? g.cw : -g.cw;
+                    const float2 er = cmul(R, make_float2(sh.x * cf, sh.y * cf));
+                    float2 k0 = make_float2(0.f, 0.f), k1 = make_float2(0.f, 0.f);
+                    if (j0 < g.m) k0 = __ldg(kmat + th * g.m + j0);
+                    if (j0 + 1 < g.m) k1 = __ldg(kmat + th * g.m + j0 + 1);
+                    const float2 a = cmulc(k0, er), b = cmulc(k1, er);
+                    e0.x += a.x;
+                    e0.y += a.y;
+                    e1.x += b.x;
+                    e1.y += b.y;
+                }
+                sm.e[h][e][ci] = make_float4(e0.x, e0.y, e1.x, e1.y);
+            }
+            __syncthreads();
+
+            // ---- cell sums over the entries covering this warp's rows ----
+            for (int s = 0; s < nseg; ++s) {
+                const uint32_t lohi = inf[4 + 8 * s + hw];
+                const int e1 = min((int)(lohi >> 16), cnt);
+                for (int e = (int)(lohi & 0xffffu); e < e1; ++e) {
+                    const float w = rec[e].wx[cx] * rec[e].wy[cy];
+                    const float4 *E = sm.e[h][e];
+                    const float2 ww = make_float2(w, w);
+#pragma unroll
+                    for (int i = 0; i < kChunks; ++i) {
+                        const float4 f = E[i];
+                        const float2 a0 = ffma2(ww, make_float2(f.x, f.y), make_float2(acc[4 * i], acc[4 * i + 1]));
+                        const float2 a1 =
+                            ffma2(ww, make_float2(f.z, f.w), make_float2(acc[4 * i + 2], acc[4 * i + 3]));
+                        acc[4 * i] = a0.x;
+                        acc[4 * i + 1] = a0.y;
+                        acc[4 * i + 2] = a1.x;
+                        acc[4 * i + 3] = a1.y;
+                    }
+                }
+            }
+            __syncthreads();  // E, the records and the segmentation of this buffer are free
+            ++seq;
+        }
+        // ---- the adjoint only needs Re IFFT2(X) = C2R of the Hermitian part
+        // H(k) = (X(k) + conj X(-k)) / 2 on the half plane kx <= n: each cell adds
+        // X(k)/2 to H(k) and conj(X(k))/2 to H(-k) where they lie in the half
+        // plane (at most two adds per H cell, onto zeros: the sum does not depend
+        // on their order); the pre-IFFT fftshift sign is applied here ----
+        const int KY = tyi * kT + cy, KX = txi * kT + cx;
+        if (zok && KY < P && KX < P) {
+            const int half = P / 2, hp = g.hpitch;
+            const long long img_half = (long long)P * hp;
+            const float sg = ((KX + KY) & 1) ? -0.5f : 0.5f;
+            const bool here = KX <= half, mirror = KX >= half || KX == 0;
+            const long long o1 = (long long)KY * hp + KX;
+            const long long o2 = (long long)((P - KY) % P) * hp + (P - KX) % P;
+            float2 *dst = spec + ((long long)z * g.m + jbase) * img_half;
+#pragma unroll
+            for (int j = 0; j < 16; ++j) {
+                if (jbase + j >= g.m) break;
+                const float2 v = make_float2(sg * acc[2 * j], sg * acc[2 * j + 1]);
+                float2 *d = dst + (long long)j * img_half;
+                if (here) atomicAdd(d + o1, v);
+                if (mirror) atomicAdd(d + o2, make_float2(v.x, -v.y));
+            }
+        }
+    }
+    cp_wait<0>();  // the cursor's last (empty) group
+}
+
+void dir_prepare() {
+    CUDA_CHECK(cudaFuncSetAttribute(k_gather_dir, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(FwdSmem)));
+    CUDA_CHECK(cudaFuncSetAttribute(k_scatter_dir, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(AdjSmem)));
+}
+
+int dir_fwd_capacity() { return kFCap; }
+
+void launch_gather_dir(float2 *rows, const float2 *spec, int zb, const GeoDev &gd, const UsGeo &g, int jbase,
+                       int accumulate, cudaStream_t s) {
+    if (gd.n_dfwd_items == 0) return;
+    if (g.T != kT) throw Error(1, "tile size must be 16");
+    if (g.zper < 1) throw Error(1, "slices per block must be positive");
+    const dim3 gs(gd.n_dfwd_items, (zb + g.zper - 1) / g.zper);
+    k_gather_dir<<<gs, kFThr, sizeof(FwdSmem), s>>>(rows, spec, gd.dfwd_pos, gd.dfwd_items, gd.sincos, gd.dray_start,
+                                                     gd.drays, gd.kmat, gd.shiftfwd, g, zb, jbase, accumulate, gd.err);
+    LAUNCH_CHECK("k_gather_dir");
+}
+
+void launch_scatter_dir(const float2 *rowsc, float2 *spec, int zb, const GeoDev &gd, const UsGeo &g, int jbase,
+                        cudaStream_t s) {
+    if (g.T != kT) throw Error(1, "tile size must be 16");
+    if (!gd.adj_recs || !gd.adj_tabs || !gd.adj_info) throw Error(1, "adjoint direction tables missing");
+    const int npairs = (zb + 1) / 2;
+    const long long nunits = (long long)npairs * gd.n_adj_busy;
+    if (nunits == 0) return;
+    if (nunits > 2147483647LL) throw Error(1, "adjoint grid too large");
+    static int nsm = 0;
+    if (nsm == 0) {
+        int dev = 0;
+        CUDA_CHECK(cudaGetDevice(&dev));
+        CUDA_CHECK(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+    }
+    const int grid = (int)std::min<long long>(nunits, g.sc_grid > 0 ? g.sc_grid : nsm);
+    k_scatter_dir<<<grid, kAThr, sizeof(AdjSmem), s>>>(rowsc, spec, gd.adj_recs, gd.adj_items, gd.adj_tabs,
+                                                       gd.adj_tab_base, gd.adj_info, gd.dray_start, gd.drays,
+                                                       gd.kmat, gd.shiftadj, g, zb, npairs, (int)nunits, jbase);
+    LAUNCH_CHECK("k_scatter_dir");
+}
+
+}  // namespace rectv

@@ -48,7 +48,7 @@ using Clock = std::chrono::steady_clock;
 // tensor-core scatter (k_scatter_tc).  Chosen per (device, n, ntheta, m,
 // slices per launch) by timing the candidates on a set-up handle, cached for
 // the process.
-using TuneKey = std::tuple<int, int, int, int, int>;  // device, n, ntheta, m, zb
+using TuneKey = std::tuple<int, int, int, int, int, int>;  // device, n, ntheta, m, zb, direction path
 std::mutex g_tune_mu;
 std::map<TuneKey, Tune> g_tune_cache;
 
@@ -87,7 +87,7 @@ double time_kernel(Handle &h, int which, int reps) {
 // decides which tensor-core kernels run), applies them (dropping captured
 // graphs) and returns them.  Cached per (device, n, ntheta, m, zb).
 Tune autotune(Handle &h, bool force) {
-    const TuneKey key{h.device, h.n, h.ntheta, h.m, h.zb};
+    const TuneKey key{h.device, h.n, h.ntheta, h.m, h.zb, h.gd.dirs ? 1 : 0};
     if (!force) {
         std::lock_guard<std::mutex> lk(g_tune_mu);
         auto it = g_tune_cache.find(key);
@@ -100,7 +100,7 @@ Tune autotune(Handle &h, bool force) {
     }
     Tune best;
     const int reps = 2;
-    if (h.gd.n_fwd_tc_items > 0) {
+    if (h.gd.n_fwd_tc_items > 0 || h.gd.n_dfwd_items > 0) {  // slices per block of either gather
         double tbest = 1e30;
         for (int zper : {64, 32, 16, 8}) {
             if (zper > 8 && zper >= 2 * h.zb) continue;  // one block covers the batch already

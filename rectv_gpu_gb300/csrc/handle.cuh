@@ -191,6 +191,7 @@ struct Handle {
     // key of the geometry on the device (set_geometry)
     bool geo_valid = false, geo_has_phi = false, geo_tc_scatter = false;
     float geo_center = 0.f, geo_tc_spr = 0.f;
+    double geo_dir_min = 0.0, geo_dir_tol = 0.0;
     std::vector<float> geo_theta, geo_phi;
     // key of the captured graphs besides the geometry (setup)
     int graph_titer = -1;
@@ -253,6 +254,7 @@ struct Handle {
         usfft_prepare();
         gather_tc_prepare();
         scatter_tc_prepare();
+        dir_prepare();
         pad_fft_prepare();
         const int P = 2 * n;
         ug.n = n;
@@ -503,14 +505,38 @@ struct Handle {
         // adjoint: tensor-core time-sample mixing (k_scatter_tc) as fixed by
         // the layout at creation
         const bool tc_scatter = lay.tc_scatter;
+        // direction path (dir_kernels.cu): rays that revisit a direction over
+        // several half-turns share its sample positions, so the USFFT
+        // interpolates once per position.  Used when the rays average at least
+        // 2.5 per direction (RECTV_DIRS=1: whenever it can run, RECTV_DIRS=0:
+        // never) and the adjoint fills Hermitian half planes; rays are grouped
+        // when their samples agree within RECTV_DIR_TOL grid cells (2e-3).
+        double dir_min = 2.5, dir_tol = 2e-3;
+        if (const char *e = std::getenv("RECTV_DIRS")) {
+            if (!std::strcmp(e, "0")) dir_min = -1.0;
+            if (!std::strcmp(e, "1")) dir_min = 1.0;
+        }
+        if (const char *e = std::getenv("RECTV_DIR_TOL")) dir_tol = std::max(0.0, std::atof(e));
+        if (!tc_scatter) dir_min = -1.0;
         const size_t nphi = phi_h ? (size_t)2 * m * ntheta : 0;
         if (geo_valid && center == geo_center && tc_min_spr == geo_tc_spr && tc_scatter == geo_tc_scatter &&
+            dir_min == geo_dir_min && dir_tol == geo_dir_tol &&
             (phi_h != nullptr) == geo_has_phi && !std::memcmp(theta_h, geo_theta.data(), sizeof(float) * ntheta) &&
             (!phi_h || !std::memcmp(phi_h, geo_phi.data(), sizeof(float) * nphi)))
             return false;
         drop_graphs();
         free_geo();
-        HostPlan hp = build_plan(theta_h, n, ntheta, ug.T, table_capacity(), 1 << 30, tc_min_spr);
+        DirPlan dplan;
+        const bool dirs =
+            dir_min > 0 && build_dir_plan(theta_h, n, ntheta, ug.T, dir_fwd_capacity(), dir_tol, dir_min, dplan);
+        HostPlan hp;
+        if (dirs) {  // per-direction sincos and adjoint entries; no per-ray items
+            hp.sincos = dplan.sincos;
+            hp.adj_pts = std::move(dplan.adj_pos);
+            hp.adj_items = std::move(dplan.adj_items);
+        } else {
+            hp = build_plan(theta_h, n, ntheta, ug.T, table_capacity(), 1 << 30, tc_min_spr);
+        }
         auto up = [&](const void *src, size_t bytes) -> void * {
             void *p = nullptr;
             CUDA_CHECK(cudaMallocAsync(&p, std::max<size_t>(bytes, 16), stream));
@@ -533,6 +559,15 @@ struct Handle {
         gd.split_tiles = (int *)up(hp.split_tiles.data(), hp.split_tiles.size() * 4);
         gd.n_split_tiles = (int)hp.split_tiles.size();
         gd.tc_scatter = tc_scatter;
+        if (dirs) {
+            gd.dirs = true;
+            gd.ndir = dplan.ndir;
+            gd.dray_start = (int *)up(dplan.ray_start.data(), dplan.ray_start.size() * sizeof(int));
+            gd.drays = (uint32_t *)up(dplan.rays.data(), dplan.rays.size() * 4);
+            gd.dfwd_pos = (uint32_t *)up(dplan.fwd_pos.data(), dplan.fwd_pos.size() * 4);
+            gd.dfwd_items = (int4 *)up(dplan.fwd_items.data(), dplan.fwd_items.size() * sizeof(int4));
+            gd.n_dfwd_items = (int)dplan.fwd_items.size();
+        }
         std::vector<int> tab_base(1, 0);  // uploaded asynchronously: kept until the stream sync below
         std::vector<int4> tabs;
         if (tc_scatter) {
@@ -633,6 +668,8 @@ struct Handle {
         geo_center = center;
         geo_tc_spr = tc_min_spr;
         geo_tc_scatter = tc_scatter;
+        geo_dir_min = dir_min;
+        geo_dir_tol = dir_tol;
         geo_valid = true;
         return true;
     }
@@ -1027,7 +1064,8 @@ struct Handle {
         // samples) and the direct one (items with few samples per ray), then the
         // fused residual rows or the forward epilogue
         const int gather_k =
-            1 + ng * (((m >= 8 && gd.n_fwd_tc_items > 0) ? 1 : 0) + (gd.n_fwd_items > 0 ? 1 : 0));
+            1 + ng * (gd.dirs ? (gd.n_dfwd_items > 0 ? 1 : 0)
+                              : ((m >= 8 && gd.n_fwd_tc_items > 0) ? 1 : 0) + (gd.n_fwd_items > 0 ? 1 : 0));
         const int fwd_k = (pad_fft ? 2 : 1) + 1 + gather_k + 1;
         const int fwd_f = (pad_fft ? 0 : f2) + (fused_rows ? 0 : 1);
         // adjoint: [row preparation], the zeroing of split tiles (direct scatter),

@@ -200,4 +200,119 @@ HostPlan build_plan(const float *theta, int n, int ntheta, int T, int fwd_cap, i
     return p;
 }
 
+// Directions of a scan over several half-turns.  Ray theta samples the line
+// through the origin in direction (sin theta, cos theta); sample k sits at
+// (k-n/2)/n times that vector, so rays theta and theta + pi (and theta + 2 pi)
+// sample the same points: sample k of the opposite ray is sample n-k of the
+// other.  Rays whose directions agree within tol_cells / n radians (their
+// samples then lie within tol_cells grid cells of each other) share the
+// positions of one representative ray, the group member of median angle.
+bool build_dir_plan(const float *theta, int n, int ntheta, int T, int fwd_cap, double tol_cells, double min_group,
+                    DirPlan &dp) {
+    dp = DirPlan();
+    const double pi = 3.14159265358979323846;
+    const double tol = tol_cells / (double)n;
+    std::vector<double> alpha(ntheta);
+    std::vector<float2> sc(ntheta);
+    std::vector<uint32_t> opp(ntheta);
+    for (int th = 0; th < ntheta; ++th) {
+        const double t = (double)theta[th];
+        float s = (float)std::sin(t), c = (float)std::cos(t);
+        uint32_t o = (s < 0.f || (s == 0.f && c < 0.f)) ? 1u : 0u;
+        if (o) {
+            s = -s;
+            c = -c;
+        }
+        double a = std::atan2((double)s, (double)c);  // [0, pi]
+        if (a > pi - tol) {                           // the same line as a - pi, reversed
+            a -= pi;
+            s = -s;
+            c = -c;
+            o ^= 1u;
+        }
+        alpha[th] = a;
+        sc[th] = make_float2(s, c);
+        opp[th] = o;
+    }
+    std::vector<int> order(ntheta);
+    for (int i = 0; i < ntheta; ++i) order[i] = i;
+    std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return alpha[a] < alpha[b]; });
+    dp.ray_start.push_back(0);
+    for (int i = 0; i < ntheta;) {
+        int j = i + 1;
+        while (j < ntheta && alpha[order[j]] - alpha[order[i]] <= tol) ++j;
+        const int med = order[i + (j - i) / 2];  // member of median angle (order is sorted by angle)
+        std::sort(order.begin() + i, order.begin() + j);  // rays of a direction in theta order
+        dp.sincos.push_back(sc[med]);
+        for (int r = i; r < j; ++r) dp.rays.push_back((uint32_t)order[r] | (opp[order[r]] << 31));
+        dp.ray_start.push_back((int)dp.rays.size());
+        i = j;
+    }
+    dp.ndir = (int)dp.sincos.size();
+    if ((double)ntheta < min_group * dp.ndir || dp.ndir >= 65536) return false;
+
+    // positions (d, q), 1 <= q < n: the same float sequence as the kernels
+    // (sample_pos), binned by the tile of the stencil origin (forward) and by
+    // every tile the stencil touches (adjoint), direction-major inside a tile
+    const int P = 2 * n;
+    const int NT = (P + T - 1) / T;
+    const int ntiles = NT * NT;
+    const float tn = (float)(2 * n);
+    std::vector<float> qk(n);
+    for (int k = 1; k < n; ++k) qk[k] = (float)(k - n / 2) / (float)n;
+    const long long npos = (long long)dp.ndir * (n - 1);
+    std::vector<int> ftile(npos);
+    std::vector<int4> atiles(npos);
+    std::vector<long long> fcnt(ntiles + 1, 0), acnt(ntiles + 1, 0);
+    long long ip = 0;
+    for (int d = 0; d < dp.ndir; ++d) {
+        const float s = dp.sincos[d].x, c = dp.sincos[d].y;
+        for (int q = 1; q < n; ++q, ++ip) {
+            float x0 = qk[q] * s, y0 = qk[q] * c;
+            if (x0 >= 0.5f) x0 = 0.5f - 1e-5f;
+            if (y0 >= 0.5f) y0 = 0.5f - 1e-5f;
+            const int KX = n + (int)std::floor(tn * x0), KY = n + (int)std::floor(tn * y0);
+            ftile[ip] = (KY / T) * NT + (KX / T);
+            fcnt[ftile[ip]]++;
+            const int xa = wrapi(KX - kR, P) / T, xb = wrapi(KX + kR, P) / T;
+            const int ya = wrapi(KY - kR, P) / T, yb = wrapi(KY + kR, P) / T;
+            const int nx = (xa == xb) ? 1 : 2, ny = (ya == yb) ? 1 : 2;
+            const int xs[2] = {xa, xb}, ys[2] = {ya, yb};
+            int tl[4] = {-1, -1, -1, -1}, nt = 0;
+            for (int a = 0; a < ny; ++a)
+                for (int b = 0; b < nx; ++b) tl[nt++] = ys[a] * NT + xs[b];
+            atiles[ip] = make_int4(tl[0], tl[1], tl[2], tl[3]);
+            for (int i = 0; i < nt; ++i) acnt[tl[i]]++;
+        }
+    }
+    std::vector<long long> foff(ntiles + 1, 0), aoff(ntiles + 1, 0);
+    for (int t = 0; t < ntiles; ++t) {
+        foff[t + 1] = foff[t] + fcnt[t];
+        aoff[t + 1] = aoff[t] + acnt[t];
+    }
+    dp.fwd_pos.resize(foff[ntiles]);
+    dp.adj_pos.resize(aoff[ntiles]);
+    {
+        std::vector<long long> fp(foff.begin(), foff.end() - 1), ap(aoff.begin(), aoff.end() - 1);
+        ip = 0;
+        for (int d = 0; d < dp.ndir; ++d)
+            for (int q = 1; q < n; ++q, ++ip) {
+                const uint32_t id = (uint32_t)d * (uint32_t)n + (uint32_t)q;
+                dp.fwd_pos[fp[ftile[ip]]++] = id;
+                const int4 a = atiles[ip];
+                const int tl[4] = {a.x, a.y, a.z, a.w};
+                for (int i = 0; i < 4; ++i)
+                    if (tl[i] >= 0) dp.adj_pos[ap[tl[i]]++] = id;
+            }
+    }
+    for (int t = 0; t < ntiles; ++t)
+        for (long long i = foff[t]; i < foff[t + 1]; i += fwd_cap)
+            dp.fwd_items.push_back(make_int4(t, (int)i, (int)std::min<long long>(fwd_cap, foff[t + 1] - i), 0));
+    for (int t = 0; t < ntiles; ++t) dp.adj_items.push_back(make_int4(t, (int)aoff[t], (int)acnt[t], 0));
+    // heaviest tiles first (the empty ones last)
+    std::stable_sort(dp.adj_items.begin(), dp.adj_items.end(),
+                     [](const int4 &a, const int4 &b) { return a.z > b.z; });
+    return true;
+}
+
 }  // namespace rectv

@@ -458,6 +458,14 @@ int rectv_get_launch_counts(rectv_handle *h, int *kernels, int *fft_execs, int *
     });
 }
 
+int rectv_get_directions(rectv_handle *h, int *ndir, int *nrays) {
+    return rectv::guarded([&] {
+        rectv::Handle *H = live(h);
+        if (ndir) *ndir = H->gd.dirs ? H->gd.ndir : 0;
+        if (nrays) *nrays = H->ntheta;
+    });
+}
+
 }  // extern "C"
 
 // ===========================================================================

@@ -111,6 +111,16 @@ struct GeoDev {
     int *adj_tab_base = nullptr;
     uint32_t *adj_info = nullptr;
     int n_adj_tabs = 0;
+    // direction path (dir_kernels.cu, DirPlan): sincos then holds one
+    // (sin, cos) per direction, adj_pts / adj_items / adj_recs / adj_tabs the
+    // direction positions' adjoint entries (ray index := direction index)
+    bool dirs = false;
+    int ndir = 0;
+    int *dray_start = nullptr;    // [ndir + 1]
+    uint32_t *drays = nullptr;    // theta | opposite << 31
+    uint32_t *dfwd_pos = nullptr; // positions d*n + q sorted by origin tile
+    int4 *dfwd_items = nullptr;   // (tile, start, count, 0)
+    int n_dfwd_items = 0;
 };
 
 // Host-side angle plan (built in plan.cpp).
@@ -128,6 +138,31 @@ struct HostPlan {
 // an item with at least tc_min_spr samples per ray goes to the tensor-core
 // gather (tc_min_spr < 0: none does).
 HostPlan build_plan(const float *theta, int n, int ntheta, int T, int fwd_cap, int adj_cap, float tc_min_spr);
+
+// Rays grouped by direction (theta modulo pi), for scans that revisit their
+// angles over several half-turns: the rays of one direction sample the same
+// positions, so the USFFT interpolates once per position (dir_kernels.cu).
+struct DirPlan {
+    int ndir = 0;
+    std::vector<float2> sincos;     // [ndir] (sin, cos) of each direction's representative ray
+    std::vector<int> ray_start;     // [ndir + 1]: rays of direction d are rays[ray_start[d] .. ray_start[d+1])
+    std::vector<uint32_t> rays;     // theta index | opposite << 31 (sample k of an opposite ray is position n - k)
+    std::vector<uint32_t> fwd_pos;  // positions d*n + q (1 <= q < n) sorted by the tile of the stencil origin
+    std::vector<int4> fwd_items;    // (tile, start, count, 0): at most fwd_cap positions of one tile
+    std::vector<uint32_t> adj_pos;  // one entry per tile a position's stencil touches
+    std::vector<int4> adj_items;    // (tile, start, count, 0), one per tile, busiest first
+};
+// Groups rays whose sample positions agree within tol_cells grid cells.
+// Returns false (plan unused) when the rays average fewer than min_group per
+// direction or there are 65536 directions or more.
+bool build_dir_plan(const float *theta, int n, int ntheta, int T, int fwd_cap, double tol_cells, double min_group,
+                    DirPlan &dp);
+
+// 32-bit words of an adjoint table's ray segmentation with nseg rays: [0]
+// nseg, [4 + 8 s + w] the table rows [lo, hi) of ray s that cover rows 2w,
+// 2w+1 of the tile (lo | hi << 16), then the first row of every ray and the
+// table size as 16-bit values; padded to 16 bytes.
+__host__ __device__ constexpr int adj_info_words(int nseg) { return (4 + 8 * nseg + (nseg + 2) / 2 + 3) & ~3; }
 
 // ---- USFFT kernel launchers (usfft_kernels.cu) ----
 void launch_deapod_pad(const float *u, float *spec, int nimg, const float *deapod, const UsGeo &g,
@@ -168,6 +203,16 @@ int scatter_tc_batch_rays();  // rays per tensor-core batch
 int scatter_tc_info_words(int nseg);
 // fill adj_info from the records (after launch_adj_records)
 void launch_adj_tabinfo(const GeoDev &gd, cudaStream_t s);
+// direction path (dir_kernels.cu): forward rows of all rays from the
+// positions' interpolated spectra (time samples [jbase, jbase + 16),
+// accumulated into rows when accumulate != 0), and the adjoint scatter into
+// the zeroed Hermitian half planes (as launch_scatter_tc)
+void launch_gather_dir(float2 *rows, const float2 *spec, int zb, const GeoDev &gd, const UsGeo &g, int jbase,
+                       int accumulate, cudaStream_t s);
+void launch_scatter_dir(const float2 *rowsc, float2 *spec, int zb, const GeoDev &gd, const UsGeo &g, int jbase,
+                        cudaStream_t s);
+void dir_prepare();           // kernel attributes; once, outside stream capture
+int dir_fwd_capacity();       // positions per forward item
 // hand-written 2D FFTs of the zero-padded grids (fft_kernels.cu), P = 2n a
 // power of two in [256, 2048]: forward = deapodise/pad/modulate + R2C into
 // the halo-padded spectra (halo not filled); inverse = C2R of the Hermitian

@@ -81,11 +81,9 @@ __device__ __forceinline__ int off32(int row, int kk) {
     return (row >> 3) * 256 + (kk >> 2) * 32 + (row & 7) * 4 + (kk & 3);
 }
 
-// 32-bit words of a table's ray segmentation: [0] nseg, [4 + 8 s + w] the
-// table rows [lo, hi) of ray s that cover rows 2w, 2w+1 of the tile (lo |
-// hi << 16; empty: lo = kTab, hi = 0), then the first row of every ray and
-// the table size as 16-bit values; padded to 16 bytes
-__host__ __device__ constexpr int info_words(int nseg) { return (4 + 8 * nseg + (nseg + 2) / 2 + 3) & ~3; }
+// 32-bit words of a table's ray segmentation (adj_info_words; an empty range
+// is lo = kTab, hi = 0)
+constexpr int info_words(int nseg) { return adj_info_words(nseg); }
 constexpr int kInfoMax = info_words(kTab);
 
 struct ScTcSmem {

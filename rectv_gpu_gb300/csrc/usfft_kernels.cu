@@ -360,6 +360,10 @@ void launch_gather_fwd(const float2 *spec, float2 *rows, int zb, const GeoDev &g
     k_zero_k0<<<(unsigned)((nrows + 255) / 256), 256, 0, s>>>(rows, nrows, g.n);
     LAUNCH_CHECK("k_zero_k0");
     if (g.T != 16) throw Error(1, "tile size must be 16");
+    if (gd.dirs) {  // rays grouped by direction: one interpolation per position (dir_kernels.cu)
+        for (int jb = 0; jb < g.m; jb += 16) launch_gather_dir(rows, spec, zb, gd, g, jb, jb > 0, s);
+        return;
+    }
     const int mp = mp_for(g.m);
     for (int jb = 0; jb < g.m; jb += 16) {
         const int acc = jb > 0;
@@ -642,6 +646,10 @@ static void scatter_adj_t(const float2 *rowsc, float2 *spec, int zb, const GeoDe
 void launch_scatter_adj(const float2 *rowsc, float2 *spec, int zb, const GeoDev &gd,
                         const UsGeo &g, cudaStream_t s) {
     if (g.T != 16) throw Error(1, "tile size must be 16");
+    if (gd.dirs) {  // rays grouped by direction, into the Hermitian half planes (dir_kernels.cu)
+        for (int jb = 0; jb < g.m; jb += 16) launch_scatter_dir(rowsc, spec, zb, gd, g, jb, s);
+        return;
+    }
     const int mp = mp_for(g.m);
     for (int jb = 0; jb < g.m; jb += 16) {
         // the tensor-core scatter fills the Hermitian half planes the spectra

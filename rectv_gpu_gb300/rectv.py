@@ -139,6 +139,13 @@ class rectv:
         _lib.check(_lib.load().rectv_op_set_geometry(self._h, _addr(theta_ptr), _addr(phi_ptr),
                                                      float(center)))
 
+    def directions(self):
+        """Number of ray directions whose rays share sample positions in the
+        current geometry (0: every ray is interpolated on its own)."""
+        nd, nr = ctypes.c_int(0), ctypes.c_int(0)
+        _lib.check(_lib.load().rectv_get_directions(self._h, ctypes.byref(nd), ctypes.byref(nr)))
+        return nd.value
+
     def op_radonapr(self, g_ptr, f_ptr, nslices, tau=1.0):
         _lib.check(_lib.load().rectv_op_radonapr(self._h, _addr(g_ptr), _addr(f_ptr), int(nslices),
                                                  float(tau)))

@@ -26,6 +26,17 @@ def env(lib_built, torch_cuda):
     return torch_cuda, rectv
 
 
+@pytest.fixture(params=["per_ray", "auto"])
+def usfft_path(request, monkeypatch):
+    """Both USFFT paths: per-ray kernels, and the default choice (rays of a
+    repeated direction share positions where they average 2.5 or more)."""
+    if request.param == "per_ray":
+        monkeypatch.setenv("RECTV_DIRS", "0")
+    else:
+        monkeypatch.delenv("RECTV_DIRS", raising=False)
+    return request.param
+
+
 def dev(torch, a):
     return torch.from_numpy(np.ascontiguousarray(a)).cuda()
 
@@ -54,7 +65,7 @@ def _geometry(n, ntheta, m, nrot, seed):
 
 
 @pytest.mark.parametrize("case", CASES)
-def test_radonapr_matches_oracle(env, case):
+def test_radonapr_matches_oracle(env, usfft_path, case):
     torch, rectv = env
     n, ntheta, m, nz, nzp, nrot, dc = case
     center = n / 2 + dc
@@ -75,7 +86,7 @@ def test_radonapr_matches_oracle(env, case):
 
 
 @pytest.mark.parametrize("case", CASES)
-def test_radonapradj_matches_oracle(env, case):
+def test_radonapradj_matches_oracle(env, usfft_path, case):
     torch, rectv = env
     n, ntheta, m, nz, nzp, nrot, dc = case
     center = n / 2 + dc

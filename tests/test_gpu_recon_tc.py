@@ -29,6 +29,12 @@ def rel(a, b):
     return float(np.linalg.norm(np.asarray(a, np.float64) - b) / max(np.linalg.norm(b), 1e-300))
 
 
+@pytest.fixture(autouse=True)
+def per_ray_path(monkeypatch):
+    """These cases revisit their directions; keep them on the per-ray tensor-core kernels."""
+    monkeypatch.setenv("RECTV_DIRS", "0")
+
+
 @pytest.fixture(scope="module")
 def Solver(lib_built, torch_cuda):
     from rectv_gpu_gb300 import Solver
