@@ -17,11 +17,24 @@
 //
 // with k = q for the rays of the representative's orientation and k = n - q
 // for the opposite ones, f(k) = (-1)^(k+1) shiftfwd(k) (pi/mu)/n and f'(k) the
-// same with shiftadj.  At 2880 angles over 8 half-turns there are 360
-// directions: one eighth of the taps of the per-ray kernels, and the [ntheta x
-// M] basis contraction becomes an 8-ray x 16-time-sample mix per position
-// (FP32 on the CUDA cores: 16 complex products per ray sample, against 1296
-// for the taps of the per-ray formulation).
+// same with shiftadj.
+//
+// The rays of a direction are grouped when their angles agree to the float32
+// resolution of the input angles (2e-3 grid cells at the spectrum's edge);
+// ray theta's own samples then lie delta = (q - n/2)/n tau_theta cells
+// across the direction from the shared positions (DirPlan::tau).  Both
+// kernels take that offset to first order: the forward interpolates S and
+// its derivative across the direction, S_perp = sum_taps dw/dperp F, and ray
+// theta reads S + delta S_perp; the adjoint scatters E and E_perp =
+// sum_theta delta conj K' f' e with the weights w and dw/dperp.  The error
+// left is O(delta^2) (the zeroth-order grouping alone errs by ~2e-4 relative
+// at n = 1024 on white-noise spectra).
+//
+// At 2880 angles over 8 half-turns there are 360 directions: one eighth of
+// the taps of the per-ray kernels, and the [ntheta x M] basis contraction
+// becomes an 8-ray x 16-time-sample mix per position (FP32 on the CUDA
+// cores: 16 complex products per ray sample, against 1296 for the taps of the
+// per-ray formulation).
 //
 // Both kernels take 16 time samples [jbase, jbase + 16) per launch.
 #include <cuda_runtime.h>
@@ -45,11 +58,16 @@ constexpr int kFThr = 256;
 constexpr int kFCap = 128;  // positions per forward item
 constexpr int kFill = 2 * kFW * (kFW / 4) * 32;  // 8-byte copies of one footprint (9216)
 
+constexpr int kWt = 5 * kTaps;  // weights per position (odd row pitch: the four positions of a warp on distinct banks)
+
 struct FwdSmem {
     float4 fp[kCells * kChunks];  // footprint of 16 time samples, cell-major; chunk i of cell c at
                                   // slot (i + 2 (c & 3)) & 7
-    float wx[kFCap][kTaps];       // (-1)^b w_b of the 9 x taps
-    float wy[kFCap][kTaps];       // (-1)^a w_a of the 9 y taps times the stencil origin's fftshift sign
+    // per position: [0,9) (-1)^b w_b of the x taps, [9,18) their derivatives
+    // along x, [18,27) (-1)^a w_a of the y taps times the stencil origin's
+    // fftshift sign, [27,36) those times cos, [36,45) minus sin times their
+    // derivatives along y (cos, sin of the direction): S_perp's row weights
+    float wt[kFCap][kWt];
     int org[kFCap];               // footprint cell of the stencil origin
     int pid[kFCap];               // d*n + q, -1: none
 };
@@ -65,6 +83,7 @@ struct AdjSmem {
     AdjRec rec[2][kATab];          // geometry records of this table and the next
     uint32_t info[2][kAInfo];      // their direction segmentation
     float4 e[2][kATab][kChunks];   // E_j of the table's entries, both slices of the pair
+    float4 ep[2][kATab][kChunks];  // E_perp_j
 };
 
 __device__ __forceinline__ uint32_t saddr(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
@@ -103,8 +122,8 @@ __global__ void __launch_bounds__(kFThr, 2)
     k_gather_dir(float2 *__restrict__ rows, const float2 *__restrict__ spec, const uint32_t *__restrict__ pos,
                  const int4 *__restrict__ items, const float2 *__restrict__ dsincos,
                  const int *__restrict__ ray_start, const uint32_t *__restrict__ rays,
-                 const float2 *__restrict__ kmat, const float2 *__restrict__ shiftf, UsGeo g, int zb, int jbase,
-                 int accumulate, int *__restrict__ err) {
+                 const float *__restrict__ tau, const float2 *__restrict__ kmat, const float2 *__restrict__ shiftf,
+                 UsGeo g, int zb, int jbase, int accumulate, int *__restrict__ err) {
     extern __shared__ __align__(16) unsigned char dir_fwd_smem[];
     FwdSmem &sm = *reinterpret_cast<FwdSmem *>(dir_fwd_smem);
     const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
@@ -116,17 +135,19 @@ __global__ void __launch_bounds__(kFThr, 2)
     const int KY0 = tyi * kT - kR, KX0 = txi * kT - kR;  // footprint cell (0, 0) in the periodic spectrum
 
     // ---- the item's positions (the same for every slice) ----
+    // derivative of a tap weight exp(-pi^2/mu d^2) along the position, per
+    // grid cell: c1 d w, c1 = 2 (pi^2/mu) / (2n)
+    const float c1 = 2.f * g.wexp / g.tn;
     for (int e = tid; e < kFCap; e += kFThr) {
         int id = -1, org = 0;
-        float wx[kTaps], wy[kTaps];
-#pragma unroll
-        for (int b = 0; b < kTaps; ++b) wx[b] = wy[b] = 0.f;
+        float *wt = sm.wt[e];
         if (e < cnt) {
             const uint32_t u = __ldg(pos + it.y + e);
             const int d = u / (uint32_t)g.n, q = u - d * g.n;
+            const float2 sc = __ldg(dsincos + d);
             float x0, y0;
             int fx, fy;
-            sample_pos(q, __ldg(dsincos + d), g, x0, y0, fx, fy);
+            sample_pos(q, sc, g, x0, y0, fx, fy);
             const int lx0 = g.n + fx - txi * kT, ly0 = g.n + fy - tyi * kT;
             if (lx0 < 0 || lx0 >= kT || ly0 < 0 || ly0 >= kT) {  // host/device bin disagreement
                 atomicAdd(err, 1);
@@ -136,19 +157,21 @@ __global__ void __launch_bounds__(kFThr, 2)
                 const float sgn = ((lx0 + ly0) & 1) ? -1.f : 1.f;
 #pragma unroll
                 for (int b = 0; b < kTaps; ++b) {
-                    const float a = tap_weight(fx, b, x0, g), c = tap_weight(fy, b, y0, g);
-                    wx[b] = (b & 1) ? -a : a;
-                    wy[b] = ((b & 1) ? -c : c) * sgn;
+                    const float dx = (float)(fx - kR + b) * g.inv2n - x0, dy = (float)(fy - kR + b) * g.inv2n - y0;
+                    const float a = tap_weight(fx, b, x0, g), c = tap_weight(fy, b, y0, g) * sgn;
+                    const float sb = (b & 1) ? -1.f : 1.f;
+                    wt[b] = sb * a;
+                    wt[kTaps + b] = sb * c1 * dx * a;
+                    wt[2 * kTaps + b] = sb * c;
+                    wt[3 * kTaps + b] = sb * c * sc.y;
+                    wt[4 * kTaps + b] = -sb * c1 * dy * c * sc.x;
                 }
             }
         }
+        if (id < 0)
+            for (int b = 0; b < kWt; ++b) wt[b] = 0.f;
         sm.pid[e] = id;
         sm.org[e] = org;
-#pragma unroll
-        for (int b = 0; b < kTaps; ++b) {
-            sm.wx[e][b] = wx[b];
-            sm.wy[e][b] = wy[b];
-        }
     }
 
     const int ngroups = (cnt + 3) / 4;  // four positions per warp
@@ -187,27 +210,39 @@ __global__ void __launch_bounds__(kFThr, 2)
             int so[4];
 #pragma unroll
             for (int bq = 0; bq < 4; ++bq) so[bq] = (ci + 2 * ((lx0 + bq) & 3)) & 7;
-            float wx[kTaps];
+            const float *wt = sm.wt[e];
+            float wx[kTaps], wxd[kTaps];
 #pragma unroll
-            for (int b = 0; b < kTaps; ++b) wx[b] = sm.wx[e][b];
-            // ---- S_j of this lane's two time samples: 81 taps ----
+            for (int b = 0; b < kTaps; ++b) {
+                wx[b] = wt[b];
+                wxd[b] = wt[kTaps + b];
+            }
+            // ---- S_j and S_perp_j of this lane's two time samples: 81 taps ----
             float2 s0 = make_float2(0.f, 0.f), s1 = make_float2(0.f, 0.f);
+            float2 p0 = make_float2(0.f, 0.f), p1 = make_float2(0.f, 0.f);
 #pragma unroll
             for (int a = 0; a < kTaps; ++a) {
                 float2 r0 = make_float2(0.f, 0.f), r1 = make_float2(0.f, 0.f);
+                float2 d0 = make_float2(0.f, 0.f), d1 = make_float2(0.f, 0.f);
 #pragma unroll
                 for (int b = 0; b < kTaps; ++b) {
                     const float4 f = fb[(a * kFW + b) * kChunks + so[b & 3]];
                     r0 = ffma2(make_float2(wx[b], wx[b]), make_float2(f.x, f.y), r0);
                     r1 = ffma2(make_float2(wx[b], wx[b]), make_float2(f.z, f.w), r1);
+                    d0 = ffma2(make_float2(wxd[b], wxd[b]), make_float2(f.x, f.y), d0);
+                    d1 = ffma2(make_float2(wxd[b], wxd[b]), make_float2(f.z, f.w), d1);
                 }
-                const float w = sm.wy[e][a];
+                const float w = wt[2 * kTaps + a], wc = wt[3 * kTaps + a], ws = wt[4 * kTaps + a];
                 s0 = ffma2(make_float2(w, w), r0, s0);
                 s1 = ffma2(make_float2(w, w), r1, s1);
+                p0 = ffma2(make_float2(wc, wc), d0, ffma2(make_float2(ws, ws), r0, p0));
+                p1 = ffma2(make_float2(wc, wc), d1, ffma2(make_float2(ws, ws), r1, p1));
             }
             if (mirrored) {  // the footprint held the conjugate-mirrored cells
                 s0.y = -s0.y;
                 s1.y = -s1.y;
+                p0.y = -p0.y;
+                p1.y = -p1.y;
             }
             // ---- rays of the position, eight per round ----
             int q = 0, rs = 0, nr = 0;
@@ -217,19 +252,24 @@ __global__ void __launch_bounds__(kFThr, 2)
                 rs = __ldg(ray_start + d);
                 nr = __ldg(ray_start + d + 1) - rs;
             }
+            const float qp = __fdiv_rn((float)(q - g.n / 2), (float)g.n);
             const int rounds = __reduce_max_sync(0xffffffffu, (nr + 7) >> 3);
             for (int rd = 0; rd < rounds; ++rd) {
                 float v[16];
 #pragma unroll
                 for (int rr = 0; rr < 8; ++rr) {
                     float2 k0 = make_float2(0.f, 0.f), k1 = make_float2(0.f, 0.f);
+                    float dl = 0.f;
                     if (8 * rd + rr < nr) {
                         const long long th = __ldg(rays + rs + 8 * rd + rr) & 0x7fffffffu;
+                        dl = qp * __ldg(tau + rs + 8 * rd + rr);  // this ray's offset across the direction
                         if (j0 < g.m) k0 = __ldg(kmat + th * g.m + j0);
                         if (j0 + 1 < g.m) k1 = __ldg(kmat + th * g.m + j0 + 1);
                     }
-                    v[2 * rr] = k0.x * s0.x - k0.y * s0.y + k1.x * s1.x - k1.y * s1.y;
-                    v[2 * rr + 1] = k0.x * s0.y + k0.y * s0.x + k1.x * s1.y + k1.y * s1.x;
+                    const float2 t0 = make_float2(fmaf(dl, p0.x, s0.x), fmaf(dl, p0.y, s0.y));
+                    const float2 t1 = make_float2(fmaf(dl, p1.x, s1.x), fmaf(dl, p1.y, s1.y));
+                    v[2 * rr] = k0.x * t0.x - k0.y * t0.y + k1.x * t1.x - k1.y * t1.y;
+                    v[2 * rr + 1] = k0.x * t0.y + k0.y * t0.x + k1.x * t1.y + k1.y * t1.x;
                 }
                 // sum over the eight lanes of the position by recursive halving;
                 // lane ci ends with ray 8 rd + ci
@@ -295,7 +335,8 @@ __global__ void __launch_bounds__(kAThr, 1)
     k_scatter_dir(const float2 *__restrict__ rowsc, float2 *__restrict__ spec, const AdjRec *__restrict__ recs,
                   const int4 *__restrict__ items, const int4 *__restrict__ tabs, const int *__restrict__ tab_base,
                   const uint32_t *__restrict__ info, const int *__restrict__ ray_start,
-                  const uint32_t *__restrict__ rays, const float2 *__restrict__ kmat,
+                  const uint32_t *__restrict__ rays, const float *__restrict__ tau,
+                  const float2 *__restrict__ dsincos, const float2 *__restrict__ kmat,
                   const float2 *__restrict__ shifta, UsGeo g, int zb, int npairs, int nunits, int jbase) {
     extern __shared__ __align__(16) unsigned char dir_adj_smem[];
     AdjSmem &sm = *reinterpret_cast<AdjSmem *>(dir_adj_smem);
@@ -307,6 +348,7 @@ __global__ void __launch_bounds__(kAThr, 1)
     const int cx = ct % kT, cy = ct / kT;
     const int ci = ct & 7;               // E phase: time samples jbase + 2 ci, + 1
     const int j0 = jbase + 2 * ci;
+    const float cb = 2.f * g.wexp / g.tn * g.inv2n;  // c1/(2n): B = cb (cos, -sin)
 
     // copy cursor: the next table (unit, table of the unit) in consumption order
     int fu = blockIdx.x, ft = 0;
@@ -357,7 +399,9 @@ __global__ void __launch_bounds__(kAThr, 1)
             for (int e = ct >> 3; e < cnt; e += kAHalf / 8) {
                 const int d = (int)((unsigned)rec[e].thm >> 16), q = rec[e].k;
                 const int rs = __ldg(ray_start + d), re = __ldg(ray_start + d + 1);
+                const float qp = __fdiv_rn((float)(q - g.n / 2), (float)g.n);
                 float2 e0 = make_float2(0.f, 0.f), e1 = make_float2(0.f, 0.f);
+                float2 f0 = make_float2(0.f, 0.f), f1 = make_float2(0.f, 0.f);
                 for (int r = rs; r < re; ++r) {
                     const uint32_t rv = __ldg(rays + r);
                     const long long th = rv & 0x7fffffffu;
@@ -372,29 +416,44 @@ __global__ void __launch_bounds__(kAThr, 1)
                     if (j0 < g.m) k0 = __ldg(kmat + th * g.m + j0);
                     if (j0 + 1 < g.m) k1 = __ldg(kmat + th * g.m + j0 + 1);
                     const float2 a = cmulc(k0, er), b = cmulc(k1, er);
+                    const float dl = qp * __ldg(tau + r);  // this ray's offset across the direction
                     e0.x += a.x;
                     e0.y += a.y;
                     e1.x += b.x;
                     e1.y += b.y;
+                    f0.x = fmaf(dl, a.x, f0.x);
+                    f0.y = fmaf(dl, a.y, f0.y);
+                    f1.x = fmaf(dl, b.x, f1.x);
+                    f1.y = fmaf(dl, b.y, f1.y);
                 }
                 sm.e[h][e][ci] = make_float4(e0.x, e0.y, e1.x, e1.y);
+                sm.ep[h][e][ci] = make_float4(f0.x, f0.y, f1.x, f1.y);
             }
             __syncthreads();
 
             // ---- cell sums over the entries covering this warp's rows ----
+            const uint16_t *segf = reinterpret_cast<const uint16_t *>(inf + 4 + 8 * nseg);  // direction starts
             for (int s = 0; s < nseg; ++s) {
                 const uint32_t lohi = inf[4 + 8 * s + hw];
                 const int e1 = min((int)(lohi >> 16), cnt);
-                for (int e = (int)(lohi & 0xffffu); e < e1; ++e) {
+                const int e0 = (int)(lohi & 0xffffu);
+                if (e0 >= e1) continue;
+                // first-order weight w (A_p + B . (cx, cy)), B across the direction
+                const float2 sc = __ldg(dsincos + ((unsigned)rec[min((int)segf[s], cnt - 1)].thm >> 16));
+                const float bxy = cb * (sc.y * (float)cx - sc.x * (float)cy);
+                for (int e = e0; e < e1; ++e) {
                     const float w = rec[e].wx[cx] * rec[e].wy[cy];
+                    const float wp = w * (rec[e].sf.x + bxy);
                     const float4 *E = sm.e[h][e];
-                    const float2 ww = make_float2(w, w);
+                    const float4 *Ep = sm.ep[h][e];
+                    const float2 ww = make_float2(w, w), pp = make_float2(wp, wp);
 #pragma unroll
                     for (int i = 0; i < kChunks; ++i) {
-                        const float4 f = E[i];
-                        const float2 a0 = ffma2(ww, make_float2(f.x, f.y), make_float2(acc[4 * i], acc[4 * i + 1]));
-                        const float2 a1 =
-                            ffma2(ww, make_float2(f.z, f.w), make_float2(acc[4 * i + 2], acc[4 * i + 3]));
+                        const float4 f = E[i], fp = Ep[i];
+                        float2 a0 = ffma2(ww, make_float2(f.x, f.y), make_float2(acc[4 * i], acc[4 * i + 1]));
+                        float2 a1 = ffma2(ww, make_float2(f.z, f.w), make_float2(acc[4 * i + 2], acc[4 * i + 3]));
+                        a0 = ffma2(pp, make_float2(fp.x, fp.y), a0);
+                        a1 = ffma2(pp, make_float2(fp.z, fp.w), a1);
                         acc[4 * i] = a0.x;
                         acc[4 * i + 1] = a0.y;
                         acc[4 * i + 2] = a1.x;
@@ -432,6 +491,59 @@ __global__ void __launch_bounds__(kAThr, 1)
     cp_wait<0>();  // the cursor's last (empty) group
 }
 
+// ---------------------------------------------------------------------------
+// Geometry records of the direction path's adjoint entries: those of
+// k_adj_records (scatter_tc.cu) for the direction's representative
+// positions, and in sf.x the constant A of the first-order weight: at tile
+// cell (cx, cy) the distance to the position along x is cx/(2n) + ax (and
+// likewise y), so cos dw/dx w_y - sin w_x dw/dy = w (A + B . (cx, cy)) with
+// A = c1 (cos ax - sin ay), B = c1/(2n) (cos, -sin), c1 = 2 (pi^2/mu)/(2n).
+// One block per work item, one thread per entry.
+// ---------------------------------------------------------------------------
+__global__ void k_adj_records_dir(AdjRec *__restrict__ recs, const uint32_t *__restrict__ pts,
+                                  const int4 *__restrict__ items, const float2 *__restrict__ dsincos, UsGeo g) {
+    const int4 it = items[blockIdx.x];
+    const int tyi = it.x / g.NT, txi = it.x - tyi * g.NT;
+    const int P = g.P, half = P / 2;
+    const float c1 = 2.f * g.wexp / g.tn;
+    for (int e = threadIdx.x; e < it.z; e += blockDim.x) {
+        const uint32_t id = pts[it.y + e];
+        const int d = id / (uint32_t)g.n;
+        const int q = id - d * g.n;
+        const float2 sc = dsincos[d];
+        float x0, y0;
+        int fx, fy;
+        sample_pos(q, sc, g, x0, y0, fx, fy);
+        int dx = g.n + fx - kR - txi * kT;
+        int dy = g.n + fy - kR - tyi * kT;
+        dx += (dx < -half) ? P : 0;
+        dx -= (dx > half) ? P : 0;
+        dy += (dy < -half) ? P : 0;
+        dy -= (dy > half) ? P : 0;
+        AdjRec r;
+        int mask = 0;
+#pragma unroll
+        for (int c = 0; c < kT; ++c) {
+            const int bx = c - dx, by = c - dy;
+            r.wx[c] = ((unsigned)bx < (unsigned)kTaps) ? tap_weight(fx, bx, x0, g) : 0.f;
+            const bool iny = (unsigned)by < (unsigned)kTaps;
+            r.wy[c] = iny ? tap_weight(fy, by, y0, g) : 0.f;
+            mask |= iny ? (1 << c) : 0;
+        }
+        r.thm = (d << 16) | mask;
+        r.k = q;
+        const float ax = (float)(fx - kR - dx) * g.inv2n - x0, ay = (float)(fy - kR - dy) * g.inv2n - y0;
+        r.sf = make_float2(c1 * (sc.y * ax - sc.x * ay), 0.f);
+        recs[(long long)it.y + e] = r;
+    }
+}
+
+void launch_adj_records_dir(AdjRec *recs, const GeoDev &gd, const UsGeo &g, cudaStream_t s) {
+    if (gd.n_adj_items == 0) return;
+    k_adj_records_dir<<<gd.n_adj_items, 256, 0, s>>>(recs, gd.adj_pts, gd.adj_items, gd.sincos, g);
+    LAUNCH_CHECK("k_adj_records_dir");
+}
+
 void dir_prepare() {
     CUDA_CHECK(cudaFuncSetAttribute(k_gather_dir, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(FwdSmem)));
     CUDA_CHECK(cudaFuncSetAttribute(k_scatter_dir, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(AdjSmem)));
@@ -446,7 +558,8 @@ void launch_gather_dir(float2 *rows, const float2 *spec, int zb, const GeoDev &g
     if (g.zper < 1) throw Error(1, "slices per block must be positive");
     const dim3 gs(gd.n_dfwd_items, (zb + g.zper - 1) / g.zper);
     k_gather_dir<<<gs, kFThr, sizeof(FwdSmem), s>>>(rows, spec, gd.dfwd_pos, gd.dfwd_items, gd.sincos, gd.dray_start,
-                                                     gd.drays, gd.kmat, gd.shiftfwd, g, zb, jbase, accumulate, gd.err);
+                                                     gd.drays, gd.dtau, gd.kmat, gd.shiftfwd, g, zb, jbase, accumulate,
+                                                     gd.err);
     LAUNCH_CHECK("k_gather_dir");
 }
 
@@ -467,7 +580,8 @@ void launch_scatter_dir(const float2 *rowsc, float2 *spec, int zb, const GeoDev 
     const int grid = (int)std::min<long long>(nunits, g.sc_grid > 0 ? g.sc_grid : nsm);
     k_scatter_dir<<<grid, kAThr, sizeof(AdjSmem), s>>>(rowsc, spec, gd.adj_recs, gd.adj_items, gd.adj_tabs,
                                                        gd.adj_tab_base, gd.adj_info, gd.dray_start, gd.drays,
-                                                       gd.kmat, gd.shiftadj, g, zb, npairs, (int)nunits, jbase);
+                                                       gd.dtau, gd.sincos, gd.kmat, gd.shiftadj, g, zb, npairs,
+                                                       (int)nunits, jbase);
     LAUNCH_CHECK("k_scatter_dir");
 }
 

@@ -564,6 +564,7 @@ struct Handle {
             gd.ndir = dplan.ndir;
             gd.dray_start = (int *)up(dplan.ray_start.data(), dplan.ray_start.size() * sizeof(int));
             gd.drays = (uint32_t *)up(dplan.rays.data(), dplan.rays.size() * 4);
+            gd.dtau = (float *)up(dplan.tau.data(), dplan.tau.size() * 4);
             gd.dfwd_pos = (uint32_t *)up(dplan.fwd_pos.data(), dplan.fwd_pos.size() * 4);
             gd.dfwd_items = (int4 *)up(dplan.fwd_items.data(), dplan.fwd_items.size() * sizeof(int4));
             gd.n_dfwd_items = (int)dplan.fwd_items.size();
@@ -658,7 +659,10 @@ struct Handle {
         }
         gd.deapod = (float *)up(dp.data(), n * sizeof(float));
         if (gd.tc_scatter) {
-            launch_adj_records(gd.adj_recs, gd, ug, stream);
+            if (gd.dirs)
+                launch_adj_records_dir(gd.adj_recs, gd, ug, stream);
+            else
+                launch_adj_records(gd.adj_recs, gd, ug, stream);
             launch_adj_tabinfo(gd, stream);
         }
         CUDA_CHECK(cudaStreamSynchronize(stream));  // host vectors go out of scope

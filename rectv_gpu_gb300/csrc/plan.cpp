@@ -206,7 +206,9 @@ HostPlan build_plan(const float *theta, int n, int ntheta, int T, int fwd_cap, i
 // sample the same points: sample k of the opposite ray is sample n-k of the
 // other.  Rays whose directions agree within tol_cells / n radians (their
 // samples then lie within tol_cells grid cells of each other) share the
-// positions of one representative ray, the group member of median angle.
+// positions of one representative ray, the group member of median angle; a
+// ray's own samples lie (q-n/2)/n * tau_r cells across the direction from the
+// shared positions (the kernels correct for it to first order).
 bool build_dir_plan(const float *theta, int n, int ntheta, int T, int fwd_cap, double tol_cells, double min_group,
                     DirPlan &dp) {
     dp = DirPlan();
@@ -244,7 +246,16 @@ bool build_dir_plan(const float *theta, int n, int ntheta, int T, int fwd_cap, d
         const int med = order[i + (j - i) / 2];  // member of median angle (order is sorted by angle)
         std::sort(order.begin() + i, order.begin() + j);  // rays of a direction in theta order
         dp.sincos.push_back(sc[med]);
-        for (int r = i; r < j; ++r) dp.rays.push_back((uint32_t)order[r] | (opp[order[r]] << 31));
+        const double sd = sc[med].x, cd = sc[med].y;
+        for (int r = i; r < j; ++r) {
+            const int th = order[r];
+            dp.rays.push_back((uint32_t)th | (opp[th] << 31));
+            // offset of the ray's samples across the direction, per unit of
+            // (q - n/2)/n, in grid cells: 2n (s_r c_d - c_r s_d) with the
+            // ray's exact (orientation-normalised) direction
+            const double t = (double)theta[th], sg = opp[th] ? -1.0 : 1.0;
+            dp.tau.push_back((float)(2.0 * n * (sg * std::sin(t) * cd - sg * std::cos(t) * sd)));
+        }
         dp.ray_start.push_back((int)dp.rays.size());
         i = j;
     }

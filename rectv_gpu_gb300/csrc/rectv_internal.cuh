@@ -118,6 +118,7 @@ struct GeoDev {
     int ndir = 0;
     int *dray_start = nullptr;    // [ndir + 1]
     uint32_t *drays = nullptr;    // theta | opposite << 31
+    float *dtau = nullptr;        // per ray: offset across the direction (DirPlan::tau)
     uint32_t *dfwd_pos = nullptr; // positions d*n + q sorted by origin tile
     int4 *dfwd_items = nullptr;   // (tile, start, count, 0)
     int n_dfwd_items = 0;
@@ -147,6 +148,8 @@ struct DirPlan {
     std::vector<float2> sincos;     // [ndir] (sin, cos) of each direction's representative ray
     std::vector<int> ray_start;     // [ndir + 1]: rays of direction d are rays[ray_start[d] .. ray_start[d+1])
     std::vector<uint32_t> rays;     // theta index | opposite << 31 (sample k of an opposite ray is position n - k)
+    std::vector<float> tau;         // per ray (order of rays): its samples' offset across the direction, in
+                                    // grid cells per unit of (q - n/2)/n
     std::vector<uint32_t> fwd_pos;  // positions d*n + q (1 <= q < n) sorted by the tile of the stencil origin
     std::vector<int4> fwd_items;    // (tile, start, count, 0): at most fwd_cap positions of one tile
     std::vector<uint32_t> adj_pos;  // one entry per tile a position's stencil touches
@@ -211,6 +214,11 @@ void launch_gather_dir(float2 *rows, const float2 *spec, int zb, const GeoDev &g
                        int accumulate, cudaStream_t s);
 void launch_scatter_dir(const float2 *rowsc, float2 *spec, int zb, const GeoDev &gd, const UsGeo &g, int jbase,
                         cudaStream_t s);
+// geometry records of the direction path's adjoint entries (as
+// launch_adj_records, with sf = (A, 0): the first-order weight of entry p at
+// tile cell (cx, cy) is w (A + B . (cx, cy)), B = c1/(2n) (cos, -sin) of the
+// direction, c1 = 2 pi^2/mu / (2n))
+void launch_adj_records_dir(AdjRec *recs, const GeoDev &gd, const UsGeo &g, cudaStream_t s);
 void dir_prepare();           // kernel attributes; once, outside stream capture
 int dir_fwd_capacity();       // positions per forward item
 // hand-written 2D FFTs of the zero-padded grids (fft_kernels.cu), P = 2n a
