@@ -56,7 +56,6 @@ constexpr int kChunks = 8;         // 16-byte chunks of a cell: time samples (2i
 // ---- forward ----
 constexpr int kFThr = 256;
 constexpr int kFCap = 128;  // positions per forward item
-constexpr int kFill = 2 * kFW * (kFW / 4) * 32;  // 8-byte copies of one footprint (9216)
 
 constexpr int kWt = 5 * kTaps;  // weights per position (odd row pitch: the four positions of a warp on distinct banks)
 
@@ -75,22 +74,20 @@ struct FwdSmem {
 // ---- adjoint ----
 constexpr int kAHalf = kT * kT;        // threads per slice: one per cell
 constexpr int kAThr = 2 * kAHalf;      // a slice pair per block
-constexpr int kATab = 256;             // entries per table (host table builder)
+constexpr int kATab = 128;             // entries per table (host table builder)
 constexpr int kAMaxSeg = 16;           // directions per table (host table builder)
 constexpr int kAInfo = adj_info_words(kAMaxSeg);
+constexpr int kMThr = 256;             // positions per k_adj_mix block
+constexpr int kMRays = 32;             // rays per staged chunk of k_adj_mix
 
 struct AdjSmem {
-    AdjRec rec[2][kATab];          // geometry records of this table and the next
-    uint32_t info[2][kAInfo];      // their direction segmentation
-    float4 e[2][kATab][kChunks];   // E_j of the table's entries, both slices of the pair
-    float4 ep[2][kATab][kChunks];  // E_perp_j
+    AdjRec rec[2][kATab];                  // geometry records of this table and the next
+    uint32_t info[2][kAInfo];              // their direction segmentation
+    float4 e[2][2][kATab][2 * kChunks];    // [buffer][slice][entry]: E_j in [0, 8), E_perp_j in [8, 16)
 };
 
 __device__ __forceinline__ uint32_t saddr(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
 
-__device__ __forceinline__ void cp_async8(void *dst, const void *src) {
-    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(saddr(dst)), "l"(src) : "memory");
-}
 __device__ __forceinline__ void cp_async16(void *dst, const void *src) {
     asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(saddr(dst)), "l"(src) : "memory");
 }
@@ -111,7 +108,7 @@ __device__ __forceinline__ float2 cmulc(float2 a, float2 b) {
 // Forward: one block (256 threads) per (work item, slices); an item is at
 // most 128 positions whose stencils start in one 16x16 tile of the
 // oversampled grid.  Per slice the tile's 24x24-cell footprint of 16 time
-// samples is copied (8-byte cp.async, cell-major) from the halo-padded
+// samples is copied (coalesced loads, cell-major stores) from the halo-padded
 // spectra (tiles right of the Nyquist column read the mirrored cells and
 // conjugate), then eight lanes per position (two time samples each) sum the
 // 81 taps, and mix the position's rays: each lane forms its two time
@@ -176,29 +173,43 @@ __global__ void __launch_bounds__(kFThr, 2)
 
     const int ngroups = (cnt + 3) / 4;  // four positions per warp
     const int pi = lane >> 3, ci = lane & 7;
+    const int fc = lane & 3, fj = lane >> 2;  // footprint copies: cell of four, time sample of eight
     const int j0 = jbase + 2 * ci;      // this lane's time samples j0, j0 + 1
     for (int z = z0; z < z1; ++z) {
-        // ---- footprint of slice z: copy t -> (jh, row, colq, jj, cl), lanes = 4 cells x 8 time samples ----
+        // ---- footprint of slice z: lane = (cell cl of four, time sample jj of
+        // eight), warp w copies rows w, w + 8, w + 16: a half-warp writes four
+        // cells x four time samples on distinct banks, a warp reads eight
+        // 32-byte runs ----
+        // (all 36 loads of a thread in flight, then the stores)
         const float2 *simg = spec + ((long long)z * g.m + jbase) * g.img_fwd;
-        for (int t = tid; t < kFill; t += kFThr) {
-            const int cl = t & 3, jj = (t >> 2) & 7;
-            int r = t >> 5;
-            const int colq = r % (kFW / 4);
-            r /= kFW / 4;
-            const int row = r % kFW, jh = r / kFW;
-            const int j = 8 * jh + jj, col = 4 * colq + cl;
-            const int cell = row * kFW + col;
-            float2 *dst = reinterpret_cast<float2 *>(&sm.fp[cell * kChunks]) + ((j + 4 * (cell & 3)) & 15);
-            if (jbase + j < g.m) {
-                const int KY = KY0 + row, KX = KX0 + col;
-                const int Y = (mirrored ? g.P - KY : KY) + kHalo, X = (mirrored ? g.P - KX : KX) + kHalo;
-                cp_async8(dst, simg + (long long)j * g.img_fwd + (long long)Y * g.qp + X);
-            } else {
-                *dst = make_float2(0.f, 0.f);
+        float2 fv[2][kFW / 8][kFW / 4];
+#pragma unroll
+        for (int jh = 0; jh < 2; ++jh) {
+            const int j = 8 * jh + fj;
+            const float2 *sj = simg + (long long)j * g.img_fwd;
+#pragma unroll
+            for (int rr = 0; rr < kFW / 8; ++rr) {
+                const int KY = KY0 + wid + 8 * rr;
+                const float2 *srow = sj + (long long)((mirrored ? g.P - KY : KY) + kHalo) * g.qp;
+#pragma unroll
+                for (int cq = 0; cq < kFW / 4; ++cq) {
+                    const int KX = KX0 + 4 * cq + fc;
+                    fv[jh][rr][cq] = (jbase + j < g.m) ? __ldg(srow + (mirrored ? g.P - KX : KX) + kHalo)
+                                                       : make_float2(0.f, 0.f);
+                }
             }
         }
-        cp_commit();
-        cp_wait<0>();
+#pragma unroll
+        for (int jh = 0; jh < 2; ++jh) {
+            const int j = 8 * jh + fj;
+#pragma unroll
+            for (int rr = 0; rr < kFW / 8; ++rr) {
+                const int row = wid + 8 * rr;
+                float2 *drow = reinterpret_cast<float2 *>(sm.fp) + (row * kFW + fc) * 16 + ((j + 4 * fc) & 15);
+#pragma unroll
+                for (int cq = 0; cq < kFW / 4; ++cq) drow[64 * cq] = fv[jh][rr][cq];
+            }
+        }
         __syncthreads();
 
         for (int gi = wid; gi < ngroups; gi += kFThr / 32) {
@@ -255,14 +266,23 @@ __global__ void __launch_bounds__(kFThr, 2)
             const float qp = __fdiv_rn((float)(q - g.n / 2), (float)g.n);
             const int rounds = __reduce_max_sync(0xffffffffu, (nr + 7) >> 3);
             for (int rd = 0; rd < rounds; ++rd) {
+                // lane ci fetches ray 8 rd + ci of its position; the eight lanes share them by shuffles
+                uint32_t rv = 0;
+                float tv = 0.f;
+                if (8 * rd + ci < nr) {
+                    rv = __ldg(rays + rs + 8 * rd + ci);
+                    tv = __ldg(tau + rs + 8 * rd + ci);
+                }
                 float v[16];
 #pragma unroll
                 for (int rr = 0; rr < 8; ++rr) {
+                    const uint32_t rvr = __shfl_sync(0xffffffffu, rv, (lane & ~7) | rr);
+                    const float tvr = __shfl_sync(0xffffffffu, tv, (lane & ~7) | rr);
                     float2 k0 = make_float2(0.f, 0.f), k1 = make_float2(0.f, 0.f);
                     float dl = 0.f;
                     if (8 * rd + rr < nr) {
-                        const long long th = __ldg(rays + rs + 8 * rd + rr) & 0x7fffffffu;
-                        dl = qp * __ldg(tau + rs + 8 * rd + rr);  // this ray's offset across the direction
+                        const long long th = rvr & 0x7fffffffu;
+                        dl = qp * tvr;  // this ray's offset across the direction
                         if (j0 < g.m) k0 = __ldg(kmat + th * g.m + j0);
                         if (j0 + 1 < g.m) k1 = __ldg(kmat + th * g.m + j0 + 1);
                     }
@@ -295,7 +315,6 @@ __global__ void __launch_bounds__(kFThr, 2)
                 }
                 const int ri = 8 * rd + ci;
                 if (ri < nr) {
-                    const uint32_t rv = __ldg(rays + rs + ri);
                     const long long th = rv & 0x7fffffffu;
                     const int k = (rv >> 31) ? g.n - q : q;
                     const float2 sh = __ldg(shiftf + k);
@@ -316,45 +335,109 @@ __global__ void __launch_bounds__(kFThr, 2)
 }
 
 // ---------------------------------------------------------------------------
-// Adjoint: persistent blocks of 512 threads, one per SM, take (tile, slice
-// pair) units round-robin (pairs fastest, so that blocks in flight share
-// their tiles' records in L2); each block half works on one slice, one thread
-// per cell of the 16x16 tile.  A tile's entries (positions whose stencil
-// touches it, direction-major) come in tables of at most 256 entries and 16
-// directions, with the geometry records of the per-ray scatter (x and y
-// weight rows over the tile, k_adj_records on the directions) and the rows of
-// each direction that cover each warp's two tile rows (k_adj_tabinfo); the
-// next table's records are copied (cp.async) while the current one is
-// processed.  Per table: E_j of every entry and slice (eight lanes per entry,
-// two time samples each, summed over the direction's rays in ray order), then
-// every cell adds w(p, c) E_j(p) of the entries covering its rows into its 16
-// time samples (FP32, entry order: reproducible).  The unit's sums go into
+// Adjoint, step 1: E_j and E_perp_j of every position and slice (time
+// samples [jbase, jbase + 16)), once per position: one block per (direction,
+// slice, 256 positions), one thread per position; the direction's rays are
+// taken 32 at a time with their K' rows staged in shared memory, in ray
+// order.  Out: emix[((z ndir + d) n + q)] = 16 float4, E of time samples
+// (2i, 2i+1) in [i], E_perp in [8 + i].
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(kMThr)
+    k_adj_mix(float4 *__restrict__ emix, const float2 *__restrict__ rowsc, const int *__restrict__ ray_start,
+              const uint32_t *__restrict__ rays, const float *__restrict__ tau, const float2 *__restrict__ kmat,
+              const float2 *__restrict__ shifta, UsGeo g, int ndir, int jbase) {
+    __shared__ float2 ks[kMRays][16];
+    __shared__ uint32_t rvs[kMRays];
+    __shared__ float tvs[kMRays];
+    const int d = blockIdx.x, z = blockIdx.y;
+    const int q = blockIdx.z * kMThr + threadIdx.x;
+    const int hn = g.n / 2 + 1;
+    const int rs = __ldg(ray_start + d), nr = __ldg(ray_start + d + 1) - rs;
+    const float qp = __fdiv_rn((float)(q - g.n / 2), (float)g.n);
+    float2 e[16], ep[16];
+#pragma unroll
+    for (int j = 0; j < 16; ++j) e[j] = ep[j] = make_float2(0.f, 0.f);
+    for (int r0 = 0; r0 < nr; r0 += kMRays) {
+        const int nc = min(kMRays, nr - r0);
+        __syncthreads();  // the previous chunk's rows are consumed
+        for (int i = threadIdx.x; i < nc * 16; i += kMThr) {
+            const int r = i >> 4, j = i & 15;
+            const long long th = __ldg(rays + rs + r0 + r) & 0x7fffffffu;
+            ks[r][j] = (jbase + j < g.m) ? __ldg(kmat + th * g.m + jbase + j) : make_float2(0.f, 0.f);
+        }
+        for (int r = threadIdx.x; r < nc; r += kMThr) {
+            rvs[r] = __ldg(rays + rs + r0 + r);
+            tvs[r] = __ldg(tau + rs + r0 + r);
+        }
+        __syncthreads();
+        if (q >= 1 && q < g.n) {
+            for (int r = 0; r < nc; ++r) {
+                const uint32_t rv = rvs[r];
+                const long long th = rv & 0x7fffffffu;
+                const int k = (rv >> 31) ? g.n - q : q;
+                float2 R = __ldg(rowsc + ((long long)z * g.ntheta + th) * hn + (k <= g.n / 2 ? k : g.n - k));
+                if (k > g.n / 2) R.y = -R.y;  // the other half of the real row's spectrum
+                const float2 sh = __ldg(shifta + k);
+                const float cf = (k & 1) ? g.cw : -g.cw;  // (-1)^(k+1) (pi/mu)/n
+                const float2 er = cmul(R, make_float2(sh.x * cf, sh.y * cf));
+                const float dl = qp * tvs[r];  // this ray's offset across the direction
+#pragma unroll
+                for (int j = 0; j < 16; ++j) {
+                    const float2 a = cmulc(ks[r][j], er);
+                    e[j].x += a.x;
+                    e[j].y += a.y;
+                    ep[j].x = fmaf(dl, a.x, ep[j].x);
+                    ep[j].y = fmaf(dl, a.y, ep[j].y);
+                }
+            }
+        }
+    }
+    if (q >= 1 && q < g.n) {
+        float4 *o = emix + (((long long)z * ndir + d) * g.n + q) * 16;
+#pragma unroll
+        for (int i = 0; i < 8; ++i) {
+            o[i] = make_float4(e[2 * i].x, e[2 * i].y, e[2 * i + 1].x, e[2 * i + 1].y);
+            o[8 + i] = make_float4(ep[2 * i].x, ep[2 * i].y, ep[2 * i + 1].x, ep[2 * i + 1].y);
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Adjoint, step 2: persistent blocks of 512 threads, one per SM, take (tile,
+// slice pair) units round-robin (pairs fastest, so that blocks in flight
+// share their tiles' records in L2); each block half works on one slice, one
+// thread per cell of the 16x16 tile.  A tile's entries (positions whose
+// stencil touches it, direction-major) come in tables of at most 128 entries
+// and 16 directions, with the geometry records of the per-ray scatter (x and
+// y weight rows over the tile, k_adj_records_dir) and the rows of each
+// direction that cover each warp's two tile rows (k_adj_tabinfo); a table's
+// records, segmentation and the E, E_perp of its entries (both slices) are
+// copied (cp.async) while the table before it is processed.  Per table every
+// cell adds w E_j + w_perp E_perp_j of the entries covering its rows into its
+// 16 time samples (FP32, entry order: reproducible).  The unit's sums go into
 // the Hermitian half planes of the C2R inverse as in k_scatter_tc.
 // ---------------------------------------------------------------------------
 __global__ void __launch_bounds__(kAThr, 1)
-    k_scatter_dir(const float2 *__restrict__ rowsc, float2 *__restrict__ spec, const AdjRec *__restrict__ recs,
-                  const int4 *__restrict__ items, const int4 *__restrict__ tabs, const int *__restrict__ tab_base,
-                  const uint32_t *__restrict__ info, const int *__restrict__ ray_start,
-                  const uint32_t *__restrict__ rays, const float *__restrict__ tau,
-                  const float2 *__restrict__ dsincos, const float2 *__restrict__ kmat,
-                  const float2 *__restrict__ shifta, UsGeo g, int zb, int npairs, int nunits, int jbase) {
+    k_scatter_dir(const float4 *__restrict__ emix, float2 *__restrict__ spec, const AdjRec *__restrict__ recs,
+                  const uint32_t *__restrict__ pts, const int4 *__restrict__ items, const int4 *__restrict__ tabs,
+                  const int *__restrict__ tab_base, const uint32_t *__restrict__ info,
+                  const float2 *__restrict__ dsincos, UsGeo g, int ndir, int zb, int npairs, int nunits,
+                  int jbase) {
     extern __shared__ __align__(16) unsigned char dir_adj_smem[];
     AdjSmem &sm = *reinterpret_cast<AdjSmem *>(dir_adj_smem);
-    const int P = g.P, hn = g.n / 2 + 1;
+    const int P = g.P;
     const int tid = threadIdx.x, wid = tid >> 5;
     const int h = tid / kAHalf;          // slice 2 pair + h
     const int ct = tid % kAHalf;         // cell (cx, cy)
     const int hw = wid % (kAHalf / 32);  // warp of the half: tile rows 2 hw, 2 hw + 1
     const int cx = ct % kT, cy = ct / kT;
-    const int ci = ct & 7;               // E phase: time samples jbase + 2 ci, + 1
-    const int j0 = jbase + 2 * ci;
     const float cb = 2.f * g.wexp / g.tn * g.inv2n;  // c1/(2n): B = cb (cos, -sin)
 
     // copy cursor: the next table (unit, table of the unit) in consumption order
     int fu = blockIdx.x, ft = 0;
     auto fetch = [&](int slot) {
         if (fu < nunits) {
-            const int item = fu / npairs;
+            const int item = fu / npairs, z0 = 2 * (fu % npairs);
             const int tb0 = __ldg(tab_base + item), tb1 = __ldg(tab_base + item + 1);
             const int4 tb = __ldg(tabs + tb0 + ft);  // (first entry, count, word offset, words)
             const int cnt = min(tb.y, kATab), nw = min(tb.w, kAInfo);
@@ -365,6 +448,17 @@ __global__ void __launch_bounds__(kAThr, 1)
             const char *is = reinterpret_cast<const char *>(info + tb.z);
             char *id = reinterpret_cast<char *>(sm.info[slot]);
             for (int c = tid; c < nw / 4; c += kAThr) cp_async16(id + 16 * c, is + 16 * c);
+            // E, E_perp of entry e, slice z0 + hh: thread = (e, hh, half of the 16 chunks)
+            {
+                const int e = tid >> 2, hh = (tid >> 1) & 1, c0 = (tid & 1) * 8;
+                if (e < cnt && z0 + hh < zb) {
+                    const uint32_t pid = __ldg(pts + tb.x + e);  // d*n + q
+                    const float4 *src = emix + ((long long)(z0 + hh) * ndir * g.n + pid) * 16 + c0;
+                    float4 *dst = &sm.e[slot][hh][e][c0];
+#pragma unroll
+                    for (int c = 0; c < 8; ++c) cp_async16(dst + c, src + c);
+                }
+            }
             if (++ft >= tb1 - tb0) {
                 ft = 0;
                 fu += gridDim.x;
@@ -394,74 +488,38 @@ __global__ void __launch_bounds__(kAThr, 1)
             const AdjRec *rec = sm.rec[buf];
             const uint32_t *inf = sm.info[buf];
             const int nseg = min(min((int)inf[0], cnt), kAMaxSeg);
-
-            // ---- E_j of the table's entries for this half's slice ----
-            for (int e = ct >> 3; e < cnt; e += kAHalf / 8) {
-                const int d = (int)((unsigned)rec[e].thm >> 16), q = rec[e].k;
-                const int rs = __ldg(ray_start + d), re = __ldg(ray_start + d + 1);
-                const float qp = __fdiv_rn((float)(q - g.n / 2), (float)g.n);
-                float2 e0 = make_float2(0.f, 0.f), e1 = make_float2(0.f, 0.f);
-                float2 f0 = make_float2(0.f, 0.f), f1 = make_float2(0.f, 0.f);
-                for (int r = rs; r < re; ++r) {
-                    const uint32_t rv = __ldg(rays + r);
-                    const long long th = rv & 0x7fffffffu;
-                    const int k = (rv >> 31) ? g.n - q : q;
-                    float2 R = make_float2(0.f, 0.f);
-                    if (zok) R = __ldg(rowsc + ((long long)z * g.ntheta + th) * hn + (k <= g.n / 2 ? k : g.n - k));
-                    if (k > g.n / 2) R.y = -R.y;  // the other half of the real row's spectrum
-                    const float2 sh = __ldg(shifta + k);
-                    const float cf = (k & 1) ? g.cw : -g.cw;
-                    const float2 er = cmul(R, make_float2(sh.x * cf, sh.y * cf));
-                    float2 k0 = make_float2(0.f, 0.f), k1 = make_float2(0.f, 0.f);
-                    if (j0 < g.m) k0 = __ldg(kmat + th * g.m + j0);
-                    if (j0 + 1 < g.m) k1 = __ldg(kmat + th * g.m + j0 + 1);
-                    const float2 a = cmulc(k0, er), b = cmulc(k1, er);
-                    const float dl = qp * __ldg(tau + r);  // this ray's offset across the direction
-                    e0.x += a.x;
-                    e0.y += a.y;
-                    e1.x += b.x;
-                    e1.y += b.y;
-                    f0.x = fmaf(dl, a.x, f0.x);
-                    f0.y = fmaf(dl, a.y, f0.y);
-                    f1.x = fmaf(dl, b.x, f1.x);
-                    f1.y = fmaf(dl, b.y, f1.y);
-                }
-                sm.e[h][e][ci] = make_float4(e0.x, e0.y, e1.x, e1.y);
-                sm.ep[h][e][ci] = make_float4(f0.x, f0.y, f1.x, f1.y);
-            }
-            __syncthreads();
-
-            // ---- cell sums over the entries covering this warp's rows ----
-            const uint16_t *segf = reinterpret_cast<const uint16_t *>(inf + 4 + 8 * nseg);  // direction starts
-            for (int s = 0; s < nseg; ++s) {
-                const uint32_t lohi = inf[4 + 8 * s + hw];
-                const int e1 = min((int)(lohi >> 16), cnt);
-                const int e0 = (int)(lohi & 0xffffu);
-                if (e0 >= e1) continue;
-                // first-order weight w (A_p + B . (cx, cy)), B across the direction
-                const float2 sc = __ldg(dsincos + ((unsigned)rec[min((int)segf[s], cnt - 1)].thm >> 16));
-                const float bxy = cb * (sc.y * (float)cx - sc.x * (float)cy);
-                for (int e = e0; e < e1; ++e) {
-                    const float w = rec[e].wx[cx] * rec[e].wy[cy];
-                    const float wp = w * (rec[e].sf.x + bxy);
-                    const float4 *E = sm.e[h][e];
-                    const float4 *Ep = sm.ep[h][e];
-                    const float2 ww = make_float2(w, w), pp = make_float2(wp, wp);
+            if (zok) {
+                const uint16_t *segf = reinterpret_cast<const uint16_t *>(inf + 4 + 8 * nseg);  // direction starts
+                for (int s = 0; s < nseg; ++s) {
+                    const uint32_t lohi = inf[4 + 8 * s + hw];
+                    const int e1 = min((int)(lohi >> 16), cnt);
+                    const int e0 = (int)(lohi & 0xffffu);
+                    if (e0 >= e1) continue;
+                    // first-order weight w (A_p + B . (cx, cy)), B across the direction
+                    const float2 sc = __ldg(dsincos + ((unsigned)rec[min((int)segf[s], cnt - 1)].thm >> 16));
+                    const float bxy = cb * (sc.y * (float)cx - sc.x * (float)cy);
+                    for (int e = e0; e < e1; ++e) {
+                        const float w = rec[e].wx[cx] * rec[e].wy[cy];
+                        const float wp = w * (rec[e].sf.x + bxy);
+                        const float4 *E = sm.e[buf][h][e];
+                        const float2 ww = make_float2(w, w), pp = make_float2(wp, wp);
 #pragma unroll
-                    for (int i = 0; i < kChunks; ++i) {
-                        const float4 f = E[i], fp = Ep[i];
-                        float2 a0 = ffma2(ww, make_float2(f.x, f.y), make_float2(acc[4 * i], acc[4 * i + 1]));
-                        float2 a1 = ffma2(ww, make_float2(f.z, f.w), make_float2(acc[4 * i + 2], acc[4 * i + 3]));
-                        a0 = ffma2(pp, make_float2(fp.x, fp.y), a0);
-                        a1 = ffma2(pp, make_float2(fp.z, fp.w), a1);
-                        acc[4 * i] = a0.x;
-                        acc[4 * i + 1] = a0.y;
-                        acc[4 * i + 2] = a1.x;
-                        acc[4 * i + 3] = a1.y;
+                        for (int i = 0; i < kChunks; ++i) {
+                            const float4 f = E[i], fp = E[kChunks + i];
+                            float2 a0 = ffma2(ww, make_float2(f.x, f.y), make_float2(acc[4 * i], acc[4 * i + 1]));
+                            float2 a1 =
+                                ffma2(ww, make_float2(f.z, f.w), make_float2(acc[4 * i + 2], acc[4 * i + 3]));
+                            a0 = ffma2(pp, make_float2(fp.x, fp.y), a0);
+                            a1 = ffma2(pp, make_float2(fp.z, fp.w), a1);
+                            acc[4 * i] = a0.x;
+                            acc[4 * i + 1] = a0.y;
+                            acc[4 * i + 2] = a1.x;
+                            acc[4 * i + 3] = a1.y;
+                        }
                     }
                 }
             }
-            __syncthreads();  // E, the records and the segmentation of this buffer are free
+            __syncthreads();  // the records, segmentation and E of this buffer are free
             ++seq;
         }
         // ---- the adjoint only needs Re IFFT2(X) = C2R of the Hermitian part
@@ -550,6 +608,9 @@ void dir_prepare() {
 }
 
 int dir_fwd_capacity() { return kFCap; }
+int dir_adj_table_capacity() { return kATab; }
+int dir_adj_table_dirs() { return kAMaxSeg; }
+size_t dir_mix_bytes(int zb, int ndir, int n) { return (size_t)zb * ndir * n * 16 * sizeof(float4); }
 
 void launch_gather_dir(float2 *rows, const float2 *spec, int zb, const GeoDev &gd, const UsGeo &g, int jbase,
                        int accumulate, cudaStream_t s) {
@@ -566,11 +627,16 @@ void launch_gather_dir(float2 *rows, const float2 *spec, int zb, const GeoDev &g
 void launch_scatter_dir(const float2 *rowsc, float2 *spec, int zb, const GeoDev &gd, const UsGeo &g, int jbase,
                         cudaStream_t s) {
     if (g.T != kT) throw Error(1, "tile size must be 16");
-    if (!gd.adj_recs || !gd.adj_tabs || !gd.adj_info) throw Error(1, "adjoint direction tables missing");
+    if (!gd.adj_recs || !gd.adj_tabs || !gd.adj_info || !gd.demix) throw Error(1, "adjoint direction tables missing");
     const int npairs = (zb + 1) / 2;
     const long long nunits = (long long)npairs * gd.n_adj_busy;
     if (nunits == 0) return;
     if (nunits > 2147483647LL) throw Error(1, "adjoint grid too large");
+    if (zb > gd.demix_slices) throw Error(1, "adjoint direction mixing buffer too small");
+    const dim3 gm(gd.ndir, zb, (g.n + kMThr - 1) / kMThr);
+    k_adj_mix<<<gm, kMThr, 0, s>>>(gd.demix, rowsc, gd.dray_start, gd.drays, gd.dtau, gd.kmat, gd.shiftadj, g, gd.ndir,
+                                   jbase);
+    LAUNCH_CHECK("k_adj_mix");
     static int nsm = 0;
     if (nsm == 0) {
         int dev = 0;
@@ -578,10 +644,9 @@ void launch_scatter_dir(const float2 *rowsc, float2 *spec, int zb, const GeoDev 
         CUDA_CHECK(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
     }
     const int grid = (int)std::min<long long>(nunits, g.sc_grid > 0 ? g.sc_grid : nsm);
-    k_scatter_dir<<<grid, kAThr, sizeof(AdjSmem), s>>>(rowsc, spec, gd.adj_recs, gd.adj_items, gd.adj_tabs,
-                                                       gd.adj_tab_base, gd.adj_info, gd.dray_start, gd.drays,
-                                                       gd.dtau, gd.sincos, gd.kmat, gd.shiftadj, g, zb, npairs,
-                                                       (int)nunits, jbase);
+    k_scatter_dir<<<grid, kAThr, sizeof(AdjSmem), s>>>(gd.demix, spec, gd.adj_recs, gd.adj_pts, gd.adj_items,
+                                                       gd.adj_tabs, gd.adj_tab_base, gd.adj_info, gd.sincos, g,
+                                                       gd.ndir, zb, npairs, (int)nunits, jbase);
     LAUNCH_CHECK("k_scatter_dir");
 }
 

@@ -568,6 +568,15 @@ struct Handle {
             gd.dfwd_pos = (uint32_t *)up(dplan.fwd_pos.data(), dplan.fwd_pos.size() * 4);
             gd.dfwd_items = (int4 *)up(dplan.fwd_items.data(), dplan.fwd_items.size() * sizeof(int4));
             gd.n_dfwd_items = (int)dplan.fwd_items.size();
+            {  // the adjoint's E, E_perp per (slice, position) of one batch
+                const size_t bytes = dir_mix_bytes(zb, dplan.ndir, n);
+                void *p = nullptr;
+                CUDA_CHECK(cudaMallocAsync(&p, bytes, stream));
+                geo_owned.push_back(p);
+                geo_bytes += bytes;
+                gd.demix = (float4 *)p;
+                gd.demix_slices = zb;
+            }
         }
         std::vector<int> tab_base(1, 0);  // uploaded asynchronously: kept until the stream sync below
         std::vector<int4> tabs;
@@ -578,11 +587,12 @@ struct Handle {
             geo_bytes += std::max<size_t>(hp.adj_pts.size() * sizeof(AdjRec), 16);
             gd.adj_recs = (AdjRec *)p;
             // tables of the busy items and the size of their ray segmentation
-            const int cap = scatter_tc_table_capacity();
+            const int cap = dirs ? dir_adj_table_capacity() : scatter_tc_table_capacity();
             long long words = 0;
             // a table holds whole rays (runs of equal theta), at most one MMA
-            // batch of them (scatter_tc_batch_rays()) and at most cap entries
-            const int max_rays = scatter_tc_batch_rays();
+            // batch of them (scatter_tc_batch_rays()) and at most cap entries;
+            // on the direction path whole directions, at most dir_adj_table_dirs()
+            const int max_rays = dirs ? dir_adj_table_dirs() : scatter_tc_batch_rays();
             for (int i = 0; i < gd.n_adj_busy; ++i) {
                 const int4 it = hp.adj_items[i];
                 const uint32_t *pts = hp.adj_pts.data() + it.y;
@@ -1074,7 +1084,8 @@ struct Handle {
         const int fwd_f = (pad_fft ? 0 : f2) + (fused_rows ? 0 : 1);
         // adjoint: [row preparation], the zeroing of split tiles (direct scatter),
         // one scatter per group, then [columns + rows | crop]
-        const int adj_k = (fused_rows ? 0 : 1) + ((!gd.tc_scatter && gd.n_split_tiles > 0) ? 1 : 0) + ng +
+        const int adj_k = (fused_rows ? 0 : 1) + ((!gd.tc_scatter && gd.n_split_tiles > 0) ? 1 : 0) +
+                          ng * (gd.dirs ? 2 : 1) +
                           (own2d ? 2 : 1);
         const int adj_f = (fused_rows ? 0 : 1) + (own2d ? 0 : f2);
         // per outer iteration: titer inner steps per batch (forward, graddiv,

@@ -119,6 +119,8 @@ struct GeoDev {
     int *dray_start = nullptr;    // [ndir + 1]
     uint32_t *drays = nullptr;    // theta | opposite << 31
     float *dtau = nullptr;        // per ray: offset across the direction (DirPlan::tau)
+    float4 *demix = nullptr;      // adjoint E, E_perp per (slice, position): dir_mix_bytes(demix_slices, ndir, n)
+    int demix_slices = 0;
     uint32_t *dfwd_pos = nullptr; // positions d*n + q sorted by origin tile
     int4 *dfwd_items = nullptr;   // (tile, start, count, 0)
     int n_dfwd_items = 0;
@@ -221,6 +223,9 @@ void launch_scatter_dir(const float2 *rowsc, float2 *spec, int zb, const GeoDev 
 void launch_adj_records_dir(AdjRec *recs, const GeoDev &gd, const UsGeo &g, cudaStream_t s);
 void dir_prepare();           // kernel attributes; once, outside stream capture
 int dir_fwd_capacity();       // positions per forward item
+int dir_adj_table_capacity(); // entries per adjoint table
+int dir_adj_table_dirs();     // directions per adjoint table
+size_t dir_mix_bytes(int zb, int ndir, int n);  // the adjoint's per-position mixing buffer
 // hand-written 2D FFTs of the zero-padded grids (fft_kernels.cu), P = 2n a
 // power of two in [256, 2048]: forward = deapodise/pad/modulate + R2C into
 // the halo-padded spectra (halo not filled); inverse = C2R of the Hermitian
