@@ -54,14 +54,16 @@ constexpr int kCells = kFW * kFW;  // 576
 constexpr int kChunks = 8;         // 16-byte chunks of a cell: time samples (2i, 2i+1), complex
 
 // ---- forward ----
-constexpr int kFThr = 256;
+constexpr int kFCons = 8;                 // consumer warps: taps and rays
+constexpr int kFProd = 8;                 // producer warps: the next slice's footprint
+constexpr int kFThr = 32 * (kFCons + kFProd);
 constexpr int kFCap = 128;  // positions per forward item
 
 constexpr int kWt = 5 * kTaps;  // weights per position (odd row pitch: the four positions of a warp on distinct banks)
 
 struct FwdSmem {
-    float4 fp[kCells * kChunks];  // footprint of 16 time samples, cell-major; chunk i of cell c at
-                                  // slot (i + 2 (c & 3)) & 7
+    float4 fp[2][kCells * kChunks];  // footprints of 16 time samples (this slice and the next),
+                                     // cell-major; chunk i of cell c at slot (i + 2 (c & 3)) & 7
     // per position: [0,9) (-1)^b w_b of the x taps, [9,18) their derivatives
     // along x, [18,27) (-1)^a w_a of the y taps times the stencil origin's
     // fftshift sign, [27,36) those times cos, [36,45) minus sin times their
@@ -72,8 +74,7 @@ struct FwdSmem {
 };
 
 // ---- adjoint ----
-constexpr int kAHalf = kT * kT;        // threads per slice: one per cell
-constexpr int kAThr = 2 * kAHalf;      // a slice pair per block
+constexpr int kAThr = kT * kT;         // one thread per cell of a tile, one slice per block
 constexpr int kATab = 128;             // entries per table (host table builder)
 constexpr int kAMaxSeg = 16;           // directions per table (host table builder)
 constexpr int kAInfo = adj_info_words(kAMaxSeg);
@@ -83,7 +84,7 @@ constexpr int kMRays = 32;             // rays per staged chunk of k_adj_mix
 struct AdjSmem {
     AdjRec rec[2][kATab];                  // geometry records of this table and the next
     uint32_t info[2][kAInfo];              // their direction segmentation
-    float4 e[2][2][kATab][2 * kChunks];    // [buffer][slice][entry]: E_j in [0, 8), E_perp_j in [8, 16)
+    float4 e[2][kATab][2 * kChunks];       // [buffer][entry]: E_j in [0, 8), E_perp_j in [8, 16)
 };
 
 __device__ __forceinline__ uint32_t saddr(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
@@ -105,17 +106,19 @@ __device__ __forceinline__ float2 cmulc(float2 a, float2 b) {
 }  // namespace
 
 // ---------------------------------------------------------------------------
-// Forward: one block (256 threads) per (work item, slices); an item is at
-// most 128 positions whose stencils start in one 16x16 tile of the
-// oversampled grid.  Per slice the tile's 24x24-cell footprint of 16 time
-// samples is copied (coalesced loads, cell-major stores) from the halo-padded
-// spectra (tiles right of the Nyquist column read the mirrored cells and
-// conjugate), then eight lanes per position (two time samples each) sum the
-// 81 taps, and mix the position's rays: each lane forms its two time
-// samples' share of all eight rays of a round, the eight lanes add their
-// shares by recursive halving (14 shuffles) and lane i keeps ray i.
+// Forward: one block (512 threads, one per SM) per (work item, slices); an
+// item is at most 128 positions whose stencils start in one 16x16 tile of
+// the oversampled grid.  Eight producer warps copy the tile's 24x24-cell
+// footprint of 16 time samples of the next slice (coalesced loads,
+// cell-major stores into the second buffer) from the halo-padded spectra
+// (tiles right of the Nyquist column read the mirrored cells and conjugate)
+// while eight consumer warps work on this slice: eight lanes per position
+// (two time samples each) sum the 81 taps, then mix the position's rays:
+// each lane forms its two time samples' share of all eight rays of a round,
+// the eight lanes add their shares by recursive halving (14 shuffles) and
+// lane i keeps ray i.  One block barrier per slice.
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(kFThr, 2)
+__global__ void __launch_bounds__(kFThr, 1)
     k_gather_dir(float2 *__restrict__ rows, const float2 *__restrict__ spec, const uint32_t *__restrict__ pos,
                  const int4 *__restrict__ items, const float2 *__restrict__ dsincos,
                  const int *__restrict__ ray_start, const uint32_t *__restrict__ rays,
@@ -173,51 +176,55 @@ __global__ void __launch_bounds__(kFThr, 2)
 
     const int ngroups = (cnt + 3) / 4;  // four positions per warp
     const int pi = lane >> 3, ci = lane & 7;
-    const int fc = lane & 3, fj = lane >> 2;  // footprint copies: cell of four, time sample of eight
     const int j0 = jbase + 2 * ci;      // this lane's time samples j0, j0 + 1
-    for (int z = z0; z < z1; ++z) {
-        // ---- footprint of slice z: lane = (cell cl of four, time sample jj of
-        // eight), warp w copies rows w, w + 8, w + 16: a half-warp writes four
-        // cells x four time samples on distinct banks, a warp reads eight
-        // 32-byte runs ----
-        // (all 36 loads of a thread in flight, then the stores)
-        const float2 *simg = spec + ((long long)z * g.m + jbase) * g.img_fwd;
-        float2 fv[2][kFW / 8][kFW / 4];
+
+    // footprint of slice zz into buffer bf by producer warp pw: lane = (cell
+    // fc of four, time sample fj of eight), rows pw, pw + 8, pw + 16; a
+    // half-warp writes four cells x four time samples on distinct banks, a
+    // warp reads eight 32-byte runs; 18 loads in flight, then their stores
+    auto fill = [&](int zz, int bf, int pw) {
+        const int fc = lane & 3, fj = lane >> 2;
+        const float2 *simg = spec + ((long long)zz * g.m + jbase) * g.img_fwd;
 #pragma unroll
         for (int jh = 0; jh < 2; ++jh) {
             const int j = 8 * jh + fj;
             const float2 *sj = simg + (long long)j * g.img_fwd;
+            float2 fv[kFW / 8][kFW / 4];
 #pragma unroll
             for (int rr = 0; rr < kFW / 8; ++rr) {
-                const int KY = KY0 + wid + 8 * rr;
+                const int KY = KY0 + pw + 8 * rr;
                 const float2 *srow = sj + (long long)((mirrored ? g.P - KY : KY) + kHalo) * g.qp;
 #pragma unroll
                 for (int cq = 0; cq < kFW / 4; ++cq) {
                     const int KX = KX0 + 4 * cq + fc;
-                    fv[jh][rr][cq] = (jbase + j < g.m) ? __ldg(srow + (mirrored ? g.P - KX : KX) + kHalo)
-                                                       : make_float2(0.f, 0.f);
+                    fv[rr][cq] = (jbase + j < g.m) ? __ldg(srow + (mirrored ? g.P - KX : KX) + kHalo)
+                                                   : make_float2(0.f, 0.f);
                 }
             }
-        }
-#pragma unroll
-        for (int jh = 0; jh < 2; ++jh) {
-            const int j = 8 * jh + fj;
 #pragma unroll
             for (int rr = 0; rr < kFW / 8; ++rr) {
-                const int row = wid + 8 * rr;
-                float2 *drow = reinterpret_cast<float2 *>(sm.fp) + (row * kFW + fc) * 16 + ((j + 4 * fc) & 15);
+                const int row = pw + 8 * rr;
+                float2 *drow = reinterpret_cast<float2 *>(sm.fp[bf]) + (row * kFW + fc) * 16 + ((j + 4 * fc) & 15);
 #pragma unroll
-                for (int cq = 0; cq < kFW / 4; ++cq) drow[64 * cq] = fv[jh][rr][cq];
+                for (int cq = 0; cq < kFW / 4; ++cq) drow[64 * cq] = fv[rr][cq];
             }
         }
-        __syncthreads();
+    };
+    static_assert(kFProd == kFW / 3, "three footprint rows per producer warp");
+    if (wid >= kFCons && z0 < z1) fill(z0, 0, wid - kFCons);
+    __syncthreads();
 
-        for (int gi = wid; gi < ngroups; gi += kFThr / 32) {
+    for (int z = z0; z < z1; ++z) {
+        const int buf = (z - z0) & 1;
+        if (wid >= kFCons) {  // producers: the next slice
+            if (z + 1 < z1) fill(z + 1, buf ^ 1, wid - kFCons);
+        } else {
+        for (int gi = wid; gi < ngroups; gi += kFCons) {
             const int e = 4 * gi + pi;
             const int id = sm.pid[e];
             const int org = sm.org[e];
             const int lx0 = org % kFW;
-            const float4 *fb = sm.fp + org * kChunks;
+            const float4 *fb = sm.fp[buf] + org * kChunks;
             int so[4];
 #pragma unroll
             for (int bq = 0; bq < 4; ++bq) so[bq] = (ci + 2 * ((lx0 + bq) & 3)) & 7;
@@ -330,7 +337,8 @@ __global__ void __launch_bounds__(kFThr, 2)
                 }
             }
         }
-        __syncthreads();  // the footprint buffer is refilled for the next slice
+        }
+        __syncthreads();  // this buffer is refilled with slice z + 2, the next one is complete
     }
 }
 
@@ -403,41 +411,36 @@ __global__ void __launch_bounds__(kMThr)
 }
 
 // ---------------------------------------------------------------------------
-// Adjoint, step 2: persistent blocks of 512 threads, one per SM, take (tile,
-// slice pair) units round-robin (pairs fastest, so that blocks in flight
-// share their tiles' records in L2); each block half works on one slice, one
-// thread per cell of the 16x16 tile.  A tile's entries (positions whose
+// Adjoint, step 2: persistent blocks of 256 threads, two per SM, take (tile,
+// slice) units round-robin (slices fastest, so that blocks in flight share
+// their tiles' records in L2), one thread per cell of the 16x16 tile.  A tile's entries (positions whose
 // stencil touches it, direction-major) come in tables of at most 128 entries
 // and 16 directions, with the geometry records of the per-ray scatter (x and
 // y weight rows over the tile, k_adj_records_dir) and the rows of each
 // direction that cover each warp's two tile rows (k_adj_tabinfo); a table's
-// records, segmentation and the E, E_perp of its entries (both slices) are
-// copied (cp.async) while the table before it is processed.  Per table every
+// records, segmentation and the E, E_perp of its entries are copied
+// (cp.async) while the table before it is processed.  Per table every
 // cell adds w E_j + w_perp E_perp_j of the entries covering its rows into its
 // 16 time samples (FP32, entry order: reproducible).  The unit's sums go into
 // the Hermitian half planes of the C2R inverse as in k_scatter_tc.
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(kAThr, 1)
+__global__ void __launch_bounds__(kAThr, 2)
     k_scatter_dir(const float4 *__restrict__ emix, float2 *__restrict__ spec, const AdjRec *__restrict__ recs,
                   const uint32_t *__restrict__ pts, const int4 *__restrict__ items, const int4 *__restrict__ tabs,
                   const int *__restrict__ tab_base, const uint32_t *__restrict__ info,
-                  const float2 *__restrict__ dsincos, UsGeo g, int ndir, int zb, int npairs, int nunits,
-                  int jbase) {
+                  const float2 *__restrict__ dsincos, UsGeo g, int ndir, int zb, int nunits, int jbase) {
     extern __shared__ __align__(16) unsigned char dir_adj_smem[];
     AdjSmem &sm = *reinterpret_cast<AdjSmem *>(dir_adj_smem);
     const int P = g.P;
-    const int tid = threadIdx.x, wid = tid >> 5;
-    const int h = tid / kAHalf;          // slice 2 pair + h
-    const int ct = tid % kAHalf;         // cell (cx, cy)
-    const int hw = wid % (kAHalf / 32);  // warp of the half: tile rows 2 hw, 2 hw + 1
-    const int cx = ct % kT, cy = ct / kT;
+    const int tid = threadIdx.x, wid = tid >> 5;  // warp wid: tile rows 2 wid, 2 wid + 1
+    const int cx = tid % kT, cy = tid / kT;
     const float cb = 2.f * g.wexp / g.tn * g.inv2n;  // c1/(2n): B = cb (cos, -sin)
 
     // copy cursor: the next table (unit, table of the unit) in consumption order
     int fu = blockIdx.x, ft = 0;
     auto fetch = [&](int slot) {
         if (fu < nunits) {
-            const int item = fu / npairs, z0 = 2 * (fu % npairs);
+            const int item = fu / zb, zf = fu % zb;
             const int tb0 = __ldg(tab_base + item), tb1 = __ldg(tab_base + item + 1);
             const int4 tb = __ldg(tabs + tb0 + ft);  // (first entry, count, word offset, words)
             const int cnt = min(tb.y, kATab), nw = min(tb.w, kAInfo);
@@ -448,13 +451,13 @@ __global__ void __launch_bounds__(kAThr, 1)
             const char *is = reinterpret_cast<const char *>(info + tb.z);
             char *id = reinterpret_cast<char *>(sm.info[slot]);
             for (int c = tid; c < nw / 4; c += kAThr) cp_async16(id + 16 * c, is + 16 * c);
-            // E, E_perp of entry e, slice z0 + hh: thread = (e, hh, half of the 16 chunks)
+            // E, E_perp of entry e: thread = (e, half of the 16 chunks)
             {
-                const int e = tid >> 2, hh = (tid >> 1) & 1, c0 = (tid & 1) * 8;
-                if (e < cnt && z0 + hh < zb) {
+                const int e = tid >> 1, c0 = (tid & 1) * 8;
+                if (e < cnt) {
                     const uint32_t pid = __ldg(pts + tb.x + e);  // d*n + q
-                    const float4 *src = emix + ((long long)(z0 + hh) * ndir * g.n + pid) * 16 + c0;
-                    float4 *dst = &sm.e[slot][hh][e][c0];
+                    const float4 *src = emix + ((long long)zf * ndir * g.n + pid) * 16 + c0;
+                    float4 *dst = &sm.e[slot][e][c0];
 #pragma unroll
                     for (int c = 0; c < 8; ++c) cp_async16(dst + c, src + c);
                 }
@@ -470,9 +473,7 @@ __global__ void __launch_bounds__(kAThr, 1)
     int seq = 0;  // tables consumed: buffer seq & 1
 
     for (int u = blockIdx.x; u < nunits; u += gridDim.x) {
-        const int item = u / npairs;
-        const int z = 2 * (u % npairs) + h;
-        const bool zok = z < zb;  // the last pair of an odd batch has one slice
+        const int item = u / zb, z = u % zb;
         const int4 it = __ldg(items + item);
         const int tyi = it.x / g.NT, txi = it.x - tyi * g.NT;
         float acc[32];  // F of this cell: 16 time samples x (re, im)
@@ -488,10 +489,10 @@ __global__ void __launch_bounds__(kAThr, 1)
             const AdjRec *rec = sm.rec[buf];
             const uint32_t *inf = sm.info[buf];
             const int nseg = min(min((int)inf[0], cnt), kAMaxSeg);
-            if (zok) {
+            {
                 const uint16_t *segf = reinterpret_cast<const uint16_t *>(inf + 4 + 8 * nseg);  // direction starts
                 for (int s = 0; s < nseg; ++s) {
-                    const uint32_t lohi = inf[4 + 8 * s + hw];
+                    const uint32_t lohi = inf[4 + 8 * s + wid];
                     const int e1 = min((int)(lohi >> 16), cnt);
                     const int e0 = (int)(lohi & 0xffffu);
                     if (e0 >= e1) continue;
@@ -501,7 +502,7 @@ __global__ void __launch_bounds__(kAThr, 1)
                     for (int e = e0; e < e1; ++e) {
                         const float w = rec[e].wx[cx] * rec[e].wy[cy];
                         const float wp = w * (rec[e].sf.x + bxy);
-                        const float4 *E = sm.e[buf][h][e];
+                        const float4 *E = sm.e[buf][e];
                         const float2 ww = make_float2(w, w), pp = make_float2(wp, wp);
 #pragma unroll
                         for (int i = 0; i < kChunks; ++i) {
@@ -528,7 +529,7 @@ __global__ void __launch_bounds__(kAThr, 1)
         // plane (at most two adds per H cell, onto zeros: the sum does not depend
         // on their order); the pre-IFFT fftshift sign is applied here ----
         const int KY = tyi * kT + cy, KX = txi * kT + cx;
-        if (zok && KY < P && KX < P) {
+        if (KY < P && KX < P) {
             const int half = P / 2, hp = g.hpitch;
             const long long img_half = (long long)P * hp;
             const float sg = ((KX + KY) & 1) ? -0.5f : 0.5f;
@@ -628,8 +629,7 @@ void launch_scatter_dir(const float2 *rowsc, float2 *spec, int zb, const GeoDev 
                         cudaStream_t s) {
     if (g.T != kT) throw Error(1, "tile size must be 16");
     if (!gd.adj_recs || !gd.adj_tabs || !gd.adj_info || !gd.demix) throw Error(1, "adjoint direction tables missing");
-    const int npairs = (zb + 1) / 2;
-    const long long nunits = (long long)npairs * gd.n_adj_busy;
+    const long long nunits = (long long)zb * gd.n_adj_busy;
     if (nunits == 0) return;
     if (nunits > 2147483647LL) throw Error(1, "adjoint grid too large");
     if (zb > gd.demix_slices) throw Error(1, "adjoint direction mixing buffer too small");
@@ -643,10 +643,10 @@ void launch_scatter_dir(const float2 *rowsc, float2 *spec, int zb, const GeoDev 
         CUDA_CHECK(cudaGetDevice(&dev));
         CUDA_CHECK(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
     }
-    const int grid = (int)std::min<long long>(nunits, g.sc_grid > 0 ? g.sc_grid : nsm);
+    const int grid = (int)std::min<long long>(nunits, g.sc_grid > 0 ? g.sc_grid : 2 * nsm);
     k_scatter_dir<<<grid, kAThr, sizeof(AdjSmem), s>>>(gd.demix, spec, gd.adj_recs, gd.adj_pts, gd.adj_items,
                                                        gd.adj_tabs, gd.adj_tab_base, gd.adj_info, gd.sincos, g,
-                                                       gd.ndir, zb, npairs, (int)nunits, jbase);
+                                                       gd.ndir, zb, (int)nunits, jbase);
     LAUNCH_CHECK("k_scatter_dir");
 }
 

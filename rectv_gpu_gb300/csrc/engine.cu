@@ -117,8 +117,11 @@ Tune autotune(Handle &h, bool force) {
     if (h.gd.tc_scatter) {
         const int nsm = sm_count(h.device);
         double tbest = 1e30;
-        for (int frac : {4, 3, 2}) {  // nsm * frac / 4 persistent blocks
-            h.ug.sc_grid = nsm * frac / 4;
+        // persistent blocks: nsm * frac / 4 (tensor-core scatter, one block per
+        // SM at most), nsm * frac / 2 (direction scatter, two per SM at most)
+        const int per = h.gd.dirs ? 2 : 4;
+        for (int frac : {4, 3, 2}) {
+            h.ug.sc_grid = nsm * frac / per;
             const double t = time_kernel(h, 1, reps);
             if (t < tbest * 0.99) {
                 tbest = t;
@@ -126,7 +129,7 @@ Tune autotune(Handle &h, bool force) {
             }
         }
         best.scatter_ms = tbest;
-        if (best.sc_grid == nsm) best.sc_grid = 0;
+        if (best.sc_grid == nsm * 4 / per) best.sc_grid = 0;
         h.ug.sc_grid = best.sc_grid;
     }
     h.drop_graphs();
