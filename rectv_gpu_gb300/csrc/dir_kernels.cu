@@ -181,15 +181,15 @@ __global__ void __launch_bounds__(kFThr, 1)
     // footprint of slice zz into buffer bf by producer warp pw: lane = (cell
     // fc of four, time sample fj of eight), rows pw, pw + 8, pw + 16; a
     // half-warp writes four cells x four time samples on distinct banks, a
-    // warp reads eight 32-byte runs; 18 loads in flight, then their stores
+    // warp reads eight 32-byte runs; all 36 loads in flight, then the stores
     auto fill = [&](int zz, int bf, int pw) {
         const int fc = lane & 3, fj = lane >> 2;
         const float2 *simg = spec + ((long long)zz * g.m + jbase) * g.img_fwd;
+        float2 fv[2][kFW / 8][kFW / 4];
 #pragma unroll
         for (int jh = 0; jh < 2; ++jh) {
             const int j = 8 * jh + fj;
             const float2 *sj = simg + (long long)j * g.img_fwd;
-            float2 fv[kFW / 8][kFW / 4];
 #pragma unroll
             for (int rr = 0; rr < kFW / 8; ++rr) {
                 const int KY = KY0 + pw + 8 * rr;
@@ -197,16 +197,20 @@ __global__ void __launch_bounds__(kFThr, 1)
 #pragma unroll
                 for (int cq = 0; cq < kFW / 4; ++cq) {
                     const int KX = KX0 + 4 * cq + fc;
-                    fv[rr][cq] = (jbase + j < g.m) ? __ldg(srow + (mirrored ? g.P - KX : KX) + kHalo)
-                                                   : make_float2(0.f, 0.f);
+                    fv[jh][rr][cq] = (jbase + j < g.m) ? __ldg(srow + (mirrored ? g.P - KX : KX) + kHalo)
+                                                       : make_float2(0.f, 0.f);
                 }
             }
+        }
+#pragma unroll
+        for (int jh = 0; jh < 2; ++jh) {
+            const int j = 8 * jh + fj;
 #pragma unroll
             for (int rr = 0; rr < kFW / 8; ++rr) {
                 const int row = pw + 8 * rr;
                 float2 *drow = reinterpret_cast<float2 *>(sm.fp[bf]) + (row * kFW + fc) * 16 + ((j + 4 * fc) & 15);
 #pragma unroll
-                for (int cq = 0; cq < kFW / 4; ++cq) drow[64 * cq] = fv[rr][cq];
+                for (int cq = 0; cq < kFW / 4; ++cq) drow[64 * cq] = fv[jh][rr][cq];
             }
         }
     };
