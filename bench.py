@@ -38,12 +38,16 @@ os.environ.setdefault("CUDA_DEVICE_MAX_CONNECTIONS", "32")
 WORKLOAD = dict(n=1024, nz=64, nzp=16, ntheta=2880, nrot=8, m=16, titer=4, lambda0=1e-3, lambda1=4.0)
 SMALL = dict(n=256, nz=16, nzp=8, ntheta=720, nrot=8, m=16, titer=4, lambda0=1e-3, lambda1=4.0)
 METRIC = "ADMM iters/s (outer iterations, titer=4) of the 4D TV reconstruction"
-# launch groups timed by rectv_launch_kernel: 0 = forward gather (k_gather_tc, plus
-# k_gather_fwd for the few items near the centre of the spectrum), 1 = adjoint
-# scatter (k_scatter_tc), 2 = fused inner TV step, 3 = shrink / dual update,
-# 4 / 5 = forward / inverse padded-grid 2D FFT (when 2n is a power of two)
+# launch groups timed by rectv_launch_kernel: 0 = forward gather, 1 = adjoint
+# scatter, 2 = fused inner TV step, 3 = shrink / dual update, 4 / 5 = forward /
+# inverse padded-grid 2D FFT (when 2n is a power of two).  The USFFT kernels
+# depend on the geometry: scans that revisit their directions interpolate once
+# per position (k_gather_dir; k_adj_mix + k_scatter_dir), others per ray on
+# the tensor cores (k_gather_tc, plus k_gather_fwd for the few items near the
+# centre of the spectrum; k_scatter_tc).
 KERNEL_NAMES = {0: "k_gather_tc", 1: "k_scatter_tc", 2: "k_graddiv", 3: "k_shrink",
                 4: "k_fft_rows_fwd+k_fft_cols_fwd", 5: "k_fft_cols_inv+k_fft_rows_inv", 6: "k_graddiv (first step)"}
+KERNEL_NAMES_DIR = {**KERNEL_NAMES, 0: "k_gather_dir", 1: "k_adj_mix+k_scatter_dir"}
 
 
 def workload_of(args):
@@ -641,6 +645,8 @@ def run_ours(args, rank, world, local_rank):
 
     # ---- device-resident timed region ----
     obj.setup_device(d_g.data_ptr(), d_theta.data_ptr(), d_phi.data_ptr(), center, lam0, lam1, titer)
+    ndir = obj.directions()
+    names = KERNEL_NAMES_DIR if ndir > 0 else KERNEL_NAMES
     t_tune = time.perf_counter()
     tuned = obj.autotune()
     t_tune = time.perf_counter() - t_tune
@@ -696,6 +702,14 @@ def run_ours(args, rank, world, local_rank):
     peak, peak_kind = measured_peaks()
     achieved = bytes_.value / (ktimes[dom] * 1e-3) / 1e9
     limiter = {
+        "k_adj_mix+k_scatter_dir": "k_scatter_dir (93% of the pair): per-cell FP32 sums of w E + w_perp E_perp over "
+                                   "the entries covering each warp's two tile rows -- shared-memory broadcast loads "
+                                   "of E (L1/shared pipe ~73% busy) and the FMA pipe (~38%), two 8-warp blocks per SM "
+                                   "at 124 registers; float2 atomics into the Hermitian half planes; DRAM ~15% of "
+                                   "peak, so not DRAM-bound",
+        "k_gather_dir": "latency of the footprint loads and block barriers (two 8-warp blocks per SM at 124 "
+                        "registers, ~30 positions per tile and slice) and shared-memory bandwidth of the 81-tap "
+                        "reads (L1/shared pipe ~70% busy); DRAM ~14% of peak",
         "k_scatter_tc": "block barriers and the per-cell ray sums on the CUDA cores (shared-memory loads), "
                         "the tcgen05 time-sample GEMM (3xTF32) at ~14% of the tensor pipe; DRAM traffic 4.0x "
                         "the algorithmic bytes (float2 atomics read and write every Hermitian half-plane cell "
@@ -704,24 +718,50 @@ def run_ours(args, rank, world, local_rank):
                        "read-out of G, block barriers; TMA-staged footprints, DRAM traffic 3.0x the spectra "
                        "(overlapping footprints) at 8% of the DRAM peak",
         "k_graddiv": "HBM bandwidth", "k_shrink": "HBM bandwidth",
-        KERNEL_NAMES[4]: "HBM bandwidth", KERNEL_NAMES[5]: "HBM bandwidth"}[KERNEL_NAMES[dom]]
+        KERNEL_NAMES[4]: "HBM bandwidth", KERNEL_NAMES[5]: "HBM bandwidth"}[names[dom]]
     fma = ctypes.c_double()
     fma2 = ctypes.c_double()
     _lib.check(lib.rectv_measure_fp32_peak(ctypes.byref(fma), ctypes.byref(fma2)))
     fp32_rate = flops.value / (ktimes[dom] * 1e-3) / 1e12
-    roofline = {"bound": "hbm", "limiter": limiter, "kernel": KERNEL_NAMES[dom], "achieved": achieved,
+    roofline = {"bound": "hbm", "limiter": limiter, "kernel": names[dom], "achieved": achieved,
                 "peak": peak,
                 "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / peak,
-                "traffic": ncu_traffic(KERNEL_NAMES[dom], workload_name(w)),
+                "traffic": ncu_traffic(names[dom], workload_name(w)),
                 "algorithmic_bytes": bytes_.value, "fp32_tflops": fp32_rate,
                 "compute": {"fp32_equivalent_tflops": fp32_rate, "fp32_peak_tflops": fma2.value,
                             "fp32_peak_scalar_tflops": fma.value, "frac": fp32_rate / fma2.value,
                             "note": "flops of the direct formulation (81 taps x M time samples per polar sample, "
-                                    "complex); the kernel does fewer on the CUDA cores (time samples mixed on the "
-                                    "tensor cores). Peaks measured in this run (rectv_measure_fp32_peak): packed "
+                                    "complex); the kernels do fewer (per-ray path: time samples mixed on the "
+                                    "tensor cores; direction path: taps once per position for all rays of a "
+                                    "direction). Peaks measured in this run (rectv_measure_fp32_peak): packed "
                                     "fma.rn.f32x2 and scalar fma.rn chains on every SM"},
                 "ms_per_launch": ktimes[dom],
-                "per_iteration_ms": {KERNEL_NAMES[k]: share[k] for k in share}}
+                "per_iteration_ms": {names[k]: share[k] for k in share}}
+
+    # ---- the same workload on the per-ray tensor-core kernels (3xTF32 time-sample
+    # mixing), for comparison: the geometry is rebuilt without direction sharing ----
+    per_ray = None
+    if ndir > 0 and rank == 0 and world == 1 and args.per_ray_steps > 0:
+        os.environ["RECTV_DIRS"] = "0"
+        try:
+            obj.setup_device(d_g.data_ptr(), d_theta.data_ptr(), d_phi.data_ptr(), center, lam0, lam1, titer)
+            obj.autotune()
+            obj.iterate(2)
+            torch.cuda.synchronize()
+            a = torch.cuda.Event(enable_timing=True)
+            b = torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            obj.iterate(args.per_ray_steps)
+            b.record(stream)
+            torch.cuda.synchronize()
+            pr_ms = a.elapsed_time(b) / args.per_ray_steps
+            per_ray = {"value": 1e3 / pr_ms, "unit": "iter/s", "ms_per_step": pr_ms, "steps": args.per_ray_steps,
+                       "what": "the same workload with RECTV_DIRS=0: every ray interpolated on its own, time "
+                               "samples mixed on the tensor cores (k_gather_tc, k_scatter_tc)"}
+        finally:
+            os.environ.pop("RECTV_DIRS", None)
+        obj.setup_device(d_g.data_ptr(), d_theta.data_ptr(), d_phi.data_ptr(), center, lam0, lam1, titer)
+        obj.autotune()
 
     # ---- end-to-end through rectv_run with pinned host buffers ----
     g_h = torch.empty((nz, ntheta, n), dtype=torch.float32, pin_memory=True)
@@ -760,6 +800,8 @@ def run_ours(args, rank, world, local_rank):
         "data": "synthetic: 10 moving ellipsoids, forward-projected with this library + 1% Gaussian noise",
         "config": {"workload": workload_name(w), "lambda0": w["lambda0"], "lambda1": lam1, "center": center,
                    "chunks": nz // nzp, "batch_slices": zbs[0].value,
+                   "usfft_path": ("directions: %d directions x %d rays share their sample positions" %
+                                  (ndir, ntheta // ndir)) if ndir > 0 else "per ray (tensor cores)",
                    "l2": "inputs larger than L2 (iterate 4.3 GB, dual variables 3x19 GB)",
                    "parallelism": "replicas" if world > 1 else "single"},
         "voxel_updates_per_s": value * voxels,
@@ -772,6 +814,7 @@ def run_ours(args, rank, world, local_rank):
         "cufft_execs": ffts[0].value * args.steps,
         "rho_final": float(hist["rho"][-1]) if len(hist["rho"]) else None,
         "rel_err_vs_fp64": acc,
+        "per_ray_path": per_ray,
         "autotune": {"gather_slices_per_block": tuned[0], "scatter_blocks": tuned[1] or "one per SM",
                      "seconds": t_tune},
         "result_finite": finite,
@@ -833,6 +876,8 @@ def main():
     ap.add_argument("--serve", type=int, default=32, help="requests of the serving run (0: skip)")
     ap.add_argument("--serve-iters", type=int, nargs=2, default=[8, 16],
                     help="range of outer iterations per request (the full serving config: 200 requests, 32 128)")
+    ap.add_argument("--per-ray-steps", type=int, default=3,
+                    help="outer iterations timed on the per-ray tensor-core kernels for comparison (0: skip)")
     ap.add_argument("--acc-iters", type=int, default=64,
                     help="outer iterations of the FP64 accuracy check on a 2-slice subset (0: skip)")
     ap.add_argument("--nz", type=int, default=None, help="slices (default: the workload's); for small ncu cases")

@@ -54,16 +54,14 @@ constexpr int kCells = kFW * kFW;  // 576
 constexpr int kChunks = 8;         // 16-byte chunks of a cell: time samples (2i, 2i+1), complex
 
 // ---- forward ----
-constexpr int kFCons = 8;                 // consumer warps: taps and rays
-constexpr int kFProd = 8;                 // producer warps: the next slice's footprint
-constexpr int kFThr = 32 * (kFCons + kFProd);
+constexpr int kFThr = 256;
 constexpr int kFCap = 128;  // positions per forward item
 
 constexpr int kWt = 5 * kTaps;  // weights per position (odd row pitch: the four positions of a warp on distinct banks)
 
 struct FwdSmem {
-    float4 fp[2][kCells * kChunks];  // footprints of 16 time samples (this slice and the next),
-                                     // cell-major; chunk i of cell c at slot (i + 2 (c & 3)) & 7
+    float4 fp[kCells * kChunks];  // footprint of 16 time samples, cell-major; chunk i of cell c at
+                                  // slot (i + 2 (c & 3)) & 7
     // per position: [0,9) (-1)^b w_b of the x taps, [9,18) their derivatives
     // along x, [18,27) (-1)^a w_a of the y taps times the stencil origin's
     // fftshift sign, [27,36) those times cos, [36,45) minus sin times their
@@ -106,19 +104,17 @@ __device__ __forceinline__ float2 cmulc(float2 a, float2 b) {
 }  // namespace
 
 // ---------------------------------------------------------------------------
-// Forward: one block (512 threads, one per SM) per (work item, slices); an
-// item is at most 128 positions whose stencils start in one 16x16 tile of
-// the oversampled grid.  Eight producer warps copy the tile's 24x24-cell
-// footprint of 16 time samples of the next slice (coalesced loads,
-// cell-major stores into the second buffer) from the halo-padded spectra
-// (tiles right of the Nyquist column read the mirrored cells and conjugate)
-// while eight consumer warps work on this slice: eight lanes per position
-// (two time samples each) sum the 81 taps, then mix the position's rays:
-// each lane forms its two time samples' share of all eight rays of a round,
-// the eight lanes add their shares by recursive halving (14 shuffles) and
-// lane i keeps ray i.  One block barrier per slice.
+// Forward: one block (256 threads) per (work item, slices); an item is at
+// most 128 positions whose stencils start in one 16x16 tile of the
+// oversampled grid.  Per slice the tile's 24x24-cell footprint of 16 time
+// samples is copied (coalesced loads, cell-major stores) from the halo-padded
+// spectra (tiles right of the Nyquist column read the mirrored cells and
+// conjugate), then eight lanes per position (two time samples each) sum the
+// 81 taps, and mix the position's rays: each lane forms its two time
+// samples' share of all eight rays of a round, the eight lanes add their
+// shares by recursive halving (14 shuffles) and lane i keeps ray i.
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(kFThr, 1)
+__global__ void __launch_bounds__(kFThr, 2)
     k_gather_dir(float2 *__restrict__ rows, const float2 *__restrict__ spec, const uint32_t *__restrict__ pos,
                  const int4 *__restrict__ items, const float2 *__restrict__ dsincos,
                  const int *__restrict__ ray_start, const uint32_t *__restrict__ rays,
@@ -176,15 +172,15 @@ __global__ void __launch_bounds__(kFThr, 1)
 
     const int ngroups = (cnt + 3) / 4;  // four positions per warp
     const int pi = lane >> 3, ci = lane & 7;
+    const int fc = lane & 3, fj = lane >> 2;  // footprint copies: cell of four, time sample of eight
     const int j0 = jbase + 2 * ci;      // this lane's time samples j0, j0 + 1
-
-    // footprint of slice zz into buffer bf by producer warp pw: lane = (cell
-    // fc of four, time sample fj of eight), rows pw, pw + 8, pw + 16; a
-    // half-warp writes four cells x four time samples on distinct banks, a
-    // warp reads eight 32-byte runs; all 36 loads in flight, then the stores
-    auto fill = [&](int zz, int bf, int pw) {
-        const int fc = lane & 3, fj = lane >> 2;
-        const float2 *simg = spec + ((long long)zz * g.m + jbase) * g.img_fwd;
+    for (int z = z0; z < z1; ++z) {
+        // ---- footprint of slice z: lane = (cell cl of four, time sample jj of
+        // eight), warp w copies rows w, w + 8, w + 16: a half-warp writes four
+        // cells x four time samples on distinct banks, a warp reads eight
+        // 32-byte runs ----
+        // (all 36 loads of a thread in flight, then the stores)
+        const float2 *simg = spec + ((long long)z * g.m + jbase) * g.img_fwd;
         float2 fv[2][kFW / 8][kFW / 4];
 #pragma unroll
         for (int jh = 0; jh < 2; ++jh) {
@@ -192,7 +188,7 @@ __global__ void __launch_bounds__(kFThr, 1)
             const float2 *sj = simg + (long long)j * g.img_fwd;
 #pragma unroll
             for (int rr = 0; rr < kFW / 8; ++rr) {
-                const int KY = KY0 + pw + 8 * rr;
+                const int KY = KY0 + wid + 8 * rr;
                 const float2 *srow = sj + (long long)((mirrored ? g.P - KY : KY) + kHalo) * g.qp;
 #pragma unroll
                 for (int cq = 0; cq < kFW / 4; ++cq) {
@@ -207,28 +203,20 @@ __global__ void __launch_bounds__(kFThr, 1)
             const int j = 8 * jh + fj;
 #pragma unroll
             for (int rr = 0; rr < kFW / 8; ++rr) {
-                const int row = pw + 8 * rr;
-                float2 *drow = reinterpret_cast<float2 *>(sm.fp[bf]) + (row * kFW + fc) * 16 + ((j + 4 * fc) & 15);
+                const int row = wid + 8 * rr;
+                float2 *drow = reinterpret_cast<float2 *>(sm.fp) + (row * kFW + fc) * 16 + ((j + 4 * fc) & 15);
 #pragma unroll
                 for (int cq = 0; cq < kFW / 4; ++cq) drow[64 * cq] = fv[jh][rr][cq];
             }
         }
-    };
-    static_assert(kFProd == kFW / 3, "three footprint rows per producer warp");
-    if (wid >= kFCons && z0 < z1) fill(z0, 0, wid - kFCons);
-    __syncthreads();
+        __syncthreads();
 
-    for (int z = z0; z < z1; ++z) {
-        const int buf = (z - z0) & 1;
-        if (wid >= kFCons) {  // producers: the next slice
-            if (z + 1 < z1) fill(z + 1, buf ^ 1, wid - kFCons);
-        } else {
-        for (int gi = wid; gi < ngroups; gi += kFCons) {
+        for (int gi = wid; gi < ngroups; gi += kFThr / 32) {
             const int e = 4 * gi + pi;
             const int id = sm.pid[e];
             const int org = sm.org[e];
             const int lx0 = org % kFW;
-            const float4 *fb = sm.fp[buf] + org * kChunks;
+            const float4 *fb = sm.fp + org * kChunks;
             int so[4];
 #pragma unroll
             for (int bq = 0; bq < 4; ++bq) so[bq] = (ci + 2 * ((lx0 + bq) & 3)) & 7;
@@ -341,8 +329,7 @@ __global__ void __launch_bounds__(kFThr, 1)
                 }
             }
         }
-        }
-        __syncthreads();  // this buffer is refilled with slice z + 2, the next one is complete
+        __syncthreads();  // the footprint buffer is refilled for the next slice
     }
 }
 
