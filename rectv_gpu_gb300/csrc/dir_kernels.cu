@@ -73,6 +73,7 @@ struct FwdSmem {
 
 // ---- adjoint ----
 constexpr int kAThr = kT * kT;         // one thread per cell of a tile, one slice per block
+constexpr int kAWarps = kAThr / 32;    // warp w: cells of rows 4 (w >> 1) .. + 3, columns 8 (w & 1) .. + 7
 constexpr int kATab = 128;             // entries per table (host table builder)
 constexpr int kAMaxSeg = 16;           // directions per table (host table builder)
 constexpr int kAInfo = adj_info_words(kAMaxSeg);
@@ -341,7 +342,7 @@ __global__ void __launch_bounds__(kFThr, 2)
 // order.  Out: emix[((z ndir + d) n + q)] = 16 float4, E of time samples
 // (2i, 2i+1) in [i], E_perp in [8 + i].
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(kMThr)
+__global__ void __launch_bounds__(kMThr, 1)
     k_adj_mix(float4 *__restrict__ emix, const float2 *__restrict__ rowsc, const int *__restrict__ ray_start,
               const uint32_t *__restrict__ rays, const float *__restrict__ tau, const float2 *__restrict__ kmat,
               const float2 *__restrict__ shifta, UsGeo g, int ndir, int jbase) {
@@ -370,23 +371,39 @@ __global__ void __launch_bounds__(kMThr)
         }
         __syncthreads();
         if (q >= 1 && q < g.n) {
-            for (int r = 0; r < nc; ++r) {
-                const uint32_t rv = rvs[r];
-                const long long th = rv & 0x7fffffffu;
-                const int k = (rv >> 31) ? g.n - q : q;
-                float2 R = __ldg(rowsc + ((long long)z * g.ntheta + th) * hn + (k <= g.n / 2 ? k : g.n - k));
-                if (k > g.n / 2) R.y = -R.y;  // the other half of the real row's spectrum
-                const float2 sh = __ldg(shifta + k);
-                const float cf = (k & 1) ? g.cw : -g.cw;  // (-1)^(k+1) (pi/mu)/n
-                const float2 er = cmul(R, make_float2(sh.x * cf, sh.y * cf));
-                const float dl = qp * tvs[r];  // this ray's offset across the direction
+            // the row factor of the two orientations: (-1)^(k+1) shiftadj(k) (pi/mu)/n, k = q or n - q
+            const int kq = q, ko = g.n - q;
+            const float2 shq = __ldg(shifta + kq), sho = __ldg(shifta + ko);
+            const float cq = (kq & 1) ? g.cw : -g.cw, co = (ko & 1) ? g.cw : -g.cw;
+            const float2 fq = make_float2(shq.x * cq, shq.y * cq), fo = make_float2(sho.x * co, sho.y * co);
+            for (int r0c = 0; r0c < nc; r0c += 8) {
+                // the row values of eight rays in flight together
+                float2 R[8];
 #pragma unroll
-                for (int j = 0; j < 16; ++j) {
-                    const float2 a = cmulc(ks[r][j], er);
-                    e[j].x += a.x;
-                    e[j].y += a.y;
-                    ep[j].x = fmaf(dl, a.x, ep[j].x);
-                    ep[j].y = fmaf(dl, a.y, ep[j].y);
+                for (int i = 0; i < 8; ++i) {
+                    R[i] = make_float2(0.f, 0.f);
+                    if (r0c + i < nc) {
+                        const uint32_t rv = rvs[r0c + i];
+                        const long long th = rv & 0x7fffffffu;
+                        const int k = (rv >> 31) ? ko : kq;
+                        R[i] = __ldg(rowsc + ((long long)z * g.ntheta + th) * hn + (k <= g.n / 2 ? k : g.n - k));
+                        if (k > g.n / 2) R[i].y = -R[i].y;  // the other half of the real row's spectrum
+                    }
+                }
+#pragma unroll
+                for (int i = 0; i < 8; ++i) {
+                    if (r0c + i >= nc) break;
+                    const uint32_t rv = rvs[r0c + i];
+                    const float2 er = cmul(R[i], (rv >> 31) ? fo : fq);
+                    const float dl = qp * tvs[r0c + i];  // this ray's offset across the direction
+#pragma unroll
+                    for (int j = 0; j < 16; ++j) {
+                        const float2 a = cmulc(ks[r0c + i][j], er);
+                        e[j].x += a.x;
+                        e[j].y += a.y;
+                        ep[j].x = fmaf(dl, a.x, ep[j].x);
+                        ep[j].y = fmaf(dl, a.y, ep[j].y);
+                    }
                 }
             }
         }
@@ -404,16 +421,18 @@ __global__ void __launch_bounds__(kMThr)
 // ---------------------------------------------------------------------------
 // Adjoint, step 2: persistent blocks of 256 threads, two per SM, take (tile,
 // slice) units round-robin (slices fastest, so that blocks in flight share
-// their tiles' records in L2), one thread per cell of the 16x16 tile.  A tile's entries (positions whose
-// stencil touches it, direction-major) come in tables of at most 128 entries
-// and 16 directions, with the geometry records of the per-ray scatter (x and
-// y weight rows over the tile, k_adj_records_dir) and the rows of each
-// direction that cover each warp's two tile rows (k_adj_tabinfo); a table's
-// records, segmentation and the E, E_perp of its entries are copied
-// (cp.async) while the table before it is processed.  Per table every
-// cell adds w E_j + w_perp E_perp_j of the entries covering its rows into its
-// 16 time samples (FP32, entry order: reproducible).  The unit's sums go into
-// the Hermitian half planes of the C2R inverse as in k_scatter_tc.
+// their tiles' records in L2), one thread per cell of the 16x16 tile and a
+// warp per 4x8-cell block (a 9x9 stencil touches fewer of these than of
+// 2x16-cell rows).  A tile's entries (positions whose stencil touches it,
+// direction-major) come in tables of at most 128 entries and 16 directions,
+// with the geometry records of the per-ray scatter (x and y weight rows over
+// the tile, k_adj_records_dir) and the entries of each direction that touch
+// each warp's block (k_adj_tabinfo); a table's records, segmentation and the
+// E, E_perp of its entries are copied (cp.async) while the table before it is
+// processed.  Per table every cell adds w E_j + w_perp E_perp_j of the entries
+// touching its block into its 16 time samples (FP32, entry order:
+// reproducible).  The unit's sums go into the Hermitian half planes of the
+// C2R inverse as in k_scatter_tc.
 // ---------------------------------------------------------------------------
 __global__ void __launch_bounds__(kAThr, 2)
     k_scatter_dir(const float4 *__restrict__ emix, float2 *__restrict__ spec, const AdjRec *__restrict__ recs,
@@ -423,8 +442,9 @@ __global__ void __launch_bounds__(kAThr, 2)
     extern __shared__ __align__(16) unsigned char dir_adj_smem[];
     AdjSmem &sm = *reinterpret_cast<AdjSmem *>(dir_adj_smem);
     const int P = g.P;
-    const int tid = threadIdx.x, wid = tid >> 5;  // warp wid: tile rows 2 wid, 2 wid + 1
-    const int cx = tid % kT, cy = tid / kT;
+    const int tid = threadIdx.x, wid = tid >> 5, lane = tid & 31;
+    // this thread's cell: warp block wid (4 rows x 8 columns), lane = (row, column) in it
+    const int cx = 8 * (wid & 1) + (lane & 7), cy = 4 * (wid >> 1) + (lane >> 3);
     const float cb = 2.f * g.wexp / g.tn * g.inv2n;  // c1/(2n): B = cb (cos, -sin)
 
     // copy cursor: the next table (unit, table of the unit) in consumption order
@@ -571,15 +591,23 @@ __global__ void k_adj_records_dir(AdjRec *__restrict__ recs, const uint32_t *__r
         dy += (dy < -half) ? P : 0;
         dy -= (dy > half) ? P : 0;
         AdjRec r;
-        int mask = 0;
+        int rows = 0, cols = 0;
 #pragma unroll
         for (int c = 0; c < kT; ++c) {
             const int bx = c - dx, by = c - dy;
-            r.wx[c] = ((unsigned)bx < (unsigned)kTaps) ? tap_weight(fx, bx, x0, g) : 0.f;
-            const bool iny = (unsigned)by < (unsigned)kTaps;
+            const bool inx = (unsigned)bx < (unsigned)kTaps, iny = (unsigned)by < (unsigned)kTaps;
+            r.wx[c] = inx ? tap_weight(fx, bx, x0, g) : 0.f;
             r.wy[c] = iny ? tap_weight(fy, by, y0, g) : 0.f;
-            mask |= iny ? (1 << c) : 0;
+            rows |= iny ? (1 << c) : 0;
+            cols |= inx ? (1 << c) : 0;
         }
+        // warp blocks of k_scatter_dir the stencil touches (block w: rows
+        // 4 (w >> 1) .. + 3, columns 8 (w & 1) .. + 7), as bits 2w and 2w + 1: the
+        // form of a row mask k_adj_tabinfo segments by
+        int mask = 0;
+#pragma unroll
+        for (int w = 0; w < kAWarps; ++w)
+            if (((rows >> (4 * (w >> 1))) & 0xf) && ((cols >> (8 * (w & 1))) & 0xff)) mask |= 3 << (2 * w);
         r.thm = (d << 16) | mask;
         r.k = q;
         const float ax = (float)(fx - kR - dx) * g.inv2n - x0, ay = (float)(fy - kR - dy) * g.inv2n - y0;
