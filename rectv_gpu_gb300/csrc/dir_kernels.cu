@@ -79,6 +79,7 @@ constexpr int kAMaxSeg = 16;           // directions per table (host table build
 constexpr int kAInfo = adj_info_words(kAMaxSeg);
 constexpr int kMThr = 256;             // positions per k_adj_mix block
 constexpr int kMRays = 32;             // rays per staged chunk of k_adj_mix
+constexpr int kMFly = 4;               // row loads in flight per thread of k_adj_mix
 
 struct AdjSmem {
     AdjRec rec[2][kATab];                  // geometry records of this table and the next
@@ -342,7 +343,7 @@ __global__ void __launch_bounds__(kFThr, 2)
 // order.  Out: emix[((z ndir + d) n + q)] = 16 float4, E of time samples
 // (2i, 2i+1) in [i], E_perp in [8 + i].
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(kMThr, 1)
+__global__ void __launch_bounds__(kMThr, 2)
     k_adj_mix(float4 *__restrict__ emix, const float2 *__restrict__ rowsc, const int *__restrict__ ray_start,
               const uint32_t *__restrict__ rays, const float *__restrict__ tau, const float2 *__restrict__ kmat,
               const float2 *__restrict__ shifta, UsGeo g, int ndir, int jbase) {
@@ -376,11 +377,11 @@ __global__ void __launch_bounds__(kMThr, 1)
             const float2 shq = __ldg(shifta + kq), sho = __ldg(shifta + ko);
             const float cq = (kq & 1) ? g.cw : -g.cw, co = (ko & 1) ? g.cw : -g.cw;
             const float2 fq = make_float2(shq.x * cq, shq.y * cq), fo = make_float2(sho.x * co, sho.y * co);
-            for (int r0c = 0; r0c < nc; r0c += 8) {
-                // the row values of eight rays in flight together
-                float2 R[8];
+            for (int r0c = 0; r0c < nc; r0c += kMFly) {
+                // the row values of kMFly rays in flight together
+                float2 R[kMFly];
 #pragma unroll
-                for (int i = 0; i < 8; ++i) {
+                for (int i = 0; i < kMFly; ++i) {
                     R[i] = make_float2(0.f, 0.f);
                     if (r0c + i < nc) {
                         const uint32_t rv = rvs[r0c + i];
@@ -391,7 +392,7 @@ __global__ void __launch_bounds__(kMThr, 1)
                     }
                 }
 #pragma unroll
-                for (int i = 0; i < 8; ++i) {
+                for (int i = 0; i < kMFly; ++i) {
                     if (r0c + i >= nc) break;
                     const uint32_t rv = rvs[r0c + i];
                     const float2 er = cmul(R[i], (rv >> 31) ? fo : fq);
