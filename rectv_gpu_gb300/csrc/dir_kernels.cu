@@ -341,13 +341,22 @@ __global__ void __launch_bounds__(kFThr, 2)
 // slice, 256 positions), one thread per position; the direction's rays are
 // taken 32 at a time with their K' rows staged in shared memory, in ray
 // order.  Out: emix[((z ndir + d) n + q)] = 16 float4, E of time samples
-// (2i, 2i+1) in [i], E_perp in [8 + i].
+// (2i, 2i+1) in [i], E_perp in [8 + i].  The blocks also clear the nzero
+// float4 of the half planes the scatter adds into (the memory pipe is idle
+// in this latency-bound kernel).
 // ---------------------------------------------------------------------------
 __global__ void __launch_bounds__(kMThr, 2)
     k_adj_mix(float4 *__restrict__ emix, const float2 *__restrict__ rowsc, const int *__restrict__ ray_start,
               const uint32_t *__restrict__ rays, const float *__restrict__ tau, const float2 *__restrict__ kmat,
-              const float2 *__restrict__ shifta, UsGeo g, int ndir, int jbase) {
+              const float2 *__restrict__ shifta, UsGeo g, int ndir, int jbase, float4 *__restrict__ zero,
+              long long nzero) {
     __shared__ float2 ks[kMRays][16];
+    {
+        const long long nthr = (long long)gridDim.x * gridDim.y * gridDim.z * kMThr;
+        const long long t0 = (((long long)blockIdx.z * gridDim.y + blockIdx.y) * gridDim.x + blockIdx.x) * kMThr +
+                             threadIdx.x;
+        for (long long i = t0; i < nzero; i += nthr) zero[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+    }
     __shared__ uint32_t rvs[kMRays];
     __shared__ float tvs[kMRays];
     const int d = blockIdx.x, z = blockIdx.y;
@@ -654,8 +663,10 @@ void launch_scatter_dir(const float2 *rowsc, float2 *spec, int zb, const GeoDev 
     if (nunits > 2147483647LL) throw Error(1, "adjoint grid too large");
     if (zb > gd.demix_slices) throw Error(1, "adjoint direction mixing buffer too small");
     const dim3 gm(gd.ndir, zb, (g.n + kMThr - 1) / kMThr);
+    // the first group of time samples also clears the half planes of all of them
+    const long long nzero = jbase == 0 ? (long long)zb * g.m * g.P * g.hpitch / 2 : 0;
     k_adj_mix<<<gm, kMThr, 0, s>>>(gd.demix, rowsc, gd.dray_start, gd.drays, gd.dtau, gd.kmat, gd.shiftadj, g, gd.ndir,
-                                   jbase);
+                                   jbase, reinterpret_cast<float4 *>(spec), nzero);
     LAUNCH_CHECK("k_adj_mix");
     static int nsm = 0;
     if (nsm == 0) {

@@ -729,7 +729,8 @@ struct Handle {
             // Re IFFT2 of the scattered grids as a C2R of their Hermitian part,
             // which the tensor-core scatter adds into zeroed half planes
             const long long img_half = (long long)ug.P * ug.hpitch;
-            CUDA_CHECK(cudaMemsetAsync(spec, 0, sizeof(float2) * (size_t)nimg * img_half, stream));
+            // (the direction path clears them inside k_adj_mix)
+            if (!gd.dirs) CUDA_CHECK(cudaMemsetAsync(spec, 0, sizeof(float2) * (size_t)nimg * img_half, stream));
             launch_scatter_adj(rowsc, spec, zb, gd, ug, stream);
             if (pad_fft) {
                 launch_pad_fft_inv_accum(spec, u, zb, tau, gd.deapod, fft_tw, fft_inv_map, gd.err, ug, stream);
