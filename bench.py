@@ -357,11 +357,12 @@ def make_job_data(torch, jobs, device):
     return jobs
 
 
-def run_engine(jobs, arrivals, max_resident=0, autotune=False, largest_first=False, age_priority=True, keep=None):
+def run_engine(jobs, arrivals, max_resident=0, autotune=False, largest_first=False, age_priority=True, keep=None,
+               shortest_first=False):
     """Runs the jobs through the engine; returns per-job info and stats."""
     from rectv_gpu_gb300.engine import Engine
     with Engine(max_resident=max_resident, autotune=autotune, largest_first=largest_first,
-                age_priority=age_priority) as eng:
+                age_priority=age_priority, shortest_first=shortest_first) as eng:
         ids = []
         for j, a in zip(jobs, arrivals):
             ids.append(eng.submit(j["g"].numpy(), j["theta"], j["phi"], nzp=j["nzp"], niter=j["niter"],
@@ -454,7 +455,9 @@ def serving_form(torch, device, throughput, count, iters, max_running, seed=5, l
     outer iterations each, at `load` times the rate the batched throughput
     sustains; continuous batching (admission by the HBM budget as memory and
     slots free up, resident state, up to `max_running` jobs overlapping on
-    the device, age priority) against one request at a time (same arrivals)."""
+    the device, age priority) against one request at a time (same arrivals),
+    each with requests admitted in arrival order and with the arrived request
+    of least work first."""
     jobs = make_job_data(torch, draw_jobs(seed, count, iters), device)
     mean_work = sum(job_work(j) for j in jobs) / count
     rate = load * throughput / mean_work
@@ -465,10 +468,13 @@ def serving_form(torch, device, throughput, count, iters, max_running, seed=5, l
                        "arrivals at %.3f requests/s (%.0f%% of the batched throughput)"
                        % (count, iters[0], iters[1], rate, 100 * load),
            "rate_per_s": rate}
-    for name, mr in (("continuous_batching", max_running), ("one_at_a_time", 1)):
-        infos, st = run_engine(jobs, arrivals, max_resident=mr, autotune=True)
+    for name, mr, sjf in (("continuous_batching", max_running, False), ("one_at_a_time", 1, False),
+                          ("continuous_batching_shortest_first", max_running, True),
+                          ("one_at_a_time_shortest_first", 1, True)):
+        infos, st = run_engine(jobs, arrivals, max_resident=mr, autotune=True, shortest_first=sjf)
         lat = np.array([x["latency"] for x in infos])
-        out[name] = {"max_running": mr or "all", "p50_latency_s": float(np.percentile(lat, 50)),
+        out[name] = {"max_running": mr or "all", "admission": "least work first" if sjf else "arrival order",
+                     "p50_latency_s": float(np.percentile(lat, 50)),
                      "p99_latency_s": float(np.percentile(lat, 99)), "mean_latency_s": float(lat.mean()),
                      "makespan_s": st["makespan"], "requests_per_s": count / st["makespan"],
                      "voxel_updates_per_s": work / st["makespan"], "peak_running": st["peak_running"]}

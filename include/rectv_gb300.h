@@ -214,9 +214,11 @@ enum {
     RECTV_ENGINE_NO_REUSE = 1,      /* free each job's handle when it finishes */
     RECTV_ENGINE_AUTOTUNE = 2,      /* rectv_autotune each job's launch shapes (cached) */
     RECTV_ENGINE_LARGEST_FIRST = 4, /* among equal arrival times, admit the most work first */
-    RECTV_ENGINE_AGE_PRIORITY = 8   /* each job's stream gets a lower priority than every job running
+    RECTV_ENGINE_AGE_PRIORITY = 8,  /* each job's stream gets a lower priority than every job running
                                        when it was admitted: the oldest runs first, newer jobs fill the
                                        SMs it leaves idle */
+    RECTV_ENGINE_SHORTEST_FIRST = 16 /* among the jobs that have arrived, admit the one with the least
+                                        work (estimated bytes x iterations) first */
 };
 
 /* hbm_budget_bytes <= 0: the free device memory minus 4 GiB; max_resident <= 0:

@@ -11,8 +11,9 @@
 // captured outer-iteration graphs, from admission until its last iteration.
 //
 // Scheduling.  Jobs are admitted in order of arrival (the batched form:
-// largest first) when their estimated device memory fits the budget and
-// fewer than max_resident jobs are running.  On admission the job's data is
+// largest first; serving may take, among the jobs that have arrived, the one
+// with the least work first) when their estimated device memory fits the
+// budget and fewer than max_resident jobs are running.  On admission the job's data is
 // uploaded and all its outer iterations are queued on the handle's own
 // stream as graph launches; the GPU interleaves the kernels of every running
 // job, so the iterations of different problems overlap on the device.  The
@@ -172,6 +173,7 @@ struct Engine {
     bool reuse;
     bool tune;
     bool largest_first = false;
+    bool shortest_first = false;
     bool age_priority = false;
     int prio_least = 0, prio_greatest = 0;  // stream priority range (numerically lower = higher)
     int device = 0;
@@ -195,6 +197,7 @@ struct Engine {
         reuse = !(flags & RECTV_ENGINE_NO_REUSE);
         tune = (flags & RECTV_ENGINE_AUTOTUNE) != 0;
         largest_first = (flags & RECTV_ENGINE_LARGEST_FIRST) != 0;
+        shortest_first = (flags & RECTV_ENGINE_SHORTEST_FIRST) != 0;
         age_priority = (flags & RECTV_ENGINE_AGE_PRIORITY) != 0;
         CUDA_CHECK(cudaDeviceGetStreamPriorityRange(&prio_least, &prio_greatest));
     }
@@ -379,9 +382,9 @@ struct Engine {
             if (largest_first) return a->est_bytes * a->niter > b->est_bytes * b->niter;
             return false;
         });
-        std::vector<Job *> active;
+        std::vector<Job *> active, pool;
         size_t next = 0;
-        while (next < order.size() || !active.empty()) {
+        while (next < order.size() || !pool.empty() || !active.empty()) {
             bool progress = false;
             for (size_t i = 0; i < active.size();) {
                 Job &j = *active[i];
@@ -400,20 +403,27 @@ struct Engine {
                 progress = true;
             }
             const double t = now();
-            while (next < order.size() && order[next]->arrival <= t && running < max_resident) {
-                Job &j = *order[next];
+            // jobs that have arrived, in arrival order
+            while (next < order.size() && order[next]->arrival <= t) pool.push_back(order[next++]);
+            while (!pool.empty() && running < max_resident) {
+                // the first in line, or the arrived job with the least work
+                size_t pick = 0;
+                if (shortest_first)
+                    for (size_t i = 1; i < pool.size(); ++i)
+                        if (pool[i]->est_bytes * pool[i]->niter < pool[pick]->est_bytes * pool[pick]->niter) pick = i;
+                Job &j = *pool[pick];
                 bool ok = false;
                 try {
                     ok = admit(j, active);
                 } catch (const std::exception &e) {
                     fail(j, e.what());
-                    ++next;
+                    pool.erase(pool.begin() + (long)pick);
                     progress = true;
                     continue;
                 }
-                if (!ok) break;  // first in line waits for memory
+                if (!ok) break;  // the chosen job waits for memory
                 active.push_back(&j);
-                ++next;
+                pool.erase(pool.begin() + (long)pick);
                 progress = true;
             }
             if (!progress) {

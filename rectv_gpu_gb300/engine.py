@@ -27,6 +27,7 @@ NO_REUSE = 1
 AUTOTUNE = 2
 LARGEST_FIRST = 4
 AGE_PRIORITY = 8
+SHORTEST_FIRST = 16
 STATUS = {0: "waiting", 1: "running", 2: "done", 3: "failed"}
 
 
@@ -43,14 +44,16 @@ def _pinned(shape, dtype=np.float32):
 
 class Engine:
     def __init__(self, budget_bytes=0.0, max_resident=0, reuse=True, autotune=False, largest_first=False,
-                 age_priority=True, pin=True):
+                 age_priority=True, pin=True, shortest_first=False):
         """budget_bytes <= 0: the free device memory minus 4 GiB; max_resident
         <= 0: no limit on running jobs; age_priority: each job's stream has a
         lower priority than the jobs running when it was admitted (the oldest
-        runs first, newer jobs fill the SMs it leaves idle)."""
+        runs first, newer jobs fill the SMs it leaves idle); shortest_first:
+        among the jobs that have arrived, the one with the least work is
+        admitted first (instead of the first to arrive)."""
         lib = _lib.load()
         flags = ((0 if reuse else NO_REUSE) | (AUTOTUNE if autotune else 0) | (LARGEST_FIRST if largest_first else 0)
-                 | (AGE_PRIORITY if age_priority else 0))
+                 | (AGE_PRIORITY if age_priority else 0) | (SHORTEST_FIRST if shortest_first else 0))
         h = ctypes.c_void_p()
         _lib.check(lib.rectv_engine_create(float(budget_bytes), int(max_resident), flags, ctypes.byref(h)))
         self._h = h

@@ -121,3 +121,22 @@ def test_autotune_keeps_results(env):
         obj.free()
     assert shapes[0] in (8, 16, 32, 64) and shapes[1] >= 0
     assert np.array_equal(outs[0], outs[1])
+
+
+def test_shortest_first_admission_order(env):
+    """With one job at a time and every job waiting from the start, the
+    shortest-first policy admits them in order of estimated work (bytes x
+    iterations); arrival order admits them as submitted."""
+    r, engine, _ = env
+    sizes = [(128, 180, 16, 4, 2, 4, 3), (32, 64, 4, 4, 2, 4, 3), (64, 128, 8, 3, 3, 4, 3)]
+    probs = [_problem(n, nt, m, nz, nrot, seed=i) for i, (n, nt, m, nz, nzp, nrot, it) in enumerate(sizes)]
+    work = [estimate_bytes(n, nt, m, nz, nzp) * it for (n, nt, m, nz, nzp, nrot, it) in sizes]
+    for sjf in (False, True):
+        with engine.Engine(max_resident=1, shortest_first=sjf) as eng:
+            ids = [eng.submit(g, th, ph, nzp=s[4], niter=s[6], titer=2, arrival=0.0)
+                   for s, (th, ph, g) in zip(sizes, probs)]
+            eng.run()
+            infos = [eng.info(i) for i in ids]
+        assert all(x["status"] == "done" for x in infos), infos
+        order = list(np.argsort([x["admitted"] for x in infos]))
+        assert order == (list(np.argsort(work)) if sjf else [0, 1, 2]), (sjf, order, work)
