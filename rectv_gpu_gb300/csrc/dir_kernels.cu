@@ -426,12 +426,11 @@ __global__ void __launch_bounds__(kMThr, 2)
 // thread per cell of the 16x16 tile and a warp per 4x8-cell block (a 9x9
 // stencil touches fewer of these than of 2x16-cell rows).  The adjoint only
 // needs Re IFFT2(X) = C2R of the Hermitian part H(k) = (X(k) + conj X(-k)) / 2
-// on the half plane, so the tile's cells k take X(k) from the positions whose
-// stencil touches the tile (launch with mirror = 0: stores sg X / 2 into every
-// half-plane cell, and zero into the row padding) and X(-k) from the
-// positions whose negated stencil touches it (weights at the cells -k; launch
-// with mirror = 1: adds sg conj(X(-k)) / 2): every half-plane cell has one
-// writer per launch, so there are no atomics and no clearing.  Each list comes in tables of at
+// on the half plane, so a unit forms both X(k) and X(-k) for its tile's
+// cells k, from two lists of entries: positions whose stencil touches the
+// tile, and positions whose negated stencil touches it (weights at the
+// cells -k), and stores H: every half-plane cell is written once, by one
+// thread, with no atomics and no clearing.  Each list comes in tables of at
 // most 128 entries and 16 directions, with the geometry records (x and y
 // weight rows over the tile, k_adj_records_dir) and the entries of each
 // direction that touch each warp's block (k_adj_tabinfo); a table's records,
@@ -444,8 +443,7 @@ __global__ void __launch_bounds__(kAThr, 2)
     k_scatter_dir(const float4 *__restrict__ emix, float2 *__restrict__ spec, const AdjRec *__restrict__ recs,
                   const uint32_t *__restrict__ pts, const int4 *__restrict__ items, const int4 *__restrict__ tabs,
                   const int *__restrict__ tab_base, const uint32_t *__restrict__ info,
-                  const float2 *__restrict__ dsincos, UsGeo g, int ndir, int zb, int nunits, int jbase,
-                  int mirror) {
+                  const float2 *__restrict__ dsincos, UsGeo g, int ndir, int zb, int nunits, int jbase) {
     extern __shared__ __align__(16) unsigned char dir_adj_smem[];
     AdjSmem &sm = *reinterpret_cast<AdjSmem *>(dir_adj_smem);
     const int P = g.P;
@@ -460,9 +458,9 @@ __global__ void __launch_bounds__(kAThr, 2)
     auto fetch = [&](int slot) {
         int tb0 = 0;
         while (fu < nunits) {
-            const int item = 2 * (fu / zb) + mirror;  // the tile's two lists are items 2t, 2t + 1
+            const int item = 2 * (fu / zb);  // the tile's two lists are items 2t, 2t + 1
             tb0 = __ldg(tab_base + item);
-            if (ft < __ldg(tab_base + item + 1) - tb0) break;
+            if (ft < __ldg(tab_base + item + 2) - tb0) break;
             ft = 0;
             fu += gridDim.x;
         }
@@ -496,15 +494,36 @@ __global__ void __launch_bounds__(kAThr, 2)
     int seq = 0;  // tables consumed: buffer seq & 1
 
     for (int u = blockIdx.x; u < nunits; u += gridDim.x) {
-        const int item = 2 * (u / zb) + mirror, z = u % zb;
-        const int tb0 = __ldg(tab_base + item), tb1 = __ldg(tab_base + item + 1);
-        if (mirror && tb0 == tb1) continue;  // nothing to add
+        const int item = 2 * (u / zb), z = u % zb;
         const int4 it = __ldg(items + item);
         const int tyi = it.x / g.NT, txi = it.x - tyi * g.NT;
-        float acc[32];  // X of this cell (or of the negated cell): 16 time samples x (re, im)
+        const int KY = tyi * kT + cy, KX = txi * kT + cx;
+        // this cell of H in time sample jbase (+ j img_half)
+        auto hcell = [&]() {
+            return spec + ((long long)z * g.m + jbase) * ((long long)P * g.hpitch) + (long long)KY * g.hpitch + KX;
+        };
+        float acc[32];  // X of this cell (then of the negated cell): 16 time samples x (re, im)
 #pragma unroll
         for (int i = 0; i < 32; ++i) acc[i] = 0.f;
-        for (int ti = tb0; ti < tb1; ++ti) {
+        const int tb0 = __ldg(tab_base + item), tbm = __ldg(tab_base + item + 1), tb1 = __ldg(tab_base + item + 2);
+        for (int ti = tb0; ti <= tb1; ++ti) {
+            if (ti == tbm && KY < P && KX < g.hpitch) {
+                // the direct list is done: H = sg X / 2 on the half plane (KX <= n),
+                // the row padding of the half planes cleared
+                const float sg = (KX > P / 2) ? 0.f : (((KX + KY) & 1) ? -0.5f : 0.5f);  // fftshift sign, 1/2
+                float2 *dst = hcell();
+                const long long img_half = (long long)P * g.hpitch;
+#pragma unroll
+                for (int j = 0; j < 16; ++j) {
+                    if (jbase + j >= g.m) break;
+                    dst[(long long)j * img_half] = make_float2(sg * acc[2 * j], sg * acc[2 * j + 1]);
+                }
+            }
+            if (ti == tbm) {
+#pragma unroll
+                for (int i = 0; i < 32; ++i) acc[i] = 0.f;
+            }
+            if (ti == tb1) break;
             const int buf = seq & 1;
             fetch(buf ^ 1);  // the next table: that buffer was released by the last barrier
             cp_wait<1>();    // this table's copies (issued one table earlier)
@@ -548,22 +567,17 @@ __global__ void __launch_bounds__(kAThr, 2)
             __syncthreads();  // the records, segmentation and E of this buffer are free
             ++seq;
         }
-        // H = sg X / 2 (direct list; zero in the row padding), or H += sg conj(X(-k)) / 2
-        const int KY = tyi * kT + cy, KX = txi * kT + cx;
-        if (KY < P && KX < (mirror ? P / 2 + 1 : g.hpitch)) {
+        // the mirrored list is done: H += sg conj(X(-k)) / 2 (this thread stored H above)
+        if (KY < P && KX <= P / 2) {
+            const float sg = ((KX + KY) & 1) ? -0.5f : 0.5f;
+            float2 *dst = hcell();
             const long long img_half = (long long)P * g.hpitch;
-            float2 *dst = spec + ((long long)z * g.m + jbase) * img_half + (long long)KY * g.hpitch + KX;
-            const float sg = (KX > P / 2) ? 0.f : (((KX + KY) & 1) ? -0.5f : 0.5f);  // fftshift sign, 1/2
 #pragma unroll
             for (int j = 0; j < 16; ++j) {
                 if (jbase + j >= g.m) break;
                 float2 *d = dst + (long long)j * img_half;
-                if (mirror) {
-                    const float2 h = *d;
-                    *d = make_float2(h.x + sg * acc[2 * j], h.y - sg * acc[2 * j + 1]);
-                } else {
-                    *d = make_float2(sg * acc[2 * j], sg * acc[2 * j + 1]);
-                }
+                const float2 h = *d;
+                *d = make_float2(h.x + sg * acc[2 * j], h.y - sg * acc[2 * j + 1]);
             }
         }
     }
@@ -679,13 +693,10 @@ void launch_scatter_dir(const float2 *rowsc, float2 *spec, int zb, const GeoDev 
         CUDA_CHECK(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
     }
     const int grid = (int)std::min<long long>(nunits, g.sc_grid > 0 ? g.sc_grid : 2 * nsm);
-    // the tile's own cells (stores, every half-plane cell), then the negated cells (adds)
-    for (int mirror = 0; mirror < 2; ++mirror) {
-        k_scatter_dir<<<grid, kAThr, sizeof(AdjSmem), s>>>(gd.demix, spec, gd.adj_recs, gd.adj_pts, gd.adj_items,
-                                                           gd.adj_tabs, gd.adj_tab_base, gd.adj_info, gd.sincos, g,
-                                                           gd.ndir, zb, (int)nunits, jbase, mirror);
-        LAUNCH_CHECK("k_scatter_dir");
-    }
+    k_scatter_dir<<<grid, kAThr, sizeof(AdjSmem), s>>>(gd.demix, spec, gd.adj_recs, gd.adj_pts, gd.adj_items,
+                                                       gd.adj_tabs, gd.adj_tab_base, gd.adj_info, gd.sincos, g,
+                                                       gd.ndir, zb, (int)nunits, jbase);
+    LAUNCH_CHECK("k_scatter_dir");
 }
 
 }  // namespace rectv

@@ -1089,7 +1089,7 @@ struct Handle {
         // adjoint: [row preparation], the zeroing of split tiles (direct scatter),
         // one scatter per group, then [columns + rows | crop]
         const int adj_k = (fused_rows ? 0 : 1) + ((!gd.tc_scatter && gd.n_split_tiles > 0) ? 1 : 0) +
-                          ng * (gd.dirs ? 3 : 1) +
+                          ng * (gd.dirs ? 2 : 1) +
                           (own2d ? 2 : 1);
         const int adj_f = (fused_rows ? 0 : 1) + (own2d ? 0 : f2);
         // per outer iteration: titer inner steps per batch (forward, graddiv,
