@@ -341,13 +341,22 @@ __global__ void __launch_bounds__(kFThr, 2)
 // slice, 256 positions), one thread per position; the direction's rays are
 // taken 32 at a time with their K' rows staged in shared memory, in ray
 // order.  Out: emix[((z ndir + d) n + q)] = 16 float4, E of time samples
-// (2i, 2i+1) in [i], E_perp in [8 + i].
+// (2i, 2i+1) in [i], E_perp in [8 + i].  The blocks also clear the nzero
+// float4 of the half planes the scatter adds into (the memory pipe is idle
+// in this latency-bound kernel).
 // ---------------------------------------------------------------------------
 __global__ void __launch_bounds__(kMThr, 2)
     k_adj_mix(float4 *__restrict__ emix, const float2 *__restrict__ rowsc, const int *__restrict__ ray_start,
               const uint32_t *__restrict__ rays, const float *__restrict__ tau, const float2 *__restrict__ kmat,
-              const float2 *__restrict__ shifta, UsGeo g, int ndir, int jbase) {
+              const float2 *__restrict__ shifta, UsGeo g, int ndir, int jbase, float4 *__restrict__ zero,
+              long long nzero) {
     __shared__ float2 ks[kMRays][16];
+    {
+        const long long nthr = (long long)gridDim.x * gridDim.y * gridDim.z * kMThr;
+        const long long t0 = (((long long)blockIdx.z * gridDim.y + blockIdx.y) * gridDim.x + blockIdx.x) * kMThr +
+                             threadIdx.x;
+        for (long long i = t0; i < nzero; i += nthr) zero[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+    }
     __shared__ uint32_t rvs[kMRays];
     __shared__ float tvs[kMRays];
     const int d = blockIdx.x, z = blockIdx.y;
@@ -422,22 +431,18 @@ __global__ void __launch_bounds__(kMThr, 2)
 // ---------------------------------------------------------------------------
 // Adjoint, step 2: persistent blocks of 256 threads, two per SM, take (tile,
 // slice) units round-robin (slices fastest, so that blocks in flight share
-// their tiles' records in L2) over the tiles of the half plane kx <= n, one
-// thread per cell of the 16x16 tile and a warp per 4x8-cell block (a 9x9
-// stencil touches fewer of these than of 2x16-cell rows).  The adjoint only
-// needs Re IFFT2(X) = C2R of the Hermitian part H(k) = (X(k) + conj X(-k)) / 2
-// on the half plane, so a unit forms both X(k) and X(-k) for its tile's
-// cells k, from two lists of entries: positions whose stencil touches the
-// tile, and positions whose negated stencil touches it (weights at the
-// cells -k), and stores H: every half-plane cell is written once, by one
-// thread, with no atomics and no clearing.  Each list comes in tables of at
-// most 128 entries and 16 directions, with the geometry records (x and y
-// weight rows over the tile, k_adj_records_dir) and the entries of each
-// direction that touch each warp's block (k_adj_tabinfo); a table's records,
-// segmentation and the E, E_perp of its entries are copied (cp.async) while
-// the table before it is processed.  Per table every cell adds w E_j +
-// w_perp E_perp_j of the entries touching its block into its 16 time samples
-// (FP32, entry order: reproducible).
+// their tiles' records in L2), one thread per cell of the 16x16 tile and a
+// warp per 4x8-cell block (a 9x9 stencil touches fewer of these than of
+// 2x16-cell rows).  A tile's entries (positions whose stencil touches it,
+// direction-major) come in tables of at most 128 entries and 16 directions,
+// with the geometry records of the per-ray scatter (x and y weight rows over
+// the tile, k_adj_records_dir) and the entries of each direction that touch
+// each warp's block (k_adj_tabinfo); a table's records, segmentation and the
+// E, E_perp of its entries are copied (cp.async) while the table before it is
+// processed.  Per table every cell adds w E_j + w_perp E_perp_j of the entries
+// touching its block into its 16 time samples (FP32, entry order:
+// reproducible).  The unit's sums go into the Hermitian half planes of the
+// C2R inverse as in k_scatter_tc.
 // ---------------------------------------------------------------------------
 __global__ void __launch_bounds__(kAThr, 2)
     k_scatter_dir(const float4 *__restrict__ emix, float2 *__restrict__ spec, const AdjRec *__restrict__ recs,
@@ -453,19 +458,11 @@ __global__ void __launch_bounds__(kAThr, 2)
     const float cb = 2.f * g.wexp / g.tn * g.inv2n;  // c1/(2n): B = cb (cos, -sin)
 
     // copy cursor: the next table (unit, table of the unit) in consumption order
-    // (units whose tile has no entries consume no table)
     int fu = blockIdx.x, ft = 0;
     auto fetch = [&](int slot) {
-        int tb0 = 0;
-        while (fu < nunits) {
-            const int item = 2 * (fu / zb);  // the tile's two lists are items 2t, 2t + 1
-            tb0 = __ldg(tab_base + item);
-            if (ft < __ldg(tab_base + item + 2) - tb0) break;
-            ft = 0;
-            fu += gridDim.x;
-        }
         if (fu < nunits) {
-            const int zf = fu % zb;
+            const int item = fu / zb, zf = fu % zb;
+            const int tb0 = __ldg(tab_base + item), tb1 = __ldg(tab_base + item + 1);
             const int4 tb = __ldg(tabs + tb0 + ft);  // (first entry, count, word offset, words)
             const int cnt = min(tb.y, kATab), nw = min(tb.w, kAInfo);
             const char *rs = reinterpret_cast<const char *>(recs + tb.x);
@@ -486,7 +483,10 @@ __global__ void __launch_bounds__(kAThr, 2)
                     for (int c = 0; c < 8; ++c) cp_async16(dst + c, src + c);
                 }
             }
-            ++ft;
+            if (++ft >= tb1 - tb0) {
+                ft = 0;
+                fu += gridDim.x;
+            }
         }
         cp_commit();
     };
@@ -494,36 +494,14 @@ __global__ void __launch_bounds__(kAThr, 2)
     int seq = 0;  // tables consumed: buffer seq & 1
 
     for (int u = blockIdx.x; u < nunits; u += gridDim.x) {
-        const int item = 2 * (u / zb), z = u % zb;
+        const int item = u / zb, z = u % zb;
         const int4 it = __ldg(items + item);
         const int tyi = it.x / g.NT, txi = it.x - tyi * g.NT;
-        const int KY = tyi * kT + cy, KX = txi * kT + cx;
-        // this cell of H in time sample jbase (+ j img_half)
-        auto hcell = [&]() {
-            return spec + ((long long)z * g.m + jbase) * ((long long)P * g.hpitch) + (long long)KY * g.hpitch + KX;
-        };
-        float acc[32];  // X of this cell (then of the negated cell): 16 time samples x (re, im)
+        float acc[32];  // F of this cell: 16 time samples x (re, im)
 #pragma unroll
         for (int i = 0; i < 32; ++i) acc[i] = 0.f;
-        const int tb0 = __ldg(tab_base + item), tbm = __ldg(tab_base + item + 1), tb1 = __ldg(tab_base + item + 2);
-        for (int ti = tb0; ti <= tb1; ++ti) {
-            if (ti == tbm && KY < P && KX < g.hpitch) {
-                // the direct list is done: H = sg X / 2 on the half plane (KX <= n),
-                // the row padding of the half planes cleared
-                const float sg = (KX > P / 2) ? 0.f : (((KX + KY) & 1) ? -0.5f : 0.5f);  // fftshift sign, 1/2
-                float2 *dst = hcell();
-                const long long img_half = (long long)P * g.hpitch;
-#pragma unroll
-                for (int j = 0; j < 16; ++j) {
-                    if (jbase + j >= g.m) break;
-                    dst[(long long)j * img_half] = make_float2(sg * acc[2 * j], sg * acc[2 * j + 1]);
-                }
-            }
-            if (ti == tbm) {
-#pragma unroll
-                for (int i = 0; i < 32; ++i) acc[i] = 0.f;
-            }
-            if (ti == tb1) break;
+        const int tb0 = __ldg(tab_base + item), tb1 = __ldg(tab_base + item + 1);
+        for (int ti = tb0; ti < tb1; ++ti) {
             const int buf = seq & 1;
             fetch(buf ^ 1);  // the next table: that buffer was released by the last barrier
             cp_wait<1>();    // this table's copies (issued one table earlier)
@@ -539,10 +517,9 @@ __global__ void __launch_bounds__(kAThr, 2)
                     const int e1 = min((int)(lohi >> 16), cnt);
                     const int e0 = (int)(lohi & 0xffffu);
                     if (e0 >= e1) continue;
-                    // first-order weight w (A_p + s B . (cx, cy)), B across the direction
-                    const AdjRec &r0 = rec[min((int)segf[s], cnt - 1)];
-                    const float2 sc = __ldg(dsincos + ((unsigned)r0.thm >> 16));
-                    const float bxy = r0.sf.y * cb * (sc.y * (float)cx - sc.x * (float)cy);
+                    // first-order weight w (A_p + B . (cx, cy)), B across the direction
+                    const float2 sc = __ldg(dsincos + ((unsigned)rec[min((int)segf[s], cnt - 1)].thm >> 16));
+                    const float bxy = cb * (sc.y * (float)cx - sc.x * (float)cy);
                     for (int e = e0; e < e1; ++e) {
                         const float w = rec[e].wx[cx] * rec[e].wy[cy];
                         const float wp = w * (rec[e].sf.x + bxy);
@@ -567,17 +544,27 @@ __global__ void __launch_bounds__(kAThr, 2)
             __syncthreads();  // the records, segmentation and E of this buffer are free
             ++seq;
         }
-        // the mirrored list is done: H += sg conj(X(-k)) / 2 (this thread stored H above)
-        if (KY < P && KX <= P / 2) {
+        // ---- the adjoint only needs Re IFFT2(X) = C2R of the Hermitian part
+        // H(k) = (X(k) + conj X(-k)) / 2 on the half plane kx <= n: each cell adds
+        // X(k)/2 to H(k) and conj(X(k))/2 to H(-k) where they lie in the half
+        // plane (at most two adds per H cell, onto zeros: the sum does not depend
+        // on their order); the pre-IFFT fftshift sign is applied here ----
+        const int KY = tyi * kT + cy, KX = txi * kT + cx;
+        if (KY < P && KX < P) {
+            const int half = P / 2, hp = g.hpitch;
+            const long long img_half = (long long)P * hp;
             const float sg = ((KX + KY) & 1) ? -0.5f : 0.5f;
-            float2 *dst = hcell();
-            const long long img_half = (long long)P * g.hpitch;
+            const bool here = KX <= half, mirror = KX >= half || KX == 0;
+            const long long o1 = (long long)KY * hp + KX;
+            const long long o2 = (long long)((P - KY) % P) * hp + (P - KX) % P;
+            float2 *dst = spec + ((long long)z * g.m + jbase) * img_half;
 #pragma unroll
             for (int j = 0; j < 16; ++j) {
                 if (jbase + j >= g.m) break;
+                const float2 v = make_float2(sg * acc[2 * j], sg * acc[2 * j + 1]);
                 float2 *d = dst + (long long)j * img_half;
-                const float2 h = *d;
-                *d = make_float2(h.x + sg * acc[2 * j], h.y - sg * acc[2 * j + 1]);
+                if (here) atomicAdd(d + o1, v);
+                if (mirror) atomicAdd(d + o2, make_float2(v.x, -v.y));
             }
         }
     }
@@ -587,12 +574,10 @@ __global__ void __launch_bounds__(kAThr, 2)
 // ---------------------------------------------------------------------------
 // Geometry records of the direction path's adjoint entries: those of
 // k_adj_records (scatter_tc.cu) for the direction's representative
-// positions -- for a mirrored list (item.w = 1) the weights at the negated
-// cells -k of the tile's cells k -- and in sf the first-order weight: at tile
-// cell (cx, cy) the distance to the position along x is ax + s cx/(2n) (and
-// likewise y; s = 1, or -1 for a mirrored list), so cos dw/dx w_y - sin w_x
-// dw/dy = w (A + s B . (cx, cy)) with A = c1 (cos ax - sin ay), B = c1/(2n)
-// (cos, -sin), c1 = 2 (pi^2/mu)/(2n); sf = (A, s).
+// positions, and in sf.x the constant A of the first-order weight: at tile
+// cell (cx, cy) the distance to the position along x is cx/(2n) + ax (and
+// likewise y), so cos dw/dx w_y - sin w_x dw/dy = w (A + B . (cx, cy)) with
+// A = c1 (cos ax - sin ay), B = c1/(2n) (cos, -sin), c1 = 2 (pi^2/mu)/(2n).
 // One block per work item, one thread per entry.
 // ---------------------------------------------------------------------------
 __global__ void k_adj_records_dir(AdjRec *__restrict__ recs, const uint32_t *__restrict__ pts,
@@ -609,12 +594,8 @@ __global__ void k_adj_records_dir(AdjRec *__restrict__ recs, const uint32_t *__r
         float x0, y0;
         int fx, fy;
         sample_pos(q, sc, g, x0, y0, fx, fy);
-        // tap index of tile column c: c - dx for the tile's own cells, dx - c
-        // for the negated cells -k of a mirrored list (k in the tile)
-        const bool mir = it.w != 0;
-        const int sg = mir ? -1 : 1;
-        int dx = mir ? P - txi * kT - (g.n + fx - kR) : g.n + fx - kR - txi * kT;
-        int dy = mir ? P - tyi * kT - (g.n + fy - kR) : g.n + fy - kR - tyi * kT;
+        int dx = g.n + fx - kR - txi * kT;
+        int dy = g.n + fy - kR - tyi * kT;
         dx += (dx < -half) ? P : 0;
         dx -= (dx > half) ? P : 0;
         dy += (dy < -half) ? P : 0;
@@ -623,7 +604,7 @@ __global__ void k_adj_records_dir(AdjRec *__restrict__ recs, const uint32_t *__r
         int rows = 0, cols = 0;
 #pragma unroll
         for (int c = 0; c < kT; ++c) {
-            const int bx = mir ? dx - c : c - dx, by = mir ? dy - c : c - dy;
+            const int bx = c - dx, by = c - dy;
             const bool inx = (unsigned)bx < (unsigned)kTaps, iny = (unsigned)by < (unsigned)kTaps;
             r.wx[c] = inx ? tap_weight(fx, bx, x0, g) : 0.f;
             r.wy[c] = iny ? tap_weight(fy, by, y0, g) : 0.f;
@@ -639,9 +620,8 @@ __global__ void k_adj_records_dir(AdjRec *__restrict__ recs, const uint32_t *__r
             if (((rows >> (4 * (w >> 1))) & 0xf) && ((cols >> (8 * (w & 1))) & 0xff)) mask |= 3 << (2 * w);
         r.thm = (d << 16) | mask;
         r.k = q;
-        // distance of tile cell c to the position along x: ax + sg c / (2n)
-        const float ax = (float)(fx - kR - sg * dx) * g.inv2n - x0, ay = (float)(fy - kR - sg * dy) * g.inv2n - y0;
-        r.sf = make_float2(c1 * (sc.y * ax - sc.x * ay), (float)sg);
+        const float ax = (float)(fx - kR - dx) * g.inv2n - x0, ay = (float)(fy - kR - dy) * g.inv2n - y0;
+        r.sf = make_float2(c1 * (sc.y * ax - sc.x * ay), 0.f);
         recs[(long long)it.y + e] = r;
     }
 }
@@ -678,13 +658,15 @@ void launch_scatter_dir(const float2 *rowsc, float2 *spec, int zb, const GeoDev 
                         cudaStream_t s) {
     if (g.T != kT) throw Error(1, "tile size must be 16");
     if (!gd.adj_recs || !gd.adj_tabs || !gd.adj_info || !gd.demix) throw Error(1, "adjoint direction tables missing");
-    const long long nunits = (long long)zb * (gd.n_adj_items / 2);  // every tile of the half plane
+    const long long nunits = (long long)zb * gd.n_adj_busy;
     if (nunits == 0) return;
     if (nunits > 2147483647LL) throw Error(1, "adjoint grid too large");
     if (zb > gd.demix_slices) throw Error(1, "adjoint direction mixing buffer too small");
     const dim3 gm(gd.ndir, zb, (g.n + kMThr - 1) / kMThr);
+    // the first group of time samples also clears the half planes of all of them
+    const long long nzero = jbase == 0 ? (long long)zb * g.m * g.P * g.hpitch / 2 : 0;
     k_adj_mix<<<gm, kMThr, 0, s>>>(gd.demix, rowsc, gd.dray_start, gd.drays, gd.dtau, gd.kmat, gd.shiftadj, g, gd.ndir,
-                                   jbase);
+                                   jbase, reinterpret_cast<float4 *>(spec), nzero);
     LAUNCH_CHECK("k_adj_mix");
     static int nsm = 0;
     if (nsm == 0) {

@@ -593,10 +593,7 @@ struct Handle {
             // batch of them (scatter_tc_batch_rays()) and at most cap entries;
             // on the direction path whole directions, at most dir_adj_table_dirs()
             const int max_rays = dirs ? dir_adj_table_dirs() : scatter_tc_batch_rays();
-            // (the direction path: every list, empty ones included -- its units are
-            // the half plane's tiles, each with a pair of lists)
-            const int nlists = dirs ? gd.n_adj_items : gd.n_adj_busy;
-            for (int i = 0; i < nlists; ++i) {
+            for (int i = 0; i < gd.n_adj_busy; ++i) {
                 const int4 it = hp.adj_items[i];
                 const uint32_t *pts = hp.adj_pts.data() + it.y;
                 int c0 = 0;
@@ -732,7 +729,7 @@ struct Handle {
             // Re IFFT2 of the scattered grids as a C2R of their Hermitian part,
             // which the tensor-core scatter adds into zeroed half planes
             const long long img_half = (long long)ug.P * ug.hpitch;
-            // (the direction path stores every half-plane cell: no clearing)
+            // (the direction path clears them inside k_adj_mix)
             if (!gd.dirs) CUDA_CHECK(cudaMemsetAsync(spec, 0, sizeof(float2) * (size_t)nimg * img_half, stream));
             launch_scatter_adj(rowsc, spec, zb, gd, ug, stream);
             if (pad_fft) {

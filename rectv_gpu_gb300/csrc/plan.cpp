@@ -263,34 +263,18 @@ bool build_dir_plan(const float *theta, int n, int ntheta, int T, int fwd_cap, d
     if ((double)ntheta < min_group * dp.ndir || dp.ndir >= 65536) return false;
 
     // positions (d, q), 1 <= q < n: the same float sequence as the kernels
-    // (sample_pos), binned by the tile of the stencil origin (forward) and,
-    // for the tiles of the half plane kx <= n (adjoint), by every such tile
-    // the stencil touches (it adds to X(k)) and every such tile its negated
-    // stencil touches (it adds to X(-k)); direction-major inside a tile
+    // (sample_pos), binned by the tile of the stencil origin (forward) and by
+    // every tile the stencil touches (adjoint), direction-major inside a tile
     const int P = 2 * n;
     const int NT = (P + T - 1) / T;
     const int ntiles = NT * NT;
-    const int NTH = std::min(NT, n / T + 1);  // tile columns holding half-plane cells
     const float tn = (float)(2 * n);
     std::vector<float> qk(n);
     for (int k = 1; k < n; ++k) qk[k] = (float)(k - n / 2) / (float)n;
     const long long npos = (long long)dp.ndir * (n - 1);
-    const int nhalf = NT * NTH;  // adjoint lists: 2 per half-plane tile (direct, mirrored)
     std::vector<int> ftile(npos);
-    std::vector<int4> atiles(npos), mtiles(npos);
-    std::vector<long long> fcnt(ntiles + 1, 0), acnt(2 * nhalf + 1, 0);
-    // tiles (half plane only) of the 9x9 box starting at (KX - kR, KY - kR), modulo P
-    auto box_tiles = [&](int KX, int KY) {
-        const int xa = wrapi(KX - kR, P) / T, xb = wrapi(KX + kR, P) / T;
-        const int ya = wrapi(KY - kR, P) / T, yb = wrapi(KY + kR, P) / T;
-        const int nx = (xa == xb) ? 1 : 2, ny = (ya == yb) ? 1 : 2;
-        const int xs[2] = {xa, xb}, ys[2] = {ya, yb};
-        int tl[4] = {-1, -1, -1, -1}, nt = 0;
-        for (int a = 0; a < ny; ++a)
-            for (int b = 0; b < nx; ++b)
-                if (xs[b] < NTH) tl[nt++] = ys[a] * NTH + xs[b];
-        return make_int4(tl[0], tl[1], tl[2], tl[3]);
-    };
+    std::vector<int4> atiles(npos);
+    std::vector<long long> fcnt(ntiles + 1, 0), acnt(ntiles + 1, 0);
     long long ip = 0;
     for (int d = 0; d < dp.ndir; ++d) {
         const float s = dp.sincos[d].x, c = dp.sincos[d].y;
@@ -298,25 +282,27 @@ bool build_dir_plan(const float *theta, int n, int ntheta, int T, int fwd_cap, d
             float x0 = qk[q] * s, y0 = qk[q] * c;
             if (x0 >= 0.5f) x0 = 0.5f - 1e-5f;
             if (y0 >= 0.5f) y0 = 0.5f - 1e-5f;
-            const int fx = (int)std::floor(tn * x0), fy = (int)std::floor(tn * y0);
-            const int KX = n + fx, KY = n + fy;
+            const int KX = n + (int)std::floor(tn * x0), KY = n + (int)std::floor(tn * y0);
             ftile[ip] = (KY / T) * NT + (KX / T);
             fcnt[ftile[ip]]++;
-            // stencil cells n + f - 4 .. n + f + 4; negated (k -> -k, i.e.
-            // K -> P - K): n - f - 4 .. n - f + 4
-            atiles[ip] = box_tiles(KX, KY);
-            mtiles[ip] = box_tiles(n - fx, n - fy);
-            for (const int t : {atiles[ip].x, atiles[ip].y, atiles[ip].z, atiles[ip].w})
-                if (t >= 0) acnt[2 * t]++;
-            for (const int t : {mtiles[ip].x, mtiles[ip].y, mtiles[ip].z, mtiles[ip].w})
-                if (t >= 0) acnt[2 * t + 1]++;
+            const int xa = wrapi(KX - kR, P) / T, xb = wrapi(KX + kR, P) / T;
+            const int ya = wrapi(KY - kR, P) / T, yb = wrapi(KY + kR, P) / T;
+            const int nx = (xa == xb) ? 1 : 2, ny = (ya == yb) ? 1 : 2;
+            const int xs[2] = {xa, xb}, ys[2] = {ya, yb};
+            int tl[4] = {-1, -1, -1, -1}, nt = 0;
+            for (int a = 0; a < ny; ++a)
+                for (int b = 0; b < nx; ++b) tl[nt++] = ys[a] * NT + xs[b];
+            atiles[ip] = make_int4(tl[0], tl[1], tl[2], tl[3]);
+            for (int i = 0; i < nt; ++i) acnt[tl[i]]++;
         }
     }
-    std::vector<long long> foff(ntiles + 1, 0), aoff(2 * nhalf + 1, 0);
-    for (int t = 0; t < ntiles; ++t) foff[t + 1] = foff[t] + fcnt[t];
-    for (int l = 0; l < 2 * nhalf; ++l) aoff[l + 1] = aoff[l] + acnt[l];
+    std::vector<long long> foff(ntiles + 1, 0), aoff(ntiles + 1, 0);
+    for (int t = 0; t < ntiles; ++t) {
+        foff[t + 1] = foff[t] + fcnt[t];
+        aoff[t + 1] = aoff[t] + acnt[t];
+    }
     dp.fwd_pos.resize(foff[ntiles]);
-    dp.adj_pos.resize(aoff[2 * nhalf]);
+    dp.adj_pos.resize(aoff[ntiles]);
     {
         std::vector<long long> fp(foff.begin(), foff.end() - 1), ap(aoff.begin(), aoff.end() - 1);
         ip = 0;
@@ -324,26 +310,19 @@ bool build_dir_plan(const float *theta, int n, int ntheta, int T, int fwd_cap, d
             for (int q = 1; q < n; ++q, ++ip) {
                 const uint32_t id = (uint32_t)d * (uint32_t)n + (uint32_t)q;
                 dp.fwd_pos[fp[ftile[ip]]++] = id;
-                for (const int t : {atiles[ip].x, atiles[ip].y, atiles[ip].z, atiles[ip].w})
-                    if (t >= 0) dp.adj_pos[ap[2 * t]++] = id;
-                for (const int t : {mtiles[ip].x, mtiles[ip].y, mtiles[ip].z, mtiles[ip].w})
-                    if (t >= 0) dp.adj_pos[ap[2 * t + 1]++] = id;
+                const int4 a = atiles[ip];
+                const int tl[4] = {a.x, a.y, a.z, a.w};
+                for (int i = 0; i < 4; ++i)
+                    if (tl[i] >= 0) dp.adj_pos[ap[tl[i]]++] = id;
             }
     }
     for (int t = 0; t < ntiles; ++t)
         for (long long i = foff[t]; i < foff[t + 1]; i += fwd_cap)
             dp.fwd_items.push_back(make_int4(t, (int)i, (int)std::min<long long>(fwd_cap, foff[t + 1] - i), 0));
-    // adjoint lists in pairs (direct, mirrored) per half-plane tile, the
-    // tile index in the full grid's numbering; heaviest pairs first
-    std::vector<int> pord(nhalf);
-    for (int t = 0; t < nhalf; ++t) pord[t] = t;
-    std::stable_sort(pord.begin(), pord.end(),
-                     [&](int a, int b) { return acnt[2 * a] + acnt[2 * a + 1] > acnt[2 * b] + acnt[2 * b + 1]; });
-    for (const int t : pord) {
-        const int tile = (t / NTH) * NT + (t % NTH);
-        dp.adj_items.push_back(make_int4(tile, (int)aoff[2 * t], (int)acnt[2 * t], 0));
-        dp.adj_items.push_back(make_int4(tile, (int)aoff[2 * t + 1], (int)acnt[2 * t + 1], 1));
-    }
+    for (int t = 0; t < ntiles; ++t) dp.adj_items.push_back(make_int4(t, (int)aoff[t], (int)acnt[t], 0));
+    // heaviest tiles first (the empty ones last)
+    std::stable_sort(dp.adj_items.begin(), dp.adj_items.end(),
+                     [](const int4 &a, const int4 &b) { return a.z > b.z; });
     return true;
 }
 

@@ -154,11 +154,8 @@ struct DirPlan {
                                     // grid cells per unit of (q - n/2)/n
     std::vector<uint32_t> fwd_pos;  // positions d*n + q (1 <= q < n) sorted by the tile of the stencil origin
     std::vector<int4> fwd_items;    // (tile, start, count, 0): at most fwd_cap positions of one tile
-    std::vector<uint32_t> adj_pos;  // adjoint entries (positions) of the lists below
-    std::vector<int4> adj_items;    // per tile of the half plane kx <= n, heaviest first, a pair of lists
-                                    // (tile, start, count, 0): positions whose stencil touches the tile
-                                    // (they add to X(k), k in the tile) and (tile, start, count, 1):
-                                    // positions whose negated stencil touches it (they add to X(-k))
+    std::vector<uint32_t> adj_pos;  // one entry per tile a position's stencil touches
+    std::vector<int4> adj_items;    // (tile, start, count, 0), one per tile, busiest first
 };
 // Groups rays whose sample positions agree within tol_cells grid cells.
 // Returns false (plan unused) when the rays average fewer than min_group per
