@@ -213,23 +213,6 @@ __global__ void __launch_bounds__(kFThr, 2)
         }
         __syncthreads();
 
-        // the next slice's footprint rows into L2 (three 128-byte lines cover a
-        // 24-cell row), so that its loads after the barrier hit L2
-        if (z + 1 < z1) {
-            const float2 *snext = spec + ((long long)(z + 1) * g.m + jbase) * g.img_fwd;
-            for (int r = tid; r < 16 * kFW; r += kFThr) {
-                const int j = r / kFW, row = r - j * kFW;
-                if (jbase + j >= g.m) continue;
-                const int KY = KY0 + row;
-                const int xlo = (mirrored ? g.P - (KX0 + kFW - 1) : KX0) + kHalo;
-                const char *p0 = reinterpret_cast<const char *>(snext + (long long)j * g.img_fwd +
-                                                                (long long)((mirrored ? g.P - KY : KY) + kHalo) * g.qp +
-                                                                xlo);
-                asm volatile("prefetch.global.L2 [%0];\n" ::"l"(p0));
-                asm volatile("prefetch.global.L2 [%0];\n" ::"l"(p0 + 128));
-                asm volatile("prefetch.global.L2 [%0];\n" ::"l"(p0 + 8 * kFW - 8));
-            }
-        }
         for (int gi = wid; gi < ngroups; gi += kFThr / 32) {
             const int e = 4 * gi + pi;
             const int id = sm.pid[e];
