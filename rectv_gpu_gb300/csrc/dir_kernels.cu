@@ -218,10 +218,11 @@ __global__ void __launch_bounds__(kFThr, 2)
             const int id = sm.pid[e];
             const int org = sm.org[e];
             const int lx0 = org % kFW;
-            const float4 *fb = sm.fp + org * kChunks;
-            int so[4];
+            // four base pointers (one per rotation of the column's chunks): every
+            // tap is then a load at a constant offset from one of them
+            const float4 *fq[4];
 #pragma unroll
-            for (int bq = 0; bq < 4; ++bq) so[bq] = (ci + 2 * ((lx0 + bq) & 3)) & 7;
+            for (int bq = 0; bq < 4; ++bq) fq[bq] = sm.fp + org * kChunks + ((ci + 2 * ((lx0 + bq) & 3)) & 7);
             const float *wt = sm.wt[e];
             float wx[kTaps], wxd[kTaps];
 #pragma unroll
@@ -238,7 +239,7 @@ __global__ void __launch_bounds__(kFThr, 2)
                 float2 d0 = make_float2(0.f, 0.f), d1 = make_float2(0.f, 0.f);
 #pragma unroll
                 for (int b = 0; b < kTaps; ++b) {
-                    const float4 f = fb[(a * kFW + b) * kChunks + so[b & 3]];
+                    const float4 f = fq[b & 3][(a * kFW + b) * kChunks];
                     r0 = ffma2(make_float2(wx[b], wx[b]), make_float2(f.x, f.y), r0);
                     r1 = ffma2(make_float2(wx[b], wx[b]), make_float2(f.z, f.w), r1);
                     d0 = ffma2(make_float2(wxd[b], wxd[b]), make_float2(f.x, f.y), d0);
