@@ -76,6 +76,8 @@ CASES = [
     (40, 60, 8, 2, 2, -1.0, "fourier"),     # 2n not a multiple of 16
     (48, 90, 16, 2, 8, 0.0, "fourier"),     # two rays per direction (RECTV_DIRS=1)
     (256, 720, 16, 1, 8, 0.0, "fourier"),   # hand-written padded-grid FFT size
+    (64, 512, 16, 2, 32, 0.5, "random"),    # 32 rays per direction: four mixing rounds
+    (64, 240, 16, 2, 12, 0.0, "fourier"),   # 12 rays per direction: a partial mixing round
 ]
 
 
