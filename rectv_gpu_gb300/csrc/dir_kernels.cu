@@ -72,11 +72,11 @@ struct FwdSmem {
 };
 
 // ---- adjoint ----
-constexpr int kAThr = kT * kT;         // one thread per cell of a tile, one slice per block
-constexpr int kAWarps = kAThr / 32;    // warp w: cells of rows 4 (w >> 1) .. + 3, columns 8 (w & 1) .. + 7
+constexpr int kAThr = 256;             // two threads per cell of a tile (8 time samples each), one slice per block
+constexpr int kABlk = 16;              // 4x4-cell blocks of a tile: block b = rows 4 (b >> 2) .. + 3, columns 4 (b & 3) .. + 3
 constexpr int kATab = 128;             // entries per table (host table builder)
 constexpr int kAMaxSeg = 16;           // directions per table (host table builder)
-constexpr int kAInfo = adj_info_words(kAMaxSeg);
+constexpr int kAInfo = dir_adj_info_words(kAMaxSeg);
 constexpr int kMThr = 256;             // positions per k_adj_mix block
 constexpr int kMRays = 32;             // rays per staged chunk of k_adj_mix
 constexpr int kMFly = 4;               // row loads in flight per thread of k_adj_mix
@@ -85,6 +85,7 @@ struct AdjSmem {
     AdjRec rec[2][kATab];                  // geometry records of this table and the next
     uint32_t info[2][kAInfo];              // their direction segmentation
     float4 e[2][kATab][2 * kChunks];       // [buffer][entry]: E_j in [0, 8), E_perp_j in [8, 16)
+    int4 meta[2];                          // (tile, slice, entries or -1: none, last table of its unit)
 };
 
 __device__ __forceinline__ uint32_t saddr(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
@@ -432,154 +433,215 @@ __global__ void __launch_bounds__(kMThr, 2)
 // ---------------------------------------------------------------------------
 // Adjoint, step 2: persistent blocks of 256 threads, two per SM, take (tile,
 // slice) units round-robin (slices fastest, so that blocks in flight share
-// their tiles' records in L2), one thread per cell of the 16x16 tile and a
-// warp per 4x8-cell block (a 9x9 stencil touches fewer of these than of
-// 2x16-cell rows).  A tile's entries (positions whose stencil touches it,
-// direction-major) come in tables of at most 128 entries and 16 directions,
-// with the geometry records of the per-ray scatter (x and y weight rows over
-// the tile, k_adj_records_dir) and the entries of each direction that touch
-// each warp's block (k_adj_tabinfo); a table's records, segmentation and the
-// E, E_perp of its entries are copied (cp.async) while the table before it is
-// processed.  Per table every cell adds w E_j + w_perp E_perp_j of the entries
-// touching its block into its 16 time samples (FP32, entry order:
-// reproducible).  The unit's sums go into the Hermitian half planes of the
-// C2R inverse as in k_scatter_tc.
+// their tiles' records in L2).  The 16x16 tile is cut into sixteen 4x4-cell
+// blocks; a warp owns blocks w and 15 - w, its lane (h, cell) the cell of
+// each block and the time samples [8h, 8h + 8).  A 9x9 stencil covers 56 %
+// of the cells of the 4x4 blocks it touches (42 % of 4x8 blocks, 34 % of
+// 2x16 rows), and two lanes per cell halve the E loads and packed FMAs a
+// lane issues per entry.  A tile's entries (positions whose stencil touches
+// it, direction-major) come in tables of at most 128 entries and 16
+// directions, with the geometry records of the per-ray scatter (x and y
+// weight rows over the tile, k_adj_records_dir) and per direction and block
+// the entries that touch the block (k_adj_tabinfo_dir); a table's records,
+// segmentation and the E, E_perp of its entries are copied (cp.async) while
+// the table before it is processed.  Per table every cell adds
+// w E_j + w_perp E_perp_j of the entries touching its block (FP32, entry
+// order: reproducible).  The unit's sums go into the Hermitian half planes
+// of the C2R inverse as in k_scatter_tc.
 // ---------------------------------------------------------------------------
+namespace {
+
+// acc += sum over entries [e0, e1) of w E + w_perp E_perp for time samples
+// [8h, 8h + 8) of cell (cx, cy); Eh = the entries' E with the lane's offset
+__device__ __forceinline__ void dir_cell_sums(float (&acc)[16], const AdjRec *__restrict__ rec,
+                                              const float4 *__restrict__ Eh, int e0, int e1, int cx, int cy,
+                                              float bxy) {
+#pragma unroll 2
+    for (int e = e0; e < e1; ++e) {
+        const float w = rec[e].wx[cx] * rec[e].wy[cy];
+        const float wp = w * (rec[e].sf.x + bxy);
+        const float4 *E = Eh + e * (2 * kChunks);
+        const float2 ww = make_float2(w, w), pp = make_float2(wp, wp);
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+            const float4 f = E[i], fp = E[kChunks + i];
+            float2 a0 = ffma2(ww, make_float2(f.x, f.y), make_float2(acc[4 * i], acc[4 * i + 1]));
+            float2 a1 = ffma2(ww, make_float2(f.z, f.w), make_float2(acc[4 * i + 2], acc[4 * i + 3]));
+            a0 = ffma2(pp, make_float2(fp.x, fp.y), a0);
+            a1 = ffma2(pp, make_float2(fp.z, fp.w), a1);
+            acc[4 * i] = a0.x;
+            acc[4 * i + 1] = a0.y;
+            acc[4 * i + 2] = a1.x;
+            acc[4 * i + 3] = a1.y;
+        }
+    }
+}
+
+// the Hermitian half-plane adds of one cell's sums (time samples [jb, jb + 8))
+__device__ __forceinline__ void dir_cell_store(float2 *__restrict__ spec, const float (&acc)[16], int KX, int KY,
+                                               const UsGeo &g, int z, int jb) {
+    const int P = g.P;
+    if (KY >= P || KX >= P) return;
+    const int half = P / 2, hp = g.hpitch;
+    const long long img_half = (long long)P * hp;
+    const float sg = ((KX + KY) & 1) ? -0.5f : 0.5f;
+    const bool here = KX <= half, mirror = KX >= half || KX == 0;
+    const long long o1 = (long long)KY * hp + KX;
+    const long long o2 = (long long)((P - KY) % P) * hp + (P - KX) % P;
+    float2 *dst = spec + ((long long)z * g.m + jb) * img_half;
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+        if (jb + j >= g.m) break;
+        const float2 v = make_float2(sg * acc[2 * j], sg * acc[2 * j + 1]);
+        float2 *d = dst + (long long)j * img_half;
+        if (here) atomicAdd(d + o1, v);
+        if (mirror) atomicAdd(d + o2, make_float2(v.x, -v.y));
+    }
+}
+
+}  // namespace
+
 __global__ void __launch_bounds__(kAThr, 2)
     k_scatter_dir(const float4 *__restrict__ emix, float2 *__restrict__ spec, const AdjRec *__restrict__ recs,
                   const uint32_t *__restrict__ pts, const int4 *__restrict__ items, const int4 *__restrict__ tabs,
-                  const int *__restrict__ tab_base, const uint32_t *__restrict__ info,
-                  const float2 *__restrict__ dsincos, UsGeo g, int ndir, int zb, int nunits, int jbase) {
+                  const int *__restrict__ tab_base, const uint32_t *__restrict__ info, UsGeo g, int ndir, int zb,
+                  int nunits, int jbase) {
     extern __shared__ __align__(16) unsigned char dir_adj_smem[];
     AdjSmem &sm = *reinterpret_cast<AdjSmem *>(dir_adj_smem);
-    const int P = g.P;
     const int tid = threadIdx.x, wid = tid >> 5, lane = tid & 31;
-    // this thread's cell: warp block wid (4 rows x 8 columns), lane = (row, column) in it
-    const int cx = 8 * (wid & 1) + (lane & 7), cy = 4 * (wid >> 1) + (lane >> 3);
-    const float cb = 2.f * g.wexp / g.tn * g.inv2n;  // c1/(2n): B = cb (cos, -sin)
+    // this thread's cells: (rx, ry) of blocks b0 = wid and b1 = 15 - wid, time samples [8h, 8h + 8)
+    const int h = lane >> 4, rx = lane & 3, ry = (lane >> 2) & 3;
+    const int b0 = wid, b1 = kABlk - 1 - wid;
+    const int cx0 = 4 * (b0 & 3) + rx, cy0 = 4 * (b0 >> 2) + ry;
+    const int cx1 = 4 * (b1 & 3) + rx, cy1 = 4 * (b1 >> 2) + ry;
 
-    // copy cursor: the next table (unit, table of the unit) in consumption order
-    int fu = blockIdx.x, ft = 0;
-    auto fetch = [&](int slot) {
+    // Copy cursor: the tables in consumption order (units u = blockIdx.x,
+    // + gridDim.x, ...; the tables of a unit in order).  The descriptor of the
+    // table to copy next and the table range and tile of the unit after the
+    // cursor's are loaded one step ahead, and a table's E, E_perp copies are
+    // issued after the sums of the table before it, so that no load latency
+    // sits in front of a copy.
+    const int pe = tid >> 1, pc0 = (tid & 1) * 8;  // entry and half of its 16 chunks this thread copies
+    int fu = blockIdx.x, fti = 0, ftb1 = 0, ftile = 0, ntb0 = 0, ntb1 = 0, ntile = 0;
+    int4 fdesc = make_int4(0, 0, 0, 0);  // (first entry, count, word offset, words)
+    int pz = 0, pcnt = 0;                // the E copy still to issue: slice, entries
+    uint32_t ppid = 0;                   // and this thread's position d*n + q
+    if (fu < nunits) {
+        const int item = fu / zb;
+        fti = __ldg(tab_base + item);
+        ftb1 = __ldg(tab_base + item + 1);
+        ftile = __ldg(items + item).x;
+        fdesc = __ldg(tabs + fti);
+    }
+    if (fu + (int)gridDim.x < nunits) {
+        const int item = (fu + (int)gridDim.x) / zb;
+        ntb0 = __ldg(tab_base + item);
+        ntb1 = __ldg(tab_base + item + 1);
+        ntile = __ldg(items + item).x;
+    }
+    // records, segmentation and the table's (tile, slice, entries, last of its
+    // unit) into slot; entries -1: no table left
+    auto fetch_a = [&](int slot) {
         if (fu < nunits) {
-            const int item = fu / zb, zf = fu % zb;
-            const int tb0 = __ldg(tab_base + item), tb1 = __ldg(tab_base + item + 1);
-            const int4 tb = __ldg(tabs + tb0 + ft);  // (first entry, count, word offset, words)
-            const int cnt = min(tb.y, kATab), nw = min(tb.w, kAInfo);
-            const char *rs = reinterpret_cast<const char *>(recs + tb.x);
+            const int cnt = min(fdesc.y, kATab), nw = min(fdesc.w, kAInfo);
+            const char *rs = reinterpret_cast<const char *>(recs + fdesc.x);
             char *rd = reinterpret_cast<char *>(sm.rec[slot]);
             constexpr int kRecChunks = (int)(sizeof(AdjRec) / 16);
             for (int c = tid; c < cnt * kRecChunks; c += kAThr) cp_async16(rd + 16 * c, rs + 16 * c);
-            const char *is = reinterpret_cast<const char *>(info + tb.z);
+            const char *is = reinterpret_cast<const char *>(info + fdesc.z);
             char *id = reinterpret_cast<char *>(sm.info[slot]);
             for (int c = tid; c < nw / 4; c += kAThr) cp_async16(id + 16 * c, is + 16 * c);
-            // E, E_perp of entry e: thread = (e, half of the 16 chunks)
-            {
-                const int e = tid >> 1, c0 = (tid & 1) * 8;
-                if (e < cnt) {
-                    const uint32_t pid = __ldg(pts + tb.x + e);  // d*n + q
-                    const float4 *src = emix + ((long long)zf * ndir * g.n + pid) * 16 + c0;
-                    float4 *dst = &sm.e[slot][e][c0];
-#pragma unroll
-                    for (int c = 0; c < 8; ++c) cp_async16(dst + c, src + c);
+            pz = fu % zb;
+            pcnt = cnt;
+            ppid = pe < cnt ? __ldg(pts + fdesc.x + pe) : 0u;
+            if (tid == 0) sm.meta[slot] = make_int4(ftile, pz, cnt, fti + 1 >= ftb1 ? 1 : 0);
+            if (++fti >= ftb1) {  // the next unit: its range and tile were loaded one unit ago
+                fu += gridDim.x;
+                fti = ntb0;
+                ftb1 = ntb1;
+                ftile = ntile;
+                const int nu = fu + (int)gridDim.x;
+                if (nu < nunits) {
+                    const int item = nu / zb;
+                    ntb0 = __ldg(tab_base + item);
+                    ntb1 = __ldg(tab_base + item + 1);
+                    ntile = __ldg(items + item).x;
                 }
             }
-            if (++ft >= tb1 - tb0) {
-                ft = 0;
-                fu += gridDim.x;
-            }
+            if (fu < nunits) fdesc = __ldg(tabs + fti);
+        } else {
+            pcnt = 0;
+            if (tid == 0) sm.meta[slot] = make_int4(0, 0, -1, 0);
         }
         cp_commit();
     };
-    fetch(0);
-    int seq = 0;  // tables consumed: buffer seq & 1
-
-    for (int u = blockIdx.x; u < nunits; u += gridDim.x) {
-        const int item = u / zb, z = u % zb;
-        const int4 it = __ldg(items + item);
-        const int tyi = it.x / g.NT, txi = it.x - tyi * g.NT;
-        float acc[32];  // F of this cell: 16 time samples x (re, im)
+    // E, E_perp of the table fetch_a last took (its position ids have arrived by now)
+    auto fetch_b = [&](int slot) {
+        if (pe < pcnt) {
+            const float4 *src = emix + ((long long)pz * ndir * g.n + ppid) * 16 + pc0;
+            float4 *dst = &sm.e[slot][pe][pc0];
 #pragma unroll
-        for (int i = 0; i < 32; ++i) acc[i] = 0.f;
-        const int tb0 = __ldg(tab_base + item), tb1 = __ldg(tab_base + item + 1);
-        for (int ti = tb0; ti < tb1; ++ti) {
-            const int buf = seq & 1;
-            fetch(buf ^ 1);  // the next table: that buffer was released by the last barrier
-            cp_wait<1>();    // this table's copies (issued one table earlier)
-            __syncthreads();
-            const int cnt = min(__ldg(tabs + ti).y, kATab);
-            const AdjRec *rec = sm.rec[buf];
-            const uint32_t *inf = sm.info[buf];
-            const int nseg = min(min((int)inf[0], cnt), kAMaxSeg);
-            {
-                const uint16_t *segf = reinterpret_cast<const uint16_t *>(inf + 4 + 8 * nseg);  // direction starts
-                for (int s = 0; s < nseg; ++s) {
-                    const uint32_t lohi = inf[4 + 8 * s + wid];
-                    const int e1 = min((int)(lohi >> 16), cnt);
-                    const int e0 = (int)(lohi & 0xffffu);
-                    if (e0 >= e1) continue;
-                    // first-order weight w (A_p + B . (cx, cy)), B across the direction
-                    const float2 sc = __ldg(dsincos + ((unsigned)rec[min((int)segf[s], cnt - 1)].thm >> 16));
-                    const float bxy = cb * (sc.y * (float)cx - sc.x * (float)cy);
-                    for (int e = e0; e < e1; ++e) {
-                        const float w = rec[e].wx[cx] * rec[e].wy[cy];
-                        const float wp = w * (rec[e].sf.x + bxy);
-                        const float4 *E = sm.e[buf][e];
-                        const float2 ww = make_float2(w, w), pp = make_float2(wp, wp);
-#pragma unroll
-                        for (int i = 0; i < kChunks; ++i) {
-                            const float4 f = E[i], fp = E[kChunks + i];
-                            float2 a0 = ffma2(ww, make_float2(f.x, f.y), make_float2(acc[4 * i], acc[4 * i + 1]));
-                            float2 a1 =
-                                ffma2(ww, make_float2(f.z, f.w), make_float2(acc[4 * i + 2], acc[4 * i + 3]));
-                            a0 = ffma2(pp, make_float2(fp.x, fp.y), a0);
-                            a1 = ffma2(pp, make_float2(fp.z, fp.w), a1);
-                            acc[4 * i] = a0.x;
-                            acc[4 * i + 1] = a0.y;
-                            acc[4 * i + 2] = a1.x;
-                            acc[4 * i + 3] = a1.y;
-                        }
-                    }
-                }
-            }
-            __syncthreads();  // the records, segmentation and E of this buffer are free
-            ++seq;
+            for (int c = 0; c < 8; ++c) cp_async16(dst + c, src + c);
         }
-        // ---- the adjoint only needs Re IFFT2(X) = C2R of the Hermitian part
-        // H(k) = (X(k) + conj X(-k)) / 2 on the half plane kx <= n: each cell adds
-        // X(k)/2 to H(k) and conj(X(k))/2 to H(-k) where they lie in the half
-        // plane (at most two adds per H cell, onto zeros: the sum does not depend
-        // on their order); the pre-IFFT fftshift sign is applied here ----
-        const int KY = tyi * kT + cy, KX = txi * kT + cx;
-        if (KY < P && KX < P) {
-            const int half = P / 2, hp = g.hpitch;
-            const long long img_half = (long long)P * hp;
-            const float sg = ((KX + KY) & 1) ? -0.5f : 0.5f;
-            const bool here = KX <= half, mirror = KX >= half || KX == 0;
-            const long long o1 = (long long)KY * hp + KX;
-            const long long o2 = (long long)((P - KY) % P) * hp + (P - KX) % P;
-            float2 *dst = spec + ((long long)z * g.m + jbase) * img_half;
+        cp_commit();
+    };
+
+    float acc0[16], acc1[16];  // F of the two cells: 8 time samples x (re, im)
 #pragma unroll
-            for (int j = 0; j < 16; ++j) {
-                if (jbase + j >= g.m) break;
-                const float2 v = make_float2(sg * acc[2 * j], sg * acc[2 * j + 1]);
-                float2 *d = dst + (long long)j * img_half;
-                if (here) atomicAdd(d + o1, v);
-                if (mirror) atomicAdd(d + o2, make_float2(v.x, -v.y));
-            }
+    for (int i = 0; i < 16; ++i) acc0[i] = acc1[i] = 0.f;
+    fetch_a(0);
+    fetch_b(0);
+    for (int buf = 0;; buf ^= 1) {
+        fetch_a(buf ^ 1);  // the next table: that buffer was released by the last barrier
+        cp_wait<1>();      // everything but that group: this table's copies
+        __syncthreads();
+        const int4 mt = sm.meta[buf];  // (tile, slice, entries, last table of the unit)
+        if (mt.z < 0) break;
+        const int cnt = mt.z;
+        const AdjRec *rec = sm.rec[buf];
+        const uint32_t *inf = sm.info[buf];
+        const float4 *Eh = &sm.e[buf][0][4 * h];
+        const int nseg = min(min((int)inf[0], cnt), kAMaxSeg);
+        const uint16_t *segf = reinterpret_cast<const uint16_t *>(inf + 4 + kABlk * nseg);  // direction starts
+        for (int s = 0; s < nseg; ++s) {
+            const uint32_t lh0 = inf[4 + kABlk * s + b0], lh1 = inf[4 + kABlk * s + b1];
+            const int e00 = (int)(lh0 & 0xffffu), e01 = min((int)(lh0 >> 16), cnt);
+            const int e10 = (int)(lh1 & 0xffffu), e11 = min((int)(lh1 >> 16), cnt);
+            if (e00 >= e01 && e10 >= e11) continue;
+            // first-order weight w (A_p + B . (cx, cy)): B of the direction from its first record
+            const AdjRec &r0 = rec[min((int)segf[s], cnt - 1)];
+            const float bx = r0.sf.y, by = __int_as_float(r0.k);
+            dir_cell_sums(acc0, rec, Eh, e00, e01, cx0, cy0, bx * (float)cx0 + by * (float)cy0);
+            dir_cell_sums(acc1, rec, Eh, e10, e11, cx1, cy1, bx * (float)cx1 + by * (float)cy1);
+        }
+        fetch_b(buf ^ 1);
+        __syncthreads();  // the records, segmentation and E of this buffer are free
+        if (mt.w) {
+            // ---- the adjoint only needs Re IFFT2(X) = C2R of the Hermitian part
+            // H(k) = (X(k) + conj X(-k)) / 2 on the half plane kx <= n: each cell adds
+            // X(k)/2 to H(k) and conj(X(k))/2 to H(-k) where they lie in the half
+            // plane (at most two adds per H cell, onto zeros: the sum does not depend
+            // on their order); the pre-IFFT fftshift sign is applied here ----
+            const int tyi = mt.x / g.NT, txi = mt.x - tyi * g.NT;
+            dir_cell_store(spec, acc0, txi * kT + cx0, tyi * kT + cy0, g, mt.y, jbase + 8 * h);
+            dir_cell_store(spec, acc1, txi * kT + cx1, tyi * kT + cy1, g, mt.y, jbase + 8 * h);
+#pragma unroll
+            for (int i = 0; i < 16; ++i) acc0[i] = acc1[i] = 0.f;
         }
     }
-    cp_wait<0>();  // the cursor's last (empty) group
+    cp_wait<0>();  // the cursor's last (empty) groups
 }
 
 // ---------------------------------------------------------------------------
 // Geometry records of the direction path's adjoint entries: those of
 // k_adj_records (scatter_tc.cu) for the direction's representative
-// positions, and in sf.x the constant A of the first-order weight: at tile
-// cell (cx, cy) the distance to the position along x is cx/(2n) + ax (and
-// likewise y), so cos dw/dx w_y - sin w_x dw/dy = w (A + B . (cx, cy)) with
-// A = c1 (cos ax - sin ay), B = c1/(2n) (cos, -sin), c1 = 2 (pi^2/mu)/(2n).
-// One block per work item, one thread per entry.
+// positions, with the first-order weight's constants in place of the
+// per-ray fields: at tile cell (cx, cy) the distance to the position along x
+// is cx/(2n) + ax (and likewise y), so cos dw/dx w_y - sin w_x dw/dy =
+// w (A + B . (cx, cy)) with A = c1 (cos ax - sin ay) in sf.x and
+// B = c1/(2n) (cos, -sin) in sf.y and k (float bits), c1 = 2 (pi^2/mu)/(2n).
+// thm holds the direction and the 4x4-cell blocks of the tile the stencil
+// touches.  One block per work item, one thread per entry.
 // ---------------------------------------------------------------------------
 __global__ void k_adj_records_dir(AdjRec *__restrict__ recs, const uint32_t *__restrict__ pts,
                                   const int4 *__restrict__ items, const float2 *__restrict__ dsincos, UsGeo g) {
@@ -612,17 +674,17 @@ __global__ void k_adj_records_dir(AdjRec *__restrict__ recs, const uint32_t *__r
             rows |= iny ? (1 << c) : 0;
             cols |= inx ? (1 << c) : 0;
         }
-        // warp blocks of k_scatter_dir the stencil touches (block w: rows
-        // 4 (w >> 1) .. + 3, columns 8 (w & 1) .. + 7), as bits 2w and 2w + 1: the
-        // form of a row mask k_adj_tabinfo segments by
+        // 4x4-cell blocks of k_scatter_dir the stencil touches (block b: rows
+        // 4 (b >> 2) .. + 3, columns 4 (b & 3) .. + 3) as bit b
         int mask = 0;
 #pragma unroll
-        for (int w = 0; w < kAWarps; ++w)
-            if (((rows >> (4 * (w >> 1))) & 0xf) && ((cols >> (8 * (w & 1))) & 0xff)) mask |= 3 << (2 * w);
+        for (int b = 0; b < kABlk; ++b)
+            if (((rows >> (4 * (b >> 2))) & 0xf) && ((cols >> (4 * (b & 3))) & 0xf)) mask |= 1 << b;
         r.thm = (d << 16) | mask;
-        r.k = q;
         const float ax = (float)(fx - kR - dx) * g.inv2n - x0, ay = (float)(fy - kR - dy) * g.inv2n - y0;
-        r.sf = make_float2(c1 * (sc.y * ax - sc.x * ay), 0.f);
+        const float cb = c1 * g.inv2n;
+        r.sf = make_float2(c1 * (sc.y * ax - sc.x * ay), cb * sc.y);
+        r.k = __float_as_int(-cb * sc.x);
         recs[(long long)it.y + e] = r;
     }
 }
@@ -631,6 +693,92 @@ void launch_adj_records_dir(AdjRec *recs, const GeoDev &gd, const UsGeo &g, cuda
     if (gd.n_adj_items == 0) return;
     k_adj_records_dir<<<gd.n_adj_items, 256, 0, s>>>(recs, gd.adj_pts, gd.adj_items, gd.sincos, g);
     LAUNCH_CHECK("k_adj_records_dir");
+}
+
+// ---------------------------------------------------------------------------
+// Segmentation of every direction-path adjoint table (geometry only, so
+// computed once), in the layout of dir_adj_info_words: the directions (runs
+// of equal thm >> 16, records are direction-major), their first rows, and per
+// direction and 4x4-cell block the rows [lo, hi) from the first to the last
+// entry whose stencil touches the block (found at the entries where a
+// touching run starts or ends; rows in between that miss the block have
+// zero weights there).  One block per table, one thread per entry.
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(kATab)
+    k_adj_tabinfo_dir(const AdjRec *__restrict__ recs, const int4 *__restrict__ tabs, uint32_t *__restrict__ info) {
+    __shared__ int seg_first[kAMaxSeg + 1];
+    __shared__ int rlo[kABlk][kAMaxSeg], rhi[kABlk][kAMaxSeg];
+    __shared__ int wsum[kATab / 32];
+    const int4 tb = tabs[blockIdx.x];  // (first entry, count, word offset, words)
+    const int ct = threadIdx.x, lane = ct & 31, w = ct >> 5, cnt = min(tb.y, kATab);
+    int thm = 0, thp = 0, thn = 0;
+    if (ct < cnt) {
+        thm = recs[(long long)tb.x + ct].thm;
+        if (ct > 0) thp = recs[(long long)tb.x + ct - 1].thm;
+        if (ct + 1 < cnt) thn = recs[(long long)tb.x + ct + 1].thm;
+    }
+    const unsigned d = (unsigned)thm >> 16;
+    const int flag = (ct < cnt && (ct == 0 || ((unsigned)thp >> 16) != d)) ? 1 : 0;
+    int incl = flag;  // inclusive scan of the direction starts
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const int y = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += y;
+    }
+    if (lane == 31) wsum[w] = incl;
+    for (int i = ct; i < kABlk * kAMaxSeg; i += kATab) {
+        rlo[i / kAMaxSeg][i % kAMaxSeg] = kATab;
+        rhi[i / kAMaxSeg][i % kAMaxSeg] = 0;
+    }
+    __syncthreads();
+    int base = 0, nseg = 0;
+#pragma unroll
+    for (int i = 0; i < kATab / 32; ++i) {
+        base += (i < w) ? wsum[i] : 0;
+        nseg += wsum[i];
+    }
+    nseg = min(nseg, kAMaxSeg);  // the host's tables hold at most kAMaxSeg directions
+    const int seg = incl + base - 1;
+    if (ct < cnt && flag && seg < kAMaxSeg) seg_first[seg] = ct;
+    if (ct == 0) seg_first[nseg] = cnt;
+    __syncthreads();
+    if (ct < cnt && seg < kAMaxSeg) {
+        const int msk = thm & 0xffff;
+        const int mprev = flag ? 0 : (thp & 0xffff);
+        const bool last = ct + 1 == cnt || ((unsigned)thn >> 16) != d;
+        const int mnext = last ? 0 : (thn & 0xffff);
+#pragma unroll
+        for (int b = 0; b < kABlk; ++b) {
+            const int bit = 1 << b;
+            if (msk & bit) {
+                if (!(mprev & bit)) atomicMin(&rlo[b][seg], ct);
+                if (!(mnext & bit)) atomicMax(&rhi[b][seg], ct + 1);
+            }
+        }
+    }
+    __syncthreads();
+    uint32_t *out = info + tb.z;
+    const int nw = min(dir_adj_info_words(nseg), tb.w);  // the host sized the slot from the same directions
+    for (int i = ct; i < nw; i += kATab) {
+        uint32_t v = 0;
+        if (i == 0) {
+            v = (uint32_t)nseg;
+        } else if (i >= 4 && i < 4 + kABlk * nseg) {
+            const int sg = (i - 4) / kABlk, b = (i - 4) % kABlk;
+            v = (uint32_t)rlo[b][sg] | ((uint32_t)rhi[b][sg] << 16);
+        } else if (i >= 4 + kABlk * nseg) {
+            const int j = 2 * (i - 4 - kABlk * nseg);  // 16-bit direction starts j, j+1
+            if (j <= nseg) v = (uint32_t)seg_first[j];
+            if (j + 1 <= nseg) v |= (uint32_t)seg_first[j + 1] << 16;
+        }
+        out[i] = v;
+    }
+}
+
+void launch_adj_tabinfo_dir(const GeoDev &gd, cudaStream_t s) {
+    if (gd.n_adj_tabs == 0) return;
+    k_adj_tabinfo_dir<<<gd.n_adj_tabs, kATab, 0, s>>>(gd.adj_recs, gd.adj_tabs, gd.adj_info);
+    LAUNCH_CHECK("k_adj_tabinfo_dir");
 }
 
 void dir_prepare() {
@@ -677,8 +825,8 @@ void launch_scatter_dir(const float2 *rowsc, float2 *spec, int zb, const GeoDev 
     }
     const int grid = (int)std::min<long long>(nunits, g.sc_grid > 0 ? g.sc_grid : 2 * nsm);
     k_scatter_dir<<<grid, kAThr, sizeof(AdjSmem), s>>>(gd.demix, spec, gd.adj_recs, gd.adj_pts, gd.adj_items,
-                                                       gd.adj_tabs, gd.adj_tab_base, gd.adj_info, gd.sincos, g,
-                                                       gd.ndir, zb, (int)nunits, jbase);
+                                                       gd.adj_tabs, gd.adj_tab_base, gd.adj_info, g, gd.ndir, zb,
+                                                       (int)nunits, jbase);
     LAUNCH_CHECK("k_scatter_dir");
 }
 

@@ -607,7 +607,7 @@ struct Handle {
                         c1 = r;
                         ++nseg;
                     }
-                    const int w = scatter_tc_info_words(nseg);
+                    const int w = dirs ? dir_adj_info_words(nseg) : scatter_tc_info_words(nseg);
                     tabs.push_back(make_int4(it.y + c0, c1 - c0, (int)words, w));
                     words += w;
                     if (words > 2147483647LL) throw Error(RECTV_ERR_ARG, "rectv: adjoint plan too large");
@@ -669,11 +669,13 @@ struct Handle {
         }
         gd.deapod = (float *)up(dp.data(), n * sizeof(float));
         if (gd.tc_scatter) {
-            if (gd.dirs)
+            if (gd.dirs) {
                 launch_adj_records_dir(gd.adj_recs, gd, ug, stream);
-            else
+                launch_adj_tabinfo_dir(gd, stream);
+            } else {
                 launch_adj_records(gd.adj_recs, gd, ug, stream);
-            launch_adj_tabinfo(gd, stream);
+                launch_adj_tabinfo(gd, stream);
+            }
         }
         CUDA_CHECK(cudaStreamSynchronize(stream));  // host vectors go out of scope
         geo_theta.assign(theta_h, theta_h + ntheta);

@@ -168,6 +168,12 @@ bool build_dir_plan(const float *theta, int n, int ntheta, int T, int fwd_cap, d
 // 2w+1 of the tile (lo | hi << 16), then the first row of every ray and the
 // table size as 16-bit values; padded to 16 bytes.
 __host__ __device__ constexpr int adj_info_words(int nseg) { return (4 + 8 * nseg + (nseg + 2) / 2 + 3) & ~3; }
+// The direction path's form: [4 + 16 s + b] the rows [lo, hi) of direction s
+// whose stencils touch 4x4-cell block b of the tile (rows 4 (b >> 2) .. + 3,
+// columns 4 (b & 3) .. + 3).
+__host__ __device__ constexpr int dir_adj_info_words(int nseg) {
+    return (4 + 16 * nseg + (nseg + 2) / 2 + 3) & ~3;
+}
 
 // ---- USFFT kernel launchers (usfft_kernels.cu) ----
 void launch_deapod_pad(const float *u, float *spec, int nimg, const float *deapod, const UsGeo &g,
@@ -217,10 +223,12 @@ void launch_gather_dir(float2 *rows, const float2 *spec, int zb, const GeoDev &g
 void launch_scatter_dir(const float2 *rowsc, float2 *spec, int zb, const GeoDev &gd, const UsGeo &g, int jbase,
                         cudaStream_t s);
 // geometry records of the direction path's adjoint entries (as
-// launch_adj_records, with sf = (A, 0): the first-order weight of entry p at
-// tile cell (cx, cy) is w (A + B . (cx, cy)), B = c1/(2n) (cos, -sin) of the
-// direction, c1 = 2 pi^2/mu / (2n))
+// launch_adj_records, with sf = (A, Bx), k = float bits of By: the first-order
+// weight of entry p at tile cell (cx, cy) is w (A + B . (cx, cy)),
+// B = c1/(2n) (cos, -sin) of the direction, c1 = 2 pi^2/mu / (2n))
 void launch_adj_records_dir(AdjRec *recs, const GeoDev &gd, const UsGeo &g, cudaStream_t s);
+// their segmentation (dir_adj_info_words per table)
+void launch_adj_tabinfo_dir(const GeoDev &gd, cudaStream_t s);
 void dir_prepare();           // kernel attributes; once, outside stream capture
 int dir_fwd_capacity();       // positions per forward item
 int dir_adj_table_capacity(); // entries per adjoint table
