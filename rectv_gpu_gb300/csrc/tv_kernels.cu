@@ -24,6 +24,10 @@ namespace {
 
 __device__ __forceinline__ int clampi(int a, int lo, int hi) { return a < lo ? lo : (a > hi ? hi : a); }
 
+__device__ __forceinline__ void prefetch_l2(const void *p) {
+    asm volatile("prefetch.global.L2 [%0];\n" ::"l"(p));
+}
+
 template <int NW>
 __device__ __forceinline__ void block_reduce3(double a, double b, double c, double *out) {
     __shared__ double sh[3][NW];
@@ -147,8 +151,20 @@ __global__ void __launch_bounds__(256, MODE == 2 ? 4 : 3)  // MODE 2 loads less:
         hmt = rho * (sgt * (f0 - f0) - p0) + m0;
         if constexpr (MODE == 1) w[2 * cs + q0 - st] = m0 - rho * p0;
     }
+    const float *wpf = w + q0 + 3 * st;  // MODE 2: w of time point tt + 3
     for (int tt = 0; tt < m; ++tt) {
         float nxt[21];
+        if constexpr (MODE == 2) {
+            // the dual lines only this thread's column brings from HBM (its own
+            // w, 16 of the 20 new bytes per voxel; the neighbours' are other
+            // threads' own), into L2 two time points before load() asks for
+            // them: registers hold only one point ahead
+            if (tt + 3 < m) {
+#pragma unroll
+                for (int i = 0; i < 4; ++i) prefetch_l2(wpf + i * cs);
+            }
+            wpf += st;
+        }
         if (tt + 1 < m) load(tt + 1, nxt);
         if constexpr (MODE == 1) {  // w at q, and at the lower boundary planes this voxel reads
             const long long q = q0 + (long long)tt * st;
