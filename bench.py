@@ -444,8 +444,9 @@ def batched_form(torch, device, count=32, iters=8, seed=4):
         "runs": runs,
         "results_equal_one_at_a_time": same,
         "autotune": {"shapes": tuned, "seconds": tune_s,
-                     "note": "(gather slices per block, scatter persistent blocks; 0 = one per SM) per "
-                             "NxNthetaxMxNz, timed in isolation before the runs"},
+                     "note": "(gather slices per block, scatter persistent blocks; 0 = the default: two per SM "
+                             "on the direction path, one per SM on the per-ray path) per NxNthetaxMxNz, timed in "
+                             "isolation before the runs"},
         "shapes": [[j["n"], j["nz"], j["ntheta"], j["m"]] for j in jobs],
     }, jobs
 
@@ -708,12 +709,13 @@ def run_ours(args, rank, world, local_rank):
     peak, peak_kind = measured_peaks()
     achieved = bytes_.value / (ktimes[dom] * 1e-3) / 1e9
     limiter = {
-        "k_adj_mix+k_scatter_dir": "k_scatter_dir (93% of the pair): per-cell FP32 sums of w E + w_perp E_perp over "
-                                   "the entries covering each warp's two tile rows -- shared-memory broadcast loads "
-                                   "of E (L1/shared pipe ~73% busy) and the FMA pipe (~38%), two 8-warp blocks per SM "
-                                   "at 124 registers; float2 atomics into the Hermitian half planes; DRAM ~15% of "
-                                   "peak, so not DRAM-bound",
-        "k_gather_dir": "latency of the footprint loads and block barriers (two 8-warp blocks per SM at 124 "
+        "k_adj_mix+k_scatter_dir": "k_scatter_dir (~90% of the pair): per-cell FP32 sums of w E + w_perp E_perp "
+                                   "over the entries touching each 4x4-cell block (two lanes per cell) -- latency of "
+                                   "the shared-memory loads of E and of the packed-FMA chains with 16 warps per SM "
+                                   "(two 8-warp blocks at 128 registers; issue ~54% active, L1/shared ~73% busy, FMA "
+                                   "pipe ~38%); float2 atomics into the Hermitian half planes; DRAM ~20% of peak, so "
+                                   "not DRAM-bound",
+        "k_gather_dir": "latency of the footprint loads and block barriers (two 8-warp blocks per SM at 121 "
                         "registers, ~30 positions per tile and slice) and shared-memory bandwidth of the 81-tap "
                         "reads (L1/shared pipe ~70% busy); DRAM ~14% of peak",
         "k_scatter_tc": "block barriers and the per-cell ray sums on the CUDA cores (shared-memory loads), "
@@ -821,7 +823,8 @@ def run_ours(args, rank, world, local_rank):
         "rho_final": float(hist["rho"][-1]) if len(hist["rho"]) else None,
         "rel_err_vs_fp64": acc,
         "per_ray_path": per_ray,
-        "autotune": {"gather_slices_per_block": tuned[0], "scatter_blocks": tuned[1] or "one per SM",
+        "autotune": {"gather_slices_per_block": tuned[0],
+                     "scatter_blocks": tuned[1] or ("two per SM" if ndir > 0 else "one per SM"),
                      "seconds": t_tune},
         "result_finite": finite,
     }
