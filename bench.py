@@ -778,6 +778,11 @@ def run_ours(args, rank, world, local_rank):
     ph_h = torch.from_numpy(phi).pin_memory()
     f_h = torch.empty((nz, m, n, n), dtype=torch.float32, pin_memory=True)
     del d_g
+    # untimed warm-up call with the same arguments: the timed call then finds
+    # the geometry, plans and captured graphs in place (as every call after a
+    # user's first does; the first call is timed separately below)
+    obj.run(f_h.data_ptr(), g_h.data_ptr(), th_h.data_ptr(), ph_h.data_ptr(), center, lam0, lam1,
+            max(1, min(args.warmup, 3)), titer)
     if dist:
         dist.barrier()
     t0 = time.perf_counter()
