@@ -160,6 +160,19 @@ int rectv_get_launch_counts(rectv_handle *h, int *kernels, int *fft_execs, int *
  * (default 2e-3). */
 int rectv_get_directions(rectv_handle *h, int *ndir, int *nrays);
 
+/* The same choice for a geometry before any handle exists, on the host alone
+ * (no GPU): *ndir = number of directions whose rays would share sample
+ * positions, 0 when the rays average fewer than min_group per direction
+ * (the per-ray kernels then run); *max_rays = the most rays grouped into one
+ * direction.  tol_cells <= 0 and min_group <= 0 take the defaults of geometry
+ * set-up (2e-3 grid cells, 2.5 rays); the environment switches are not read,
+ * and a handle also needs the tensor-core adjoint (M >= 8) for the path.
+ * Measured angles with a calibration factor (a scan that does not return to
+ * its angles after each half-turn) are not grouped.  No reference
+ * counterpart. */
+int rectv_plan_directions(const float *theta, int n, int ntheta, double tol_cells, double min_group, int *ndir,
+                          int *max_rays);
+
 /* Self-test of the bounded waits of the tensor-core and TMA kernels: queues
  * on the handle's stream one block that waits on an mbarrier nothing arrives
  * on, first for limit_cycles SM cycles, then nwait - 1 more times with the

@@ -6,9 +6,9 @@ include/rectv_gb300.h); importing the classes does not require a GPU, creating
 a solver does.
 """
 
-from .rectv import rectv
+from .rectv import plan_directions, rectv
 from .solver import Solver, getp, takephi
 from . import phantom
 
-__all__ = ["rectv", "Solver", "getp", "takephi", "phantom"]
+__all__ = ["rectv", "plan_directions", "Solver", "getp", "takephi", "phantom"]
 __version__ = "1.0.0"

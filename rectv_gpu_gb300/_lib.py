@@ -43,6 +43,7 @@ SIGNATURES = {
     "rectv_kernel_cost": (_I, [_P, _I, _P, _P]),
     "rectv_get_launch_counts": (_I, [_P, _IP, _IP, _IP]),
     "rectv_get_directions": (_I, [_P, _IP, _IP]),
+    "rectv_plan_directions": (_I, [_P, _I, _I, _D, _D, _IP, _IP]),
     "rectv_selftest_wait": (_I, [_P, ctypes.c_longlong, _I]),
     "rectv_autotune": (_I, [_P, _I, _IP, _IP]),
     "rectv_measure_fp32_peak": (_I, [_P, _P]),

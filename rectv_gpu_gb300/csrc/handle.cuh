@@ -511,7 +511,7 @@ struct Handle {
         // 2.5 per direction (RECTV_DIRS=1: whenever it can run, RECTV_DIRS=0:
         // never) and the adjoint fills Hermitian half planes; rays are grouped
         // when their samples agree within RECTV_DIR_TOL grid cells (2e-3).
-        double dir_min = 2.5, dir_tol = 2e-3;
+        double dir_min = kDirMinGroup, dir_tol = kDirTolCells;
         if (const char *e = std::getenv("RECTV_DIRS")) {
             if (!std::strcmp(e, "0")) dir_min = -1.0;
             if (!std::strcmp(e, "1")) dir_min = 1.0;

@@ -466,6 +466,22 @@ int rectv_get_directions(rectv_handle *h, int *ndir, int *nrays) {
     });
 }
 
+int rectv_plan_directions(const float *theta, int n, int ntheta, double tol_cells, double min_group, int *ndir,
+                          int *max_rays) {
+    return rectv::guarded([&] {
+        if (!theta) throw rectv::Error(RECTV_ERR_ARG, "rectv_plan_directions: null pointer");
+        if (n < 2 || ntheta < 1) throw rectv::Error(RECTV_ERR_ARG, "rectv_plan_directions: bad sizes");
+        rectv::DirPlan dp;
+        const bool used = rectv::build_dir_plan(theta, n, ntheta, 16, rectv::dir_fwd_capacity(),
+                                                tol_cells > 0 ? tol_cells : rectv::kDirTolCells,
+                                                min_group > 0 ? min_group : rectv::kDirMinGroup, dp);
+        int mr = 0;
+        for (size_t d = 0; d + 1 < dp.ray_start.size(); ++d) mr = std::max(mr, dp.ray_start[d + 1] - dp.ray_start[d]);
+        if (ndir) *ndir = used ? dp.ndir : 0;
+        if (max_rays) *max_rays = mr;
+    });
+}
+
 }  // extern "C"
 
 // ===========================================================================

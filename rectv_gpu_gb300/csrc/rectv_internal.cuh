@@ -157,6 +157,11 @@ struct DirPlan {
     std::vector<uint32_t> adj_pos;  // one entry per tile a position's stencil touches
     std::vector<int4> adj_items;    // (tile, start, count, 0), one per tile, busiest first
 };
+// Defaults of the direction path: rays are grouped when their samples agree
+// within kDirTolCells grid cells, and the path is taken when the rays average
+// at least kDirMinGroup per direction.
+constexpr double kDirTolCells = 2e-3;
+constexpr double kDirMinGroup = 2.5;
 // Groups rays whose sample positions agree within tol_cells grid cells.
 // Returns false (plan unused) when the rays average fewer than min_group per
 // direction or there are 65536 directions or more.

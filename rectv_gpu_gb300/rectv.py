@@ -182,3 +182,17 @@ def estimate_bytes(n, ntheta, m, nz, nzp):
     b = ctypes.c_double()
     _lib.check(_lib.load().rectv_estimate_bytes(int(n), int(ntheta), int(m), int(nz), int(nzp), ctypes.byref(b)))
     return b.value
+
+
+def plan_directions(theta, n, tol_cells=0.0, min_group=0.0):
+    """(directions, most rays in one direction) of a geometry, on the host.
+
+    directions is the number of ray directions (theta modulo pi) whose rays
+    would share sample positions, 0 when the geometry keeps the per-ray
+    kernels; the defaults (0) are those of geometry set-up: 2e-3 grid cells,
+    2.5 rays per direction.  No GPU is needed."""
+    th = np.ascontiguousarray(theta, dtype=np.float32)
+    nd, mr = ctypes.c_int(), ctypes.c_int()
+    _lib.check(_lib.load().rectv_plan_directions(th.ctypes.data, int(n), int(th.size), float(tol_cells),
+                                                 float(min_group), ctypes.byref(nd), ctypes.byref(mr)))
+    return nd.value, mr.value

@@ -80,6 +80,32 @@ def test_estimate_bytes_is_host_arithmetic(lib_built):
         estimate_bytes(64, 128, 8, 4, 8)  # nzp > nz
 
 
+def test_direction_grouping_is_host_logic(lib_built):
+    """Which USFFT path a geometry takes (build_dir_plan, no GPU): scans that
+    return to their angles every half-turn share sample positions; the
+    reference test's angles and calibrated measured angles keep the per-ray
+    kernels."""
+    import numpy as np
+    from rectv_gpu_gb300 import _lib, plan_directions
+    from rectv_gpu_gb300.phantom import scan_angles
+    # 2880 angles over 8 half-turns (the foam example's linspace without the end point)
+    assert plan_directions(scan_angles(2880, 8), 1024) == (360, 8)
+    assert plan_directions(scan_angles(1440, 8), 512) == (180, 8)
+    # the reference test's angles (tests/test_adjoint.py: linspace with the end point)
+    assert plan_directions(np.linspace(0, 8 * np.pi, 2400).astype(np.float32), 504)[0] == 0
+    # measured angles scaled by a calibration factor (examples/tao/tao.py: 0.9977)
+    th = (np.linspace(0, 16 * np.pi, 1440, endpoint=False) * 0.9977).astype(np.float32)
+    assert plan_directions(th, 1024) == (0, 1)
+    # two rays per direction: below the default 2.5, taken with min_group = 1
+    assert plan_directions(scan_angles(90, 2), 64) == (0, 2)
+    assert plan_directions(scan_angles(90, 2), 64, min_group=1.0) == (45, 2)
+    # theta and theta + pi are one direction (opposite orientation)
+    th = np.array([0.3, 0.3 + np.pi, 0.3 + 2 * np.pi, 1.1, 1.1 + np.pi, 1.1 + 3 * np.pi], np.float32)
+    assert plan_directions(th, 256) == (2, 3)
+    with pytest.raises(_lib.RectvError):
+        plan_directions(th, 1)
+
+
 def test_engine_without_gpu_reports_an_error(lib_built):
     torch = pytest.importorskip("torch")
     if torch.cuda.is_available():
