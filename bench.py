@@ -135,7 +135,7 @@ class ClockSampler:
         except Exception:
             self.proc.kill()
         self.out.close()
-        sm, mx, reasons = [], [], set()
+        sm, mx, pw, reasons = [], [], [], set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
         with open(self.path) as f:
             for line in f:
@@ -147,14 +147,18 @@ class ClockSampler:
                     mx.append(float(p[2].split()[0]))
                 except ValueError:
                     continue
+                try:
+                    pw.append(float(p[3].split()[0]))
+                except ValueError:
+                    pass
                 for nm, v in zip(names, p[5:9]):
                     if v.lower().startswith("active"):
                         reasons.add(nm)
         os.unlink(self.path)
         if not sm:
             return None
-        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
-                "samples": len(sm)}
+        return {"sm_mhz": statistics.median(sm), "sm_min_mhz": min(sm), "sm_max_mhz": max(mx),
+                "power_w": statistics.median(pw) if pw else None, "reasons": sorted(reasons), "samples": len(sm)}
 
 
 # ---------------------------------------------------------------------------
@@ -785,10 +789,19 @@ def run_ours(args, rank, world, local_rank):
             max(1, min(args.warmup, 3)), titer)
     if dist:
         dist.barrier()
+    e2e_sampler = ClockSampler(local_rank)
+    e2e_sampler.start()
+    ea = torch.cuda.Event(enable_timing=True)
+    eb = torch.cuda.Event(enable_timing=True)
+    ea.record(stream)
     t0 = time.perf_counter()
     obj.run(f_h.data_ptr(), g_h.data_ptr(), th_h.data_ptr(), ph_h.data_ptr(), center, lam0, lam1, args.steps,
             titer)
     t1 = time.perf_counter()
+    eb.record(stream)
+    torch.cuda.synchronize()
+    e2e_clocks = e2e_sampler.stop()
+    e2e_gpu_s = ea.elapsed_time(eb) * 1e-3  # the call's span on the library's stream (copies and kernels)
     e2e_s = max_over_ranks(t1 - t0, dist, dev)
     h2d = g_h.numel() * 4 + th_h.numel() * 4 + ph_h.numel() * 4
     d2h = f_h.numel() * 4
@@ -819,7 +832,8 @@ def run_ours(args, rank, world, local_rank):
                    "parallelism": "replicas" if world > 1 else "single"},
         "voxel_updates_per_s": value * voxels,
         "e2e": {"value": whole_job_rate(args.steps, world, e2e_s * 1e3), "unit": "iter/s", "h2d_bytes_per_step": h2d / args.steps,
-                "d2h_bytes_per_step": d2h / args.steps, "seconds": e2e_s, "api": "rectv_run (C ABI)"},
+                "d2h_bytes_per_step": d2h / args.steps, "seconds": e2e_s, "stream_seconds": e2e_gpu_s,
+                "api": "rectv_run (C ABI)", "clocks": e2e_clocks},
         "roofline": roofline,
         "cpu_baseline": cpu,
         "clocks": clocks,
