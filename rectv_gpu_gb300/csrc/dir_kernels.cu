@@ -809,7 +809,7 @@ void launch_scatter_dir(const float2 *rowsc, float2 *spec, int zb, const GeoDev 
     if (!gd.adj_recs || !gd.adj_tabs || !gd.adj_info || !gd.demix) throw Error(1, "adjoint direction tables missing");
     const long long nunits = (long long)zb * gd.n_adj_busy;
     if (nunits == 0) return;
-    if (nunits > 2147483647LL) throw Error(1, "adjoint grid too large");
+    if (nunits > 2147483647LL - 65536) throw Error(1, "adjoint grid too large");  // the cursor adds the grid size
     if (zb > gd.demix_slices) throw Error(1, "adjoint direction mixing buffer too small");
     const dim3 gm(gd.ndir, zb, (g.n + kMThr - 1) / kMThr);
     // the first group of time samples also clears the half planes of all of them
