@@ -442,9 +442,12 @@ __global__ void __launch_bounds__(kMThr, 2)
 // it, direction-major) come in tables of at most 128 entries and 16
 // directions, with the geometry records of the per-ray scatter (x and y
 // weight rows over the tile, k_adj_records_dir) and per direction and block
-// the entries that touch the block (k_adj_tabinfo_dir); a table's records,
-// segmentation and the E, E_perp of its entries are copied (cp.async) while
-// the table before it is processed.  Per table every cell adds
+// the entries that touch the block (k_adj_tabinfo_dir).  A copy cursor
+// brings each table in (cp.async) while the table before it is processed:
+// records and segmentation at its start, the entries' E, E_perp after its
+// sums (their position ids have arrived by then), and the table's (tile,
+// slice, entries) into shared memory beside them, so the sums wait on no
+// global load.  Per table every cell adds
 // w E_j + w_perp E_perp_j of the entries touching its block (FP32, entry
 // order: reproducible).  The unit's sums go into the Hermitian half planes
 // of the C2R inverse as in k_scatter_tc.
